@@ -1,0 +1,432 @@
+// gt_kernels.cuh -- device kernels of the Gturbo hot path (templated on the grid size N).
+//
+// Field layout (identical to the reference): spectral complex(8) z(N/2+1, N) == double2
+// z[N][NH] (NH = N/2+1, kx fastest); physical real(8) z(N+2, N) == double z[N][N+2].
+//
+// The nonlinear term nlt (src/nlt.f90) is three fused passes instead of the reference's
+// 5 cuFFT calls and 8 elementwise kernels:
+//   A  column pass, inverse y-FFT of q, u = i ky/|k|^a q and v = -i kx/|k|^a q
+//      (the multiplies of nlt.f90:22-36 fused into the load);
+//   B  row pass: C2R of q and of u+iv, the physical product (produ.f90:11-23), R2C of
+//      (u+iv)q, and the split into the two product spectra;
+//   C  column pass: forward y-FFT of both products, N = -i(kx A + ky B)/N^2 (nlt.f90:54-61,
+//      fft_dir.f90:17-21), the 2/3 mask (trunc.f90:10-25) and the Runge-Kutta stage update
+//      of rkstep.f90 fused into the store.
+// With truncate=1 the columns kx > kxlim hold no retained mode: pass C writes N=0 there
+// without transforming, and pass A skips any such column block whose input is entirely zero;
+// a device flag tells pass B whether the skipped columns are known to be zero.
+#pragma once
+
+#include "gt_fft.cuh"
+
+namespace gt {
+
+// Runge-Kutta epilogues of pass C (rkstep.f90). nh = the nonlinear term just computed.
+enum Epi : int {
+  EPI_NLT = 0,   // out = N                                              (nlt)
+  EPI_RK2A = 1,  // znl = e (z + dt/2 N), znl(1,1)=0                     (rkstep.f90:31-43)
+  EPI_RK2B = 2,  // z   = e (e z + dt N), z(1,1)=0                       (rkstep.f90:61-73)
+  EPI_RK4A = 3,  // znew = e e (z + dt/6 N); znl = e (z + dt/2 N)        (rkstep.f90:95-102)
+  EPI_RK4B = 4,  // znew += dt/3 e N; znl = e z + dt/2 N                 (rkstep.f90:104-111)
+  EPI_RK4C = 5,  // znew += dt/3 e N; znl = e (e z + dt N)               (rkstep.f90:113-120)
+  EPI_RK4D = 6,  // z = znew + dt/6 N, z(1,1)=0                          (rkstep.f90:122-128)
+};
+
+struct EpiArgs {
+  int mode;
+  int split;            // 1: e = emkx(i)*emky(j) (rkstep.f90:21-27, 51-57)
+  double2* out;         // N (EPI_NLT) / znl / z
+  double2* znew;
+  const double2* z;     // state read by the stage update
+  const double* emk;    // [N][NH]
+  const double* emkx;   // [NH]
+  const double* emky;   // [N]
+  double dt, dt2, dt3, dt6;
+};
+
+__device__ __forceinline__ void epilogue(const EpiArgs& E, int i, int j, int NH, double2 nh) {
+  const size_t o = (size_t)j * NH + i;
+  if (E.mode == EPI_NLT) {
+    E.out[o] = nh;
+    return;
+  }
+  const double e = E.split ? __ldg(&E.emkx[i]) * __ldg(&E.emky[j]) : __ldg(&E.emk[o]);
+  const bool origin = (i == 0 && j == 0);
+  switch (E.mode) {
+    case EPI_RK2A: {
+      const double2 z = E.z[o];
+      const double2 r = make_double2(e * (z.x + E.dt2 * nh.x), e * (z.y + E.dt2 * nh.y));
+      E.out[o] = origin ? make_double2(0.0, 0.0) : r;
+      break;
+    }
+    case EPI_RK2B: {
+      const double2 z = E.z[o];
+      const double2 r = make_double2(e * (e * z.x + E.dt * nh.x), e * (e * z.y + E.dt * nh.y));
+      E.out[o] = origin ? make_double2(0.0, 0.0) : r;
+      break;
+    }
+    case EPI_RK4A: {
+      const double2 z = E.z[o];
+      const double ee = e * e;
+      E.znew[o] = make_double2(ee * (z.x + E.dt6 * nh.x), ee * (z.y + E.dt6 * nh.y));
+      E.out[o] = make_double2(e * (z.x + E.dt2 * nh.x), e * (z.y + E.dt2 * nh.y));
+      break;
+    }
+    case EPI_RK4B: {
+      const double2 z = E.z[o];
+      const double2 w = E.znew[o];
+      const double d3 = E.dt3 * e;
+      E.znew[o] = make_double2(w.x + d3 * nh.x, w.y + d3 * nh.y);
+      E.out[o] = make_double2(e * z.x + E.dt2 * nh.x, e * z.y + E.dt2 * nh.y);
+      break;
+    }
+    case EPI_RK4C: {
+      const double2 z = E.z[o];
+      const double2 w = E.znew[o];
+      const double d3 = E.dt3 * e;
+      E.znew[o] = make_double2(w.x + d3 * nh.x, w.y + d3 * nh.y);
+      E.out[o] = make_double2(e * (e * z.x + E.dt * nh.x), e * (e * z.y + E.dt * nh.y));
+      break;
+    }
+    case EPI_RK4D: {
+      const double2 w = E.znew[o];
+      const double2 r = make_double2(w.x + E.dt6 * nh.x, w.y + E.dt6 * nh.y);
+      E.out[o] = origin ? make_double2(0.0, 0.0) : r;
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// Launch shapes. Column kernels: COLS columns per CTA (interleaved in shared memory so that a
+// warp's loads cover COLS*16 contiguous bytes of each row), T = N/16 threads per column.
+// Row kernels: ROWS rows per CTA, T threads per row.
+template <int N>
+struct Shape {
+  static constexpr int NH = N / 2 + 1;
+  static constexpr int T = N / 16;
+  static constexpr int COLS = (N >= 4096) ? 1 : (N == 2048) ? 2 : (128 / T > 16 ? 16 : 128 / T);
+  static constexpr int COL_THREADS = COLS * T;
+  static constexpr int COL_CTAS = (NH + COLS - 1) / COLS;
+  static constexpr size_t COL_SMEM = (size_t)padded(N) * COLS * sizeof(double2);
+  static constexpr int ROWS = (T >= 128) ? 1 : (128 / T > N ? N : 128 / T);
+  static constexpr int ROW_THREADS = ROWS * T;
+  static constexpr int ROW_CTAS = N / ROWS;
+  static constexpr size_t ROW_SMEM = (size_t)(padded(N) + padded(N / 2)) * ROWS * sizeof(double2);
+};
+
+__device__ __forceinline__ double2 czero() { return make_double2(0.0, 0.0); }
+
+// ---------------------------------------------------------------------------------------
+// Pass A: inverse y-transforms of u, v and q (in that order: zin may alias qo, as the
+// reference destroys z, so q is re-read from zin before the q column is overwritten).
+// ---------------------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::COL_THREADS)
+k_nlt_colinv(const double2* zin, double2* qo, double2* __restrict__ uo, double2* __restrict__ vo,
+             const double* __restrict__ kainv, const double* __restrict__ fkx,
+             const double* __restrict__ fky, const double2* __restrict__ tw, int kxlim, int* flag) {
+  using S = Shape<N>;
+  constexpr int T = S::T, C = S::COLS, NH = S::NH;
+  extern __shared__ double2 smem[];
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  const int i = blockIdx.x * C + c;
+  const bool valid = i < NH;
+  const int ic = valid ? i : NH - 1;
+  double2* sm = smem + c;
+  double2 v[16];
+#pragma unroll
+  for (int s = 0; s < 16; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
+  // A column beyond the 2/3 ellipse (i > kxlim) carries data only if the caller passed an
+  // untruncated field: then raise the flag so that pass B reads every column. A block made
+  // only of such columns is skipped when all of them are zero.
+  int nz = 0;
+  if (valid && i > kxlim) {
+#pragma unroll
+    for (int s = 0; s < 16; ++s) nz |= (v[s].x != 0.0) | (v[s].y != 0.0);
+  }
+  if (blockIdx.x * C > kxlim) {
+    if (!__syncthreads_or(nz)) return;
+  }
+  if (nz) atomicExch(flag, 1);
+  const double kx = __ldg(&fkx[ic]);
+  // u = i ky/|k|^a q  (nlt.f90:29-32)
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    const int j = t + s * T;
+    const double m = __ldg(&fky[j]) * __ldg(&kainv[(size_t)j * NH + ic]);
+    v[s] = make_double2(-m * v[s].y, m * v[s].x);
+  }
+  fft_regs<N, 16, true, C>(v, sm, t, tw, 0);
+  if (valid) {
+#pragma unroll
+    for (int s = 0; s < 16; ++s) uo[(size_t)(t + s * T) * NH + i] = v[s];
+  }
+  // v = -i kx/|k|^a q  (nlt.f90:33-34)
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    const int j = t + s * T;
+    const double2 q = valid ? zin[(size_t)j * NH + ic] : czero();
+    const double m = kx * __ldg(&kainv[(size_t)j * NH + ic]);
+    v[s] = make_double2(m * q.y, -m * q.x);
+  }
+  __syncthreads();
+  fft_regs<N, 16, true, C>(v, sm, t, tw, 0);
+  if (valid) {
+#pragma unroll
+    for (int s = 0; s < 16; ++s) vo[(size_t)(t + s * T) * NH + i] = v[s];
+  }
+  // q (nlt.f90:41)
+#pragma unroll
+  for (int s = 0; s < 16; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
+  __syncthreads();
+  fft_regs<N, 16, true, C>(v, sm, t, tw, 0);
+  if (valid) {
+#pragma unroll
+    for (int s = 0; s < 16; ++s) qo[(size_t)(t + s * T) * NH + i] = v[s];
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Pass B: per row y, C2R of q (half-length packing) and of u+iv (one complex transform of
+// length N), p = (u+iv) q, R2C of p, then A = P[k] + conj P[N-k] = 2 FFT(uq)[k] and
+// B = -i (P[k] - conj P[N-k]) = 2 FFT(vq)[k] written over U and V for k <= kout.
+// Inputs beyond column kin are taken as zero unless *flag says pass A wrote them.
+// ---------------------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::ROW_THREADS)
+k_nlt_row(const double2* __restrict__ qf, double2* uf, double2* vf, const double2* __restrict__ tw,
+          int kin, int kout, const int* __restrict__ flag) {
+  using S = Shape<N>;
+  constexpr int T = S::T, NH = S::NH, M = N / 2;
+  extern __shared__ double2 smem[];
+  const int r = threadIdx.x / T, t = threadIdx.x % T;
+  const int y = blockIdx.x * S::ROWS + r;
+  double2* cs = smem + (size_t)r * (padded(N) + padded(M));
+  double2* zs = cs + padded(N);
+  const int kl = (*flag) ? M : kin;
+  const double2* qrow = qf + (size_t)y * NH;
+  const double2* urow = uf + (size_t)y * NH;
+  const double2* vrow = vf + (size_t)y * NH;
+  // C[k] = U[k] + i V[k], C[N-k] = conj U[k] + i conj V[k]; Im of U, V at k=0, N/2 dropped
+#pragma unroll
+  for (int s = 0; s <= 8; ++s) {
+    const int k = t + s * T;
+    if (k <= M) {
+      const double2 U = (k <= kl) ? urow[k] : czero();
+      const double2 V = (k <= kl) ? vrow[k] : czero();
+      if (k == 0 || k == M) {
+        cs[padix(k)] = make_double2(U.x, V.x);
+      } else {
+        cs[padix(k)] = make_double2(U.x - V.y, U.y + V.x);
+        cs[padix(N - k)] = make_double2(U.x + V.y, V.x - U.y);
+      }
+    }
+  }
+  // Z[k] = (Q[k] + conj Q[M-k]) + i W^-k (Q[k] - conj Q[M-k]), k < M; Im Q[0], Q[M] dropped
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {
+    const int k = t + s * T;
+    double2 a = (k <= kl) ? qrow[k] : czero();
+    double2 b = (M - k <= kl) ? qrow[M - k] : czero();
+    if (k == 0) { a.y = 0.0; b.y = 0.0; }
+    const double2 sm_ = make_double2(a.x + b.x, a.y - b.y);
+    const double2 d = make_double2(a.x - b.x, a.y + b.y);
+    const double2 w = __ldg(&tw[k]);
+    const double2 tt = twmul<true>(d, w);  // W^-k d
+    zs[padix(k)] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
+  }
+  __syncthreads();
+  // q: inverse length-M transform, 8 values per thread; result back to zs
+  {
+    double2 h[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) h[s] = zs[padix(t + s * T)];
+    __syncthreads();
+    fft_regs<M, 8, true, 1>(h, zs, t, tw, 1);
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 8; ++s) zs[padix(t + s * T)] = h[s];
+  }
+  // u + i v: inverse length-N transform
+  double2 v[16];
+#pragma unroll
+  for (int s = 0; s < 16; ++s) v[s] = cs[padix(t + s * T)];
+  __syncthreads();
+  fft_regs<N, 16, true, 1>(v, cs, t, tw, 0);
+  __syncthreads();
+  // p = (u + i v) q  (produ.f90:18-19); q[2m] = Re z[m], q[2m+1] = Im z[m]
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    const int x = t + s * T;
+    const double2 zq = zs[padix(x >> 1)];
+    const double q = (x & 1) ? zq.y : zq.x;
+    v[s] = make_double2(v[s].x * q, v[s].y * q);
+  }
+  fft_regs<N, 16, false, 1>(v, cs, t, tw, 0);
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < 16; ++s) cs[padix(t + s * T)] = v[s];
+  __syncthreads();
+  double2* urw = uf + (size_t)y * NH;
+  double2* vrw = vf + (size_t)y * NH;
+#pragma unroll
+  for (int s = 0; s <= 8; ++s) {
+    const int k = t + s * T;
+    if (k <= kout) {
+      const double2 P = cs[padix(k)];
+      const double2 Q = cs[padix((N - k) & (N - 1))];
+      urw[k] = make_double2(P.x + Q.x, P.y - Q.y);
+      vrw[k] = make_double2(P.y + Q.y, Q.x - P.x);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Pass C: forward y-transforms of A and B, N = -i (kx A + ky B) / (2 N^2), the 2/3 mask
+// (row j of column i is kept iff min(j, N-j) <= kcut[i]) and the stage epilogue.
+// ---------------------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::COL_THREADS)
+k_nlt_colfwd(double2* af, const double2* __restrict__ bf, const double* __restrict__ fkx,
+             const double* __restrict__ fky, const int* __restrict__ kcut,
+             const double2* __restrict__ tw, int kxlim, int truncate, int* flag, EpiArgs E) {
+  using S = Shape<N>;
+  constexpr int T = S::T, C = S::COLS, NH = S::NH;
+  extern __shared__ double2 smem[];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *flag = 0;  // pass B of this nlt is complete
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  const int i = blockIdx.x * C + c;
+  const bool valid = i < NH;
+  const int ic = valid ? i : NH - 1;
+  if (blockIdx.x * C > kxlim) {
+    // no retained mode in this block of columns: N = 0
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < 16; ++s) epilogue(E, i, t + s * T, NH, czero());
+    }
+    return;
+  }
+  double2* sm = smem + c;
+  const double scale = 0.5 / ((double)N * (double)N);
+  const double kxs = __ldg(&fkx[ic]) * scale;
+  double2 v[16];
+#pragma unroll
+  for (int s = 0; s < 16; ++s) v[s] = valid ? af[(size_t)(t + s * T) * NH + ic] : czero();
+  fft_regs<N, 16, false, C>(v, sm, t, tw, 0);
+  // keep kx*FA in place of A (the same thread re-reads it below)
+  if (valid) {
+#pragma unroll
+    for (int s = 0; s < 16; ++s)
+      af[(size_t)(t + s * T) * NH + i] = make_double2(kxs * v[s].x, kxs * v[s].y);
+  }
+#pragma unroll
+  for (int s = 0; s < 16; ++s) v[s] = valid ? bf[(size_t)(t + s * T) * NH + ic] : czero();
+  __syncthreads();
+  fft_regs<N, 16, false, C>(v, sm, t, tw, 0);
+  if (!valid) return;
+  const int kc = truncate ? __ldg(&kcut[i]) : N;
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    const int j = t + s * T;
+    const double kys = __ldg(&fky[j]) * scale;
+    const double2 a = af[(size_t)j * NH + i];
+    // N = -i (kx A + ky B): re = kx Im A + ky Im B, im = -(kx Re A + ky Re B)
+    double2 nh = make_double2(fma(kys, v[s].y, a.y), -fma(kys, v[s].x, a.x));
+    const int aj = min(j, N - j);
+    if (aj > kc || (i == 0 && j == 0 && truncate)) nh = czero();
+    epilogue(E, i, j, NH, nh);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Standalone transforms (fft_inv.f90, fft_dir.f90) and elementwise routines.
+// ---------------------------------------------------------------------------------------
+
+// y-transform of every column; forward results are multiplied by `scale`.
+template <int N, bool INV>
+__global__ void __launch_bounds__(Shape<N>::COL_THREADS)
+k_col_fft(double2* z, const double2* __restrict__ tw, double scale) {
+  using S = Shape<N>;
+  constexpr int T = S::T, C = S::COLS, NH = S::NH;
+  extern __shared__ double2 smem[];
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  const int i = blockIdx.x * C + c;
+  const bool valid = i < NH;
+  const int ic = valid ? i : NH - 1;
+  double2 v[16];
+#pragma unroll
+  for (int s = 0; s < 16; ++s) v[s] = valid ? z[(size_t)(t + s * T) * NH + ic] : czero();
+  fft_regs<N, 16, INV, C>(v, smem + c, t, tw, 0);
+  if (valid) {
+#pragma unroll
+    for (int s = 0; s < 16; ++s)
+      z[(size_t)(t + s * T) * NH + i] = INV ? v[s] : make_double2(v[s].x * scale, v[s].y * scale);
+  }
+}
+
+// Row C2R in place (NH complex -> N real + 2 zero pads), half-length packing.
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::ROW_THREADS)
+k_row_c2r(double* z, const double2* __restrict__ tw) {
+  using S = Shape<N>;
+  constexpr int T = S::T, NH = S::NH, M = N / 2;
+  extern __shared__ double2 smem[];
+  const int r = threadIdx.x / T, t = threadIdx.x % T;
+  const int y = blockIdx.x * S::ROWS + r;
+  double2* zs = smem + (size_t)r * padded(M);
+  double2* row = reinterpret_cast<double2*>(z) + (size_t)y * NH;
+  double2 h[8];
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {
+    const int k = t + s * T;
+    double2 a = row[k], b = row[M - k];
+    if (k == 0) { a.y = 0.0; b.y = 0.0; }
+    const double2 sm_ = make_double2(a.x + b.x, a.y - b.y);
+    const double2 d = make_double2(a.x - b.x, a.y + b.y);
+    const double2 tt = twmul<true>(d, __ldg(&tw[k]));
+    h[s] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
+  }
+  fft_regs<M, 8, true, 1>(h, zs, t, tw, 1);
+  __syncthreads();  // every thread has read its row values before the row is overwritten
+#pragma unroll
+  for (int s = 0; s < 8; ++s) row[t + s * T] = h[s];
+  if (t == 0) row[M] = czero();
+}
+
+// Row R2C in place (N real -> NH complex), half-length packing.
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::ROW_THREADS)
+k_row_r2c(double* z, const double2* __restrict__ tw) {
+  using S = Shape<N>;
+  constexpr int T = S::T, NH = S::NH, M = N / 2;
+  extern __shared__ double2 smem[];
+  const int r = threadIdx.x / T, t = threadIdx.x % T;
+  const int y = blockIdx.x * S::ROWS + r;
+  double2* zs = smem + (size_t)r * padded(M);
+  double2* row = reinterpret_cast<double2*>(z) + (size_t)y * NH;
+  double2 h[8];
+#pragma unroll
+  for (int s = 0; s < 8; ++s) h[s] = row[t + s * T];  // z[m] = x[2m] + i x[2m+1]
+  fft_regs<M, 8, false, 1>(h, zs, t, tw, 1);
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < 8; ++s) zs[padix(t + s * T)] = h[s];
+  __syncthreads();
+  // X[k] = 1/2 (Z[k] + conj Z[M-k]) - i/2 W^k (Z[k] - conj Z[M-k]), k in [0, M]
+#pragma unroll
+  for (int s = 0; s <= 8; ++s) {
+    const int k = t + s * T;
+    if (k <= M) {
+      const double2 a = zs[padix(k & (M - 1))];
+      const double2 b = zs[padix((M - k) & (M - 1))];
+      const double2 sm_ = make_double2(a.x + b.x, a.y - b.y);
+      const double2 d = make_double2(a.x - b.x, a.y + b.y);
+      const double2 tt = twmul<false>(d, __ldg(&tw[k]));
+      row[k] = make_double2(0.5 * (sm_.x + tt.y), 0.5 * (sm_.y - tt.x));
+    }
+  }
+}
+
+}  // namespace gt

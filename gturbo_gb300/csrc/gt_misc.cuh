@@ -1,0 +1,226 @@
+// gt_misc.cuh -- non-templated kernels of the Gturbo hot path: trunc, produ, the stochastic
+// forcing, the diagnostics and the table set-up. Included by the host translation unit only.
+#pragma once
+
+#include "gt_kernels.cuh"
+
+namespace gt {
+
+// trunc (trunc.f90:10-25): zero outside the ellipse, then the mean mode.
+__global__ void k_trunc(double2* z, int n, int nh, const int* __restrict__ kcut) {
+  const size_t total = (size_t)n * nh;
+  for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < total;
+       o += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(o / nh), i = (int)(o % nh);
+    if (min(j, n - j) > __ldg(&kcut[i]) || o == 0) z[o] = czero();
+  }
+}
+
+// produ (produ.f90:11-23)
+__global__ void k_produ(const double* __restrict__ z, double* u, double* v, int n) {
+  const int ns = n + 2;
+  const size_t total = (size_t)ns * n;
+  for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < total;
+       o += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(o % ns);
+    if (i < n) {
+      const double zz = z[o];
+      u[o] = zz * u[o];
+      v[o] = zz * v[o];
+    } else {
+      u[o] = 0.0;
+      v[o] = 0.0;
+    }
+  }
+}
+
+// forcing (forcing.f90:16-33). Mode k uses the LCG state after k+1 draws from seed0:
+// x_{k+1} = (A[k] x0 + B[k]) mod 2^31 with A, B the jump-ahead coefficients of the map
+// x -> 69069 x + 1 (computed on the host), so the phases equal the serial rann sequence.
+// Distinct modes never touch the same value except a self-conjugate mode, which one thread
+// handles in the reference's order.
+__global__ void k_forcing(double2* z, int nh, int nf, const int* __restrict__ ikx,
+                          const int* __restrict__ iky, const int* __restrict__ jc,
+                          const uint32_t* __restrict__ lcga, const uint32_t* __restrict__ lcgb,
+                          const double2* __restrict__ ff, uint32_t seed0, double sf) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nf) return;
+  const double pi2 = 2.0 * 3.14159265358979;  // forcing.f90:10
+  const uint32_t x = (lcga[k] * seed0 + lcgb[k]) & 0x7FFFFFFFu;
+  const float rr = (float)((double)x / 2147483647.0);
+  const double te = pi2 * (double)rr;
+  double cs, cc;
+  sincos(te, &cs, &cc);
+  const int i = ikx[k], j = iky[k];
+  const double2 f = ff[k];
+  double2* p = z + (size_t)j * nh + i;
+  double2 a = *p;
+  a.x = a.x + sf * f.x * cc;
+  a.y = a.y + sf * f.y * cs;
+  *p = a;
+  if (i == 0 || i == nh - 1) {
+    double2* pc = z + (size_t)jc[j] * nh + i;
+    double2 b = *pc;
+    b.x = b.x + sf * f.x * cc;
+    b.y = b.y - sf * f.y * cs;
+    *pc = b;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Diagnostics (diagnostics.f90): deterministic, atomics-free.
+// Shell sums: thread (b, g) sums bin b over rows j in group g (ROWG rows) in (j, i) order;
+// a second kernel adds the groups in order. Global sums: per-row block reductions in a
+// fixed tree order, then the rows in order.
+// ---------------------------------------------------------------------------------------
+constexpr int kDiagRowGroup = 32;
+
+struct DiagArgs {
+  const double2* z;
+  const double2* znl;   // may be null: no fluxes
+  const double* fkxs;
+  const double* fkys;
+  int n, nh, nbin;
+  double dk, alpv;
+  double nu, mu, alpnu, alpmu;
+  double* part;         // [ngroups][nbin][4]: sp, sz, flem, flzm
+  double* rowsum;       // [n][6]
+};
+
+__device__ __forceinline__ int diag_bin(const DiagArgs& D, int i, int j) {
+  const double k = sqrt(__ldg(&D.fkxs[i]) + __ldg(&D.fkys[j]));
+  return (int)(k / D.dk);  // 0-based: reference ib - 1
+}
+
+__global__ void k_diag_bins(DiagArgs D) {
+  const int ngroups = (D.n + kDiagRowGroup - 1) / kDiagRowGroup;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= ngroups * D.nbin) return;
+  const int b = gid % D.nbin, g = gid / D.nbin;
+  double sp = 0.0, sz = 0.0, fe = 0.0, fz = 0.0;
+  if (b < D.nbin - 1) {
+    const int j0 = g * kDiagRowGroup, j1 = min(D.n, j0 + kDiagRowGroup);
+    for (int j = j0; j < j1; ++j) {
+      const double fkys = __ldg(&D.fkys[j]);
+      // The bin index is non-decreasing in i along a row. Start from the analytic estimate of
+      // the first i with bin >= b and correct it with the exact bin function.
+      const double kb = (double)b * D.dk;
+      const double rem = kb * kb - fkys;
+      int lo = rem > 0.0 ? (int)ceil(sqrt(rem) / D.dk) : 0;
+      lo = min(max(lo, 0), D.nh);
+      while (lo > 0 && diag_bin(D, lo - 1, j) >= b) --lo;
+      while (lo < D.nh && diag_bin(D, lo, j) < b) ++lo;
+      for (int i = lo; i < D.nh; ++i) {
+        if (diag_bin(D, i, j) != b) break;
+        if (i == 0 && j == 0) continue;
+        const double2 q = D.z[(size_t)j * D.nh + i];
+        const double k2 = __ldg(&D.fkxs[i]) + fkys;
+        const double ka = pow(k2, D.alpv / 2.0);
+        double a2 = hypot(q.x, q.y);
+        a2 = a2 * a2;
+        const double fac = (i == 0 || i == D.nh - 1) ? 0.5 : 1.0;
+        sp = sp + fac * a2 / ka;
+        sz = sz + fac * a2;
+        if (D.znl) {
+          const double2 w = D.znl[(size_t)j * D.nh + i];
+          const double ff = (i == 0 || i == D.nh - 1) ? 1.0 : 2.0;
+          const double f = q.x * w.x + q.y * w.y;
+          fz = fz + ff * f;
+          fe = fe + ff * (f / ka);
+        }
+      }
+    }
+  }
+  double* p = D.part + ((size_t)g * D.nbin + b) * 4;
+  p[0] = sp; p[1] = sz; p[2] = fe; p[3] = fz;
+}
+
+// out[b*4 + q] = sum over groups (in order); then spectra / dk and flux suffix sums.
+__global__ void k_diag_bins_final(DiagArgs D, double* out /* [nbin][4] */) {
+  const int ngroups = (D.n + kDiagRowGroup - 1) / kDiagRowGroup;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < D.nbin) {
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int g = 0; g < ngroups; ++g)
+      for (int q = 0; q < 4; ++q) s[q] += D.part[((size_t)g * D.nbin + b) * 4 + q];
+    out[b * 4 + 0] = s[0] / D.dk;
+    out[b * 4 + 1] = s[1] / D.dk;
+    out[b * 4 + 2] = s[2];
+    out[b * 4 + 3] = s[3];
+  }
+}
+
+__global__ void k_diag_suffix(const double* bins, double* fl, int nbin) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbin) return;
+  double se = 0.0, sq = 0.0;
+  for (int b2 = b; b2 < nbin; ++b2) {  // sum(flem(i:NBIN)), diagnostics.f90:106-107
+    se += bins[b2 * 4 + 2];
+    sq += bins[b2 * 4 + 3];
+  }
+  fl[b * 2 + 0] = se;
+  fl[b * 2 + 1] = sq;
+}
+
+// glob (diagnostics.f90:147-163): per-row sums with a fixed-order block reduction.
+__global__ void k_diag_glob_rows(DiagArgs D) {
+  const int j = blockIdx.x;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  const double fkys = __ldg(&D.fkys[j]);
+  for (int i = threadIdx.x; i < D.nh; i += blockDim.x) {
+    if (i == 0 && j == 0) continue;
+    const double2 q = D.z[(size_t)j * D.nh + i];
+    const double k2 = __ldg(&D.fkxs[i]) + fkys;
+    const double ka = pow(k2, D.alpv / 2.0);
+    double a2 = hypot(q.x, q.y);
+    a2 = a2 * a2;
+    const double fac = (i == 0 || i == D.nh - 1) ? 0.5 : 1.0;
+    acc[0] += fac * a2 / ka;
+    acc[1] += fac * a2;
+    acc[2] += 2.0 * fac * D.nu * pow(k2, D.alpnu) * a2;
+    acc[3] += 2.0 * fac * D.mu * pow(k2, D.alpmu) * a2;
+    acc[4] += 2.0 * fac * D.nu * pow(k2, D.alpnu - D.alpv / 2.0) * a2;
+    acc[5] += 2.0 * fac * D.mu * pow(k2, D.alpmu - D.alpv / 2.0) * a2;
+  }
+  __shared__ double red[6][256];
+  for (int q = 0; q < 6; ++q) red[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int q = 0; q < 6; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) D.rowsum[(size_t)j * 6 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void k_diag_glob_final(DiagArgs D, double* glob) {
+  const int q = threadIdx.x;
+  if (q >= 6) return;
+  double s = 0.0;
+  for (int j = 0; j < D.n; ++j) s += D.rowsum[(size_t)j * 6 + q];
+  glob[q] = s;
+}
+
+// ---------------------------------------------------------------------------------------
+// Table set-up (defk.f90:43-50 and nlt.f90:26-27 on the device).
+// ---------------------------------------------------------------------------------------
+__global__ void k_init_tables(double* emk, double* kainv, const double* __restrict__ fkxs,
+                              const double* __restrict__ fkys, int n, int nh, double nu,
+                              double alpnu, double mu, double alpmu, double alpv, double dt) {
+  const size_t total = (size_t)n * nh;
+  for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < total;
+       o += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(o / nh), i = (int)(o % nh);
+    if (o == 0) {
+      emk[0] = 0.0;
+      kainv[0] = 0.0;
+      continue;
+    }
+    const double fk2 = fkxs[i] + fkys[j];
+    const double scra = nu * pow(fk2, alpnu) + mu * pow(fk2, alpmu);
+    emk[o] = exp(-0.5 * dt * scra);
+    kainv[o] = 1.0 / pow(fk2, alpv / 2.0);
+  }
+}
+
+}  // namespace gt

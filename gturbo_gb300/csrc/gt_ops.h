@@ -1,0 +1,56 @@
+// gt_ops.h -- host-side description of one kernel launch, dispatched to the per-N
+// instantiation units (gt_inst_<N>.cu) so that every grid size compiles in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gt_kernels.cuh"
+
+namespace gt {
+
+enum OpKind : int {
+  OP_NLT_COLINV = 0,  // pass A
+  OP_NLT_ROW = 1,     // pass B
+  OP_NLT_COLFWD = 2,  // pass C (+ epilogue)
+  OP_COL_INV = 3,     // column inverse transform (fft_inv, first half)
+  OP_COL_FWD = 4,     // column forward transform, scaled (fft_dir, second half)
+  OP_ROW_C2R = 5,     // row C2R (fft_inv, second half)
+  OP_ROW_R2C = 6,     // row R2C (fft_dir, first half)
+};
+
+struct GtOp {
+  int kind;
+  cudaStream_t stream;
+  const double2* zin;
+  double2* a;
+  double2* b;
+  double2* c;
+  const double* kainv;
+  const double* fkx;
+  const double* fky;
+  const int* kcut;
+  const double2* tw;
+  int kxlim, kin, kout, truncate;
+  int* flag;
+  double scale;
+  EpiArgs epi;
+};
+
+// Per-N entry points (defined in gt_inst_<N>.cu).
+#define GT_DECLARE_N(NN)                              \
+  cudaError_t prepare_##NN();                         \
+  cudaError_t dispatch_##NN(const GtOp& op);
+GT_DECLARE_N(16)
+GT_DECLARE_N(32)
+GT_DECLARE_N(64)
+GT_DECLARE_N(128)
+GT_DECLARE_N(256)
+GT_DECLARE_N(512)
+GT_DECLARE_N(1024)
+GT_DECLARE_N(2048)
+GT_DECLARE_N(4096)
+GT_DECLARE_N(8192)
+#undef GT_DECLARE_N
+
+}  // namespace gt

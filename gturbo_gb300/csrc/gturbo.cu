@@ -1,0 +1,593 @@
+// gturbo.cu -- host side of the C-ABI declared in include/gturbo.h.
+//
+// A handle owns the tables of one parameter set (defk + iniforcing of the reference, the
+// twiddles, the truncation cut-offs and the LCG jump-ahead coefficients) on the device that
+// was current at gt_create. Fields are owned by the caller and passed as device pointers.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gturbo.h"
+#include "gt_misc.cuh"
+#include "gt_ops.h"
+
+using gt::GtOp;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+struct gt_handle {
+  gt_params p;
+  int N = 0, NH = 0, NBIN = 0, split = 0, rko = 2, truncate = 1;
+  int kxlim = 0;
+  double dkx = 0, dky = 0, dt2 = 0, dt3 = 0, dt6 = 0, sdt = 0;
+  double fkxsmax = 0, fkysmax = 0, rtrunc2 = 0;
+  int nf = 0;
+  double inpz = 0, inpe = 0;
+  std::vector<double> fkx, fky, fkxs, fkys, emkx, emky;
+  std::vector<int> jc, kcut, ikxf, ikyf;
+  std::vector<uint32_t> lcga, lcgb;  // index k: coefficients of the (k+1)-th draw
+  uint32_t lcga_nf = 1, lcgb_nf = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // device tables
+  double2* d_tw = nullptr;
+  double* d_emk = nullptr;
+  double* d_kainv = nullptr;
+  double *d_fkx = nullptr, *d_fky = nullptr, *d_fkxs = nullptr, *d_fkys = nullptr;
+  double *d_emkx = nullptr, *d_emky = nullptr;
+  int *d_kcut = nullptr, *d_jc = nullptr, *d_ikxf = nullptr, *d_ikyf = nullptr;
+  uint32_t *d_lcga = nullptr, *d_lcgb = nullptr;
+  double2* d_ff = nullptr;
+  int* d_flag = nullptr;
+  // diagnostics scratch
+  double *d_part = nullptr, *d_rowsum = nullptr, *d_bins = nullptr, *d_fl = nullptr, *d_glob = nullptr;
+  double* h_diag = nullptr;  // pinned: bins [nbin*4] + fl [nbin*2] + glob [6]
+  cudaError_t (*dispatch)(const GtOp&) = nullptr;
+};
+
+namespace {
+
+int fail(gt_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+int cuda_fail(gt_handle* h, cudaError_t e, const char* what) {
+  return fail(h, GT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define GT_CUDA(h, call)                                   \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+bool pow2_in_range(int n) { return n >= 16 && n <= 8192 && (n & (n - 1)) == 0; }
+
+// exp(-2 pi i k / n) for k in [0, n), each value from an argument reduced to [0, pi/4].
+void make_twiddles(int n, std::vector<double2>& tw) {
+  tw.resize(n);
+  const double twopi = 2.0 * 3.14159265358979323846;
+  const int q4 = n / 4;
+  for (int k = 0; k < n; ++k) {
+    const int quad = k / q4, r = k % q4;
+    double c, s;
+    if (2 * r <= q4) {
+      c = std::cos(twopi * (double)r / (double)n);
+      s = std::sin(twopi * (double)r / (double)n);
+    } else {
+      c = std::sin(twopi * (double)(q4 - r) / (double)n);
+      s = std::cos(twopi * (double)(q4 - r) / (double)n);
+    }
+    double C, S;
+    switch (quad) {
+      case 0: C = c; S = s; break;
+      case 1: C = -s; S = c; break;
+      case 2: C = -c; S = -s; break;
+      default: C = s; S = -c; break;
+    }
+    tw[k] = make_double2(C, -S);
+  }
+}
+
+template <typename T>
+int upload(gt_handle* h, T** dst, const T* src, size_t count) {
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)dst, sizeof(T) * count);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc");
+  if (src) {
+    e = cudaMemcpy(*dst, src, sizeof(T) * count, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpy");
+  }
+  return GT_OK;
+}
+
+cudaError_t (*dispatch_for(int n))(const GtOp&) {
+  switch (n) {
+    case 16: return gt::dispatch_16;
+    case 32: return gt::dispatch_32;
+    case 64: return gt::dispatch_64;
+    case 128: return gt::dispatch_128;
+    case 256: return gt::dispatch_256;
+    case 512: return gt::dispatch_512;
+    case 1024: return gt::dispatch_1024;
+    case 2048: return gt::dispatch_2048;
+    case 4096: return gt::dispatch_4096;
+    case 8192: return gt::dispatch_8192;
+    default: return nullptr;
+  }
+}
+
+cudaError_t prepare_for(int n) {
+  switch (n) {
+    case 16: return gt::prepare_16();
+    case 32: return gt::prepare_32();
+    case 64: return gt::prepare_64();
+    case 128: return gt::prepare_128();
+    case 256: return gt::prepare_256();
+    case 512: return gt::prepare_512();
+    case 1024: return gt::prepare_1024();
+    case 2048: return gt::prepare_2048();
+    case 4096: return gt::prepare_4096();
+    case 8192: return gt::prepare_8192();
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+void free_device(gt_handle* h) {
+  void* ptrs[] = {h->d_tw, h->d_emk, h->d_kainv, h->d_fkx, h->d_fky, h->d_fkxs, h->d_fkys,
+                  h->d_emkx, h->d_emky, h->d_kcut, h->d_jc, h->d_ikxf, h->d_ikyf, h->d_lcga,
+                  h->d_lcgb, h->d_ff, h->d_flag, h->d_part, h->d_rowsum, h->d_bins, h->d_fl,
+                  h->d_glob};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (h->h_diag) cudaFreeHost(h->h_diag);
+}
+
+GtOp base_op(const gt_handle* h) {
+  GtOp op;
+  std::memset(&op, 0, sizeof(op));
+  op.stream = h->stream;
+  op.kainv = h->d_kainv;
+  op.fkx = h->d_fkx;
+  op.fky = h->d_fky;
+  op.kcut = h->d_kcut;
+  op.tw = h->d_tw;
+  op.truncate = h->truncate;
+  op.kxlim = h->truncate ? h->kxlim : h->N / 2;
+  op.kin = op.kxlim;
+  op.kout = op.kxlim;
+  op.flag = h->d_flag;
+  op.epi.split = 0;
+  op.epi.emk = h->d_emk;
+  op.epi.emkx = h->d_emkx;
+  op.epi.emky = h->d_emky;
+  op.epi.dt = h->p.dt;
+  op.epi.dt2 = h->dt2;
+  op.epi.dt3 = h->dt3;
+  op.epi.dt6 = h->dt6;
+  return op;
+}
+
+int run(gt_handle* h, const GtOp& op) {
+  cudaError_t e = h->dispatch(op);
+  if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
+  return GT_OK;
+}
+
+// One nonlinear-term evaluation: input zin, work fields (qbuf receives the transformed q;
+// it may alias zin), u, v; pass C applies the epilogue `epi`.
+int nlt_passes(gt_handle* h, const double* zin, double* qbuf, double* u, double* v,
+               const gt::EpiArgs& epi) {
+  GtOp op = base_op(h);
+  op.kind = gt::OP_NLT_COLINV;
+  op.zin = reinterpret_cast<const double2*>(zin);
+  op.a = reinterpret_cast<double2*>(qbuf);
+  op.b = reinterpret_cast<double2*>(u);
+  op.c = reinterpret_cast<double2*>(v);
+  int rc = run(h, op);
+  if (rc) return rc;
+  op.kind = gt::OP_NLT_ROW;
+  op.zin = reinterpret_cast<const double2*>(qbuf);
+  rc = run(h, op);
+  if (rc) return rc;
+  op.kind = gt::OP_NLT_COLFWD;
+  op.epi = epi;
+  return run(h, op);
+}
+
+gt::EpiArgs make_epi(const gt_handle* h, int mode, double* out, double* znew, const double* z) {
+  gt::EpiArgs E = base_op(h).epi;
+  E.mode = mode;
+  E.out = reinterpret_cast<double2*>(out);
+  E.znew = reinterpret_cast<double2*>(znew);
+  E.z = reinterpret_cast<const double2*>(z);
+  return E;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gt_create(const gt_params* p, gt_handle** out) {
+  if (!p || !out) return fail(nullptr, GT_ERR_ARG, "gt_create: null argument");
+  *out = nullptr;
+  if (!pow2_in_range(p->n))
+    return fail(nullptr, GT_ERR_ARG, "gt_create: n must be a power of two in [16, 8192]");
+  if (!(p->xlx > 0.0) || !(p->xly > 0.0) || !(p->dt > 0.0))
+    return fail(nullptr, GT_ERR_ARG, "gt_create: xlx, xly and dt must be positive");
+  gt_handle* h = new (std::nothrow) gt_handle();
+  if (!h) return fail(nullptr, GT_ERR_NOMEM, "gt_create: out of host memory");
+  h->p = *p;
+  const int N = h->N = p->n;
+  const int NH = h->NH = N / 2 + 1;
+  h->NBIN = N / 2;
+  h->dispatch = dispatch_for(N);
+  // inieuler.f90:22-36, 237-244
+  int split = 0;
+  if (p->alpnu < 1.0005 && p->alpnu > 0.9995 && p->alpmu < 0.0005 && p->alpmu > -0.0005) split = 1;
+  if (p->rko == 4) split = 0;
+  if (p->split == 0 || p->split == 1) split = p->split;
+  h->split = split;
+  h->rko = (p->rko == 4) ? 4 : 2;
+  if (h->split && h->rko == 4) {
+    delete h;
+    return fail(nullptr, GT_ERR_ARG, "gt_create: the split integrator exists only for RK2");
+  }
+  h->truncate = p->truncate;
+  // inieuler.f90:78-81
+  h->sdt = std::sqrt(p->dt);
+  h->dt2 = p->dt / 2.0;
+  h->dt3 = p->dt / 3.0;
+  h->dt6 = p->dt / 6.0;
+  // defk.f90:12-73
+  h->jc.resize(N);
+  h->jc[0] = 0;
+  for (int j = 1; j < N; ++j) h->jc[j] = N - j;
+  h->dkx = 2.0 * 3.14159265358979323846 / p->xlx;
+  h->dky = 2.0 * 3.14159265358979323846 / p->xly;
+  h->fkx.resize(NH);
+  h->fkxs.resize(NH);
+  h->fky.resize(N);
+  h->fkys.resize(N);
+  for (int i = 0; i < NH; ++i) h->fkx[i] = (double)i * h->dkx;
+  for (int j = 0; j <= N / 2; ++j) h->fky[j] = (double)j * h->dky;
+  for (int j = N / 2 + 1; j < N; ++j) h->fky[j] = (double)(j - N) * h->dky;
+  for (int i = 0; i < NH; ++i) h->fkxs[i] = h->fkx[i] * h->fkx[i];
+  for (int j = 0; j < N; ++j) h->fkys[j] = h->fky[j] * h->fky[j];
+  h->emky.resize(N);
+  h->emkx.resize(NH);
+  for (int j = 0; j < N; ++j)
+    h->emky[j] = std::exp(-0.5 * p->dt * (p->nu * std::pow(h->fkys[j], p->alpnu) + p->mu));
+  for (int i = 0; i < NH; ++i)
+    h->emkx[i] = std::exp(-0.5 * p->dt * (p->nu * std::pow(h->fkxs[i], p->alpnu)));
+  h->fkxsmax = h->fkxs[N / 2];
+  h->fkysmax = h->fkys[N / 2];
+  h->rtrunc2 = p->rtrunc * p->rtrunc;
+  // truncation cut-off per column: largest |ky| row kept by trunc.f90:12-16 (monotone in |ky|)
+  h->kcut.resize(NH);
+  h->kxlim = -1;
+  for (int i = 0; i < NH; ++i) {
+    int a = 0;
+    while (a <= N / 2) {
+      const double k1 = h->fkys[a] / h->fkysmax;
+      const double k2 = k1 + h->fkxs[i] / h->fkxsmax;
+      if (k2 > h->rtrunc2) break;
+      ++a;
+    }
+    h->kcut[i] = a - 1;
+    if (a > 0) h->kxlim = i;
+  }
+  // iniforcing.f90:11-68
+  const double famp = p->famp, k1f2 = p->k1f * p->k1f, k2f2 = p->k2f * p->k2f;
+  for (int pass = 0; pass < 3; ++pass) {
+    const int ilo = pass == 0 ? 0 : pass == 1 ? 1 : N / 2;
+    const int ihi = pass == 0 ? 0 : pass == 1 ? N / 2 - 1 : N / 2;
+    for (int i = ilo; i <= ihi; ++i) {
+      const int jlo = pass == 0 ? 1 : 0;
+      const int jhi = pass == 1 ? N - 1 : N / 2;
+      for (int j = jlo; j <= jhi; ++j) {
+        const double k2 = h->fkxs[i] + h->fkys[j];
+        const double k2n = h->fkxs[i] / h->fkxsmax + h->fkys[j] / h->fkysmax;
+        if (k2n <= h->rtrunc2 && k2 <= k2f2 && k2 > k1f2) {
+          if ((int)h->ikxf.size() >= GT_NFORC) {
+            delete h;
+            return fail(nullptr, GT_ERR_NFORC, "NFORC too small !");
+          }
+          h->ikxf.push_back(i);
+          h->ikyf.push_back(j);
+          h->inpz = h->inpz + famp * famp;
+          h->inpe = h->inpe + famp * famp / std::pow(k2, p->alpv / 2.0);
+        }
+      }
+    }
+  }
+  h->nf = (int)h->ikxf.size();
+  // LCG jump-ahead: x_{k+1} = A_{k+1} x_0 + B_{k+1} (mod 2^32, masked to 31 bits)
+  uint32_t A = 1, B = 0;
+  for (int k = 0; k < h->nf; ++k) {
+    A = 69069u * A;
+    B = 69069u * B + 1u;
+    h->lcga.push_back(A);
+    h->lcgb.push_back(B);
+  }
+  h->lcga_nf = A;
+  h->lcgb_nf = B;
+
+  // device side
+  int rc = GT_OK;
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e != cudaSuccess) rc = cuda_fail(h, e, "cudaGetDevice");
+  if (!rc) {
+    e = prepare_for(N);
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "cudaFuncSetAttribute");
+  }
+  std::vector<double2> tw;
+  make_twiddles(N, tw);
+  std::vector<double2> ff(h->nf > 0 ? h->nf : 1, make_double2(1.0, 1.0));
+  const size_t nc = (size_t)N * NH;
+  if (!rc) rc = upload(h, &h->d_tw, tw.data(), tw.size());
+  if (!rc) rc = upload<double>(h, &h->d_emk, nullptr, nc);
+  if (!rc) rc = upload<double>(h, &h->d_kainv, nullptr, nc);
+  if (!rc) rc = upload(h, &h->d_fkx, h->fkx.data(), NH);
+  if (!rc) rc = upload(h, &h->d_fky, h->fky.data(), N);
+  if (!rc) rc = upload(h, &h->d_fkxs, h->fkxs.data(), NH);
+  if (!rc) rc = upload(h, &h->d_fkys, h->fkys.data(), N);
+  if (!rc) rc = upload(h, &h->d_emkx, h->emkx.data(), NH);
+  if (!rc) rc = upload(h, &h->d_emky, h->emky.data(), N);
+  if (!rc) rc = upload(h, &h->d_kcut, h->kcut.data(), NH);
+  if (!rc) rc = upload(h, &h->d_jc, h->jc.data(), N);
+  if (!rc) rc = upload(h, &h->d_ikxf, h->ikxf.data(), h->nf);
+  if (!rc) rc = upload(h, &h->d_ikyf, h->ikyf.data(), h->nf);
+  if (!rc) rc = upload(h, &h->d_lcga, h->lcga.data(), h->nf);
+  if (!rc) rc = upload(h, &h->d_lcgb, h->lcgb.data(), h->nf);
+  if (!rc) rc = upload(h, &h->d_ff, ff.data(), ff.size());
+  const int zero = 0;
+  if (!rc) rc = upload(h, &h->d_flag, &zero, 1);
+  const int ngroups = (N + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
+  if (!rc) rc = upload<double>(h, &h->d_part, nullptr, (size_t)ngroups * h->NBIN * 4);
+  if (!rc) rc = upload<double>(h, &h->d_rowsum, nullptr, (size_t)N * 6);
+  if (!rc) rc = upload<double>(h, &h->d_bins, nullptr, (size_t)h->NBIN * 4);
+  if (!rc) rc = upload<double>(h, &h->d_fl, nullptr, (size_t)h->NBIN * 2);
+  if (!rc) rc = upload<double>(h, &h->d_glob, nullptr, 6);
+  if (!rc) {
+    e = cudaMallocHost((void**)&h->h_diag, sizeof(double) * ((size_t)h->NBIN * 6 + 6));
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "cudaMallocHost");
+  }
+  if (!rc) {
+    gt::k_init_tables<<<1024, 256>>>(h->d_emk, h->d_kainv, h->d_fkxs, h->d_fkys, N, NH, p->nu,
+                                      p->alpnu, p->mu, p->alpmu, p->alpv, p->dt);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "table set-up");
+  }
+  if (rc) {
+    g_create_error = h->err;
+    free_device(h);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return GT_OK;
+}
+
+int gt_destroy(gt_handle* h) {
+  if (!h) return GT_OK;
+  cudaDeviceSynchronize();
+  free_device(h);
+  delete h;
+  return GT_OK;
+}
+
+int gt_set_stream(gt_handle* h, void* stream) {
+  if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_stream: null handle");
+  h->stream = (cudaStream_t)stream;
+  return GT_OK;
+}
+
+int gt_get_info(const gt_handle* h, gt_info* info) {
+  if (!h || !info) return GT_ERR_ARG;
+  std::memset(info, 0, sizeof(*info));
+  info->n = h->N;
+  info->nh = h->NH;
+  info->nbin = h->NBIN;
+  info->rko = h->rko;
+  info->split = h->split;
+  info->truncate = h->truncate;
+  info->nf = h->nf;
+  info->field_doubles = (int64_t)(h->N + 2) * h->N;
+  info->dkx = h->dkx;
+  info->dky = h->dky;
+  info->inpz = h->inpz;
+  info->inpe = h->inpe;
+  info->fkxsmax = h->fkxsmax;
+  info->fkysmax = h->fkysmax;
+  info->rtrunc2 = h->rtrunc2;
+  return GT_OK;
+}
+
+int gt_get_forcing_modes(const gt_handle* h, int32_t* ikxf, int32_t* ikyf, int32_t* nf) {
+  if (!h || !nf) return GT_ERR_ARG;
+  *nf = h->nf;
+  for (int k = 0; k < h->nf; ++k) {
+    if (ikxf) ikxf[k] = h->ikxf[k];
+    if (ikyf) ikyf[k] = h->ikyf[k];
+  }
+  return GT_OK;
+}
+
+const char* gt_last_error(const gt_handle* h) {
+  return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+int gt_sync(gt_handle* h) {
+  if (!h) return fail(nullptr, GT_ERR_ARG, "gt_sync: null handle");
+  GT_CUDA(h, cudaStreamSynchronize(h->stream));
+  GT_CUDA(h, cudaGetLastError());
+  return GT_OK;
+}
+
+int gt_fft_dir(gt_handle* h, double* z) {
+  if (!h || !z) return fail(h, GT_ERR_ARG, "gt_fft_dir: null argument");
+  GtOp op = base_op(h);
+  op.a = reinterpret_cast<double2*>(z);
+  op.kind = gt::OP_ROW_R2C;
+  int rc = run(h, op);
+  if (rc) return rc;
+  op.kind = gt::OP_COL_FWD;
+  op.scale = 1.0 / ((double)h->N * (double)h->N);
+  return run(h, op);
+}
+
+int gt_fft_inv(gt_handle* h, double* z) {
+  if (!h || !z) return fail(h, GT_ERR_ARG, "gt_fft_inv: null argument");
+  GtOp op = base_op(h);
+  op.a = reinterpret_cast<double2*>(z);
+  op.kind = gt::OP_COL_INV;
+  int rc = run(h, op);
+  if (rc) return rc;
+  op.kind = gt::OP_ROW_C2R;
+  return run(h, op);
+}
+
+int gt_trunc(gt_handle* h, double* z) {
+  if (!h || !z) return fail(h, GT_ERR_ARG, "gt_trunc: null argument");
+  gt::k_trunc<<<4 * 152, 256, 0, h->stream>>>(reinterpret_cast<double2*>(z), h->N, h->NH, h->d_kcut);
+  GT_CUDA(h, cudaGetLastError());
+  return GT_OK;
+}
+
+int gt_produ(gt_handle* h, const double* z, double* u, double* v) {
+  if (!h || !z || !u || !v) return fail(h, GT_ERR_ARG, "gt_produ: null argument");
+  gt::k_produ<<<4 * 152, 256, 0, h->stream>>>(z, u, v, h->N);
+  GT_CUDA(h, cudaGetLastError());
+  return GT_OK;
+}
+
+int gt_nlt(gt_handle* h, double* z, double* u, double* v) {
+  if (!h || !z || !u || !v) return fail(h, GT_ERR_ARG, "gt_nlt: null argument");
+  if (z == u || z == v || u == v) return fail(h, GT_ERR_ARG, "gt_nlt: z, u, v must be distinct");
+  return nlt_passes(h, z, z, u, v, make_epi(h, gt::EPI_NLT, z, nullptr, nullptr));
+}
+
+int gt_step_rk2(gt_handle* h, double* z, double* znl, double* u, double* v) {
+  if (!h || !z || !znl || !u || !v) return fail(h, GT_ERR_ARG, "gt_step_rk2: null argument");
+  gt::EpiArgs E1 = make_epi(h, gt::EPI_RK2A, znl, nullptr, z);
+  gt::EpiArgs E2 = make_epi(h, gt::EPI_RK2B, z, nullptr, z);
+  E1.split = E2.split = h->split;
+  int rc = nlt_passes(h, z, znl, u, v, E1);
+  if (rc) return rc;
+  return nlt_passes(h, znl, znl, u, v, E2);
+}
+
+int gt_step_rk4(gt_handle* h, double* z, double* znl, double* znew, double* u, double* v) {
+  if (!h || !z || !znl || !znew || !u || !v) return fail(h, GT_ERR_ARG, "gt_step_rk4: null argument");
+  if (h->split) return fail(h, GT_ERR_ARG, "gt_step_rk4: the split integrator exists only for RK2");
+  int rc = nlt_passes(h, z, znl, u, v, make_epi(h, gt::EPI_RK4A, znl, znew, z));
+  if (!rc) rc = nlt_passes(h, znl, znl, u, v, make_epi(h, gt::EPI_RK4B, znl, znew, z));
+  if (!rc) rc = nlt_passes(h, znl, znl, u, v, make_epi(h, gt::EPI_RK4C, znl, znew, z));
+  if (!rc) rc = nlt_passes(h, znl, znl, u, v, make_epi(h, gt::EPI_RK4D, z, znew, nullptr));
+  return rc;
+}
+
+float gt_rann(int32_t* seed) {
+  uint32_t x = (uint32_t)(*seed);
+  x = (69069u * x + 1u) & 0x7FFFFFFFu;
+  *seed = (int32_t)x;
+  return (float)((double)x / (double)0x7FFFFFFF);
+}
+
+int gt_forcing(gt_handle* h, double* z, int32_t* seed) {
+  if (!h || !z || !seed) return fail(h, GT_ERR_ARG, "gt_forcing: null argument");
+  if (h->nf == 0) return GT_OK;
+  const uint32_t x0 = (uint32_t)(*seed);
+  const double sf = h->sdt * h->p.famp;
+  gt::k_forcing<<<(h->nf + 127) / 128, 128, 0, h->stream>>>(
+      reinterpret_cast<double2*>(z), h->NH, h->nf, h->d_ikxf, h->d_ikyf, h->d_jc, h->d_lcga,
+      h->d_lcgb, h->d_ff, x0, sf);
+  GT_CUDA(h, cudaGetLastError());
+  *seed = (int32_t)((h->lcga_nf * x0 + h->lcgb_nf) & 0x7FFFFFFFu);
+  return GT_OK;
+}
+
+int gt_diag(gt_handle* h, const double* z, const double* znl, double* sp, double* sz, double* fle,
+            double* flz, double* glob) {
+  if (!h || !z) return fail(h, GT_ERR_ARG, "gt_diag: null argument");
+  if ((fle || flz) && !znl) return fail(h, GT_ERR_ARG, "gt_diag: fluxes need znl");
+  gt::DiagArgs D;
+  D.z = reinterpret_cast<const double2*>(z);
+  D.znl = reinterpret_cast<const double2*>(znl);
+  D.fkxs = h->d_fkxs;
+  D.fkys = h->d_fkys;
+  D.n = h->N;
+  D.nh = h->NH;
+  D.nbin = h->NBIN;
+  D.dk = h->dkx;
+  D.alpv = h->p.alpv;
+  D.nu = h->p.nu;
+  D.mu = h->p.mu;
+  D.alpnu = h->p.alpnu;
+  D.alpmu = h->p.alpmu;
+  D.part = h->d_part;
+  D.rowsum = h->d_rowsum;
+  const int nb = h->NBIN;
+  double* hb = h->h_diag;
+  double* hf = hb + (size_t)nb * 4;
+  double* hg = hf + (size_t)nb * 2;
+  const bool want_bins = sp || sz || fle || flz;
+  if (want_bins) {
+    const int ngroups = (h->N + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
+    const int nthr = ngroups * nb;
+    gt::k_diag_bins<<<(nthr + 127) / 128, 128, 0, h->stream>>>(D);
+    gt::k_diag_bins_final<<<(nb + 127) / 128, 128, 0, h->stream>>>(D, h->d_bins);
+    GT_CUDA(h, cudaGetLastError());
+    GT_CUDA(h, cudaMemcpyAsync(hb, h->d_bins, sizeof(double) * nb * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (znl) {
+      gt::k_diag_suffix<<<(nb + 127) / 128, 128, 0, h->stream>>>(h->d_bins, h->d_fl, nb);
+      GT_CUDA(h, cudaGetLastError());
+      GT_CUDA(h, cudaMemcpyAsync(hf, h->d_fl, sizeof(double) * nb * 2, cudaMemcpyDeviceToHost, h->stream));
+    }
+  }
+  if (glob) {
+    gt::k_diag_glob_rows<<<h->N, 256, 0, h->stream>>>(D);
+    gt::k_diag_glob_final<<<1, 32, 0, h->stream>>>(D, h->d_glob);
+    GT_CUDA(h, cudaGetLastError());
+    GT_CUDA(h, cudaMemcpyAsync(hg, h->d_glob, sizeof(double) * 6, cudaMemcpyDeviceToHost, h->stream));
+  }
+  GT_CUDA(h, cudaStreamSynchronize(h->stream));
+  for (int b = 0; b < nb; ++b) {
+    if (sp) sp[b] = hb[b * 4 + 0];
+    if (sz) sz[b] = hb[b * 4 + 1];
+    if (fle) fle[b] = hf[b * 2 + 0];
+    if (flz) flz[b] = hf[b * 2 + 1];
+  }
+  if (glob) {
+    bool finite = true;
+    for (int q = 0; q < 6; ++q) {
+      glob[q] = hg[q];
+      finite = finite && std::isfinite(hg[q]);
+    }
+    if (!finite) return fail(h, GT_ERR_NONFINITE, "gt_diag: non-finite global budget");
+  }
+  return GT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,168 @@
+"""Host-side mirror of the reference's time-stepping interface, on the CUDA C-ABI.
+
+The method names and argument meanings follow the Fortran routines they replace:
+
+================  =====================================  ==============================
+method            reference                              C-ABI
+================  =====================================  ==============================
+``fft_dir(z)``    src/fft_dir.f90:1-24                   ``gt_fft_dir``
+``fft_inv(z)``    src/fft_inv.f90:1-16                   ``gt_fft_inv``
+``trunc(z)``      src/trunc.f90:1-28                     ``gt_trunc``
+``produ(z,u,v)``  src/produ.f90:1-26                     ``gt_produ``
+``nlt(z,u,v)``    src/nlt.f90:1-66                       ``gt_nlt``
+``step(...)``     src/rkstep.f90:2-76                    ``gt_step_rk2``
+``step4(...)``    src/rkstep.f90:82-131                  ``gt_step_rk4``
+``forcing(z,s)``  src/forcing.f90:1-36                   ``gt_forcing``
+``diag(z,znl)``   src/diagnostics.f90 spectrum/fluxes/glob  ``gt_diag``
+================  =====================================  ==============================
+
+Fields are CUDA float64 tensors of shape (N, N+2) (the physical view ``real(8) z(N+2,N)``);
+``spec(z)`` is the complex (N, N/2+1) view of the same memory. Work is enqueued on the
+solver's stream (the current torch stream at construction unless one is given).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .params import GtInfo, Params
+
+
+def spec(z: torch.Tensor) -> torch.Tensor:
+    """Complex (N, N/2+1) view of an (N, N+2) float64 field."""
+    n = z.shape[0]
+    return z.view(torch.complex128).view(n, n // 2 + 1)
+
+
+class Solver:
+    """One parameter set on one device: tables, forced modes and the hot-path routines."""
+
+    def __init__(self, p: Params, device: int | torch.device | None = None,
+                 stream: torch.cuda.Stream | None = None):
+        self.lib = _lib.load()
+        self.p = p
+        self.n = p.n
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else
+                                   torch.device(device).index or 0)
+        self._cp = p.to_ctypes()
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            torch.cuda.init()
+            rc = self.lib.gt_create(ctypes.byref(self._cp), ctypes.byref(h))
+            if rc != 0:
+                raise _lib.GturboError(rc, self.lib.gt_last_error(None).decode())
+        self.h = h
+        self.stream = stream if stream is not None else torch.cuda.current_stream(self.device)
+        self._check(self.lib.gt_set_stream(self.h, ctypes.c_void_p(self.stream.cuda_stream)))
+        info = GtInfo()
+        self._check(self.lib.gt_get_info(self.h, ctypes.byref(info)))
+        self.info = info
+        self.nf = info.nf
+
+    # -- bookkeeping ---------------------------------------------------------------------
+    def _check(self, rc: int) -> None:
+        _lib.check(self.lib, self.h, rc)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.gt_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def field(self) -> torch.Tensor:
+        return torch.zeros((self.n, self.n + 2), dtype=torch.float64, device=self.device)
+
+    def work(self, count: int = 4) -> list[torch.Tensor]:
+        return [self.field() for _ in range(count)]
+
+    def _ptr(self, t: torch.Tensor) -> int:
+        if t.dtype != torch.float64 or not t.is_cuda or not t.is_contiguous():
+            raise ValueError("fields must be contiguous float64 CUDA tensors")
+        if t.numel() != (self.n + 2) * self.n:
+            raise ValueError(f"field has {t.numel()} values, expected (N+2)*N = {(self.n + 2) * self.n}")
+        return t.data_ptr()
+
+    def forcing_modes(self):
+        ik = (ctypes.c_int32 * 2048)()
+        jk = (ctypes.c_int32 * 2048)()
+        nf = ctypes.c_int32()
+        self._check(self.lib.gt_get_forcing_modes(self.h, ik, jk, ctypes.byref(nf)))
+        return np.array(ik[:nf.value], np.int32), np.array(jk[:nf.value], np.int32)
+
+    def sync(self) -> None:
+        self._check(self.lib.gt_sync(self.h))
+
+    # -- the reference's routines -----------------------------------------------------------
+    def fft_dir(self, z: torch.Tensor) -> None:
+        self._check(self.lib.gt_fft_dir(self.h, self._ptr(z)))
+
+    def fft_inv(self, z: torch.Tensor) -> None:
+        self._check(self.lib.gt_fft_inv(self.h, self._ptr(z)))
+
+    def trunc(self, z: torch.Tensor) -> None:
+        self._check(self.lib.gt_trunc(self.h, self._ptr(z)))
+
+    def produ(self, z, u, v) -> None:
+        self._check(self.lib.gt_produ(self.h, self._ptr(z), self._ptr(u), self._ptr(v)))
+
+    def nlt(self, z, u, v) -> None:
+        self._check(self.lib.gt_nlt(self.h, self._ptr(z), self._ptr(u), self._ptr(v)))
+
+    def step(self, z, znl, u, v) -> None:
+        self._check(self.lib.gt_step_rk2(self.h, self._ptr(z), self._ptr(znl), self._ptr(u), self._ptr(v)))
+
+    def step4(self, z, znl, znew, u, v) -> None:
+        self._check(self.lib.gt_step_rk4(self.h, self._ptr(z), self._ptr(znl), self._ptr(znew),
+                                         self._ptr(u), self._ptr(v)))
+
+    def rk_step(self, z, work) -> None:
+        """``step4`` when rko=4, else ``step`` (src/main.f90:100-104). work = [znl, znew, u, v]."""
+        znl, znew, u, v = work
+        if self.info.rko == 4:
+            self.step4(z, znl, znew, u, v)
+        else:
+            self.step(z, znl, u, v)
+
+    def forcing(self, z, seed: int) -> int:
+        """Adds one kick; returns the LCG state after the nf draws."""
+        s = ctypes.c_int32(int(seed))
+        self._check(self.lib.gt_forcing(self.h, self._ptr(z), ctypes.byref(s)))
+        return s.value
+
+    def diag(self, z, znl=None) -> dict:
+        """spectrum / fluxes / glob of src/diagnostics.f90 (synchronous)."""
+        nb = self.n // 2
+        out = {k: np.zeros(nb) for k in ("sp", "sz")}
+        glob = np.zeros(6)
+        dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        if znl is not None:
+            out["fle"], out["flz"] = np.zeros(nb), np.zeros(nb)
+            rc = self.lib.gt_diag(self.h, self._ptr(z), self._ptr(znl), dp(out["sp"]), dp(out["sz"]),
+                                  dp(out["fle"]), dp(out["flz"]), dp(glob))
+        else:
+            rc = self.lib.gt_diag(self.h, self._ptr(z), None, dp(out["sp"]), dp(out["sz"]),
+                                  None, None, dp(glob))
+        self._check(rc)
+        out["glob"] = glob
+        return out
+
+    def main_step(self, z, seed: int, work, diag: bool = False):
+        """One iteration of src/main.f90:97-137 (step, diagnostics when asked, forcing)."""
+        self.rk_step(z, work)
+        out = None
+        if diag:
+            znl, _, u, v = work
+            with torch.cuda.stream(self.stream):
+                znl.copy_(z)
+            self.nlt(znl, u, v)
+            out = self.diag(z, znl)
+        seed = self.forcing(z, seed)
+        return seed, out

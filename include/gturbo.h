@@ -1,0 +1,146 @@
+/*
+ * gturbo.h -- C-ABI of the GB300-native time-stepping hot path of the Gturbo
+ * 2D alpha-turbulence pseudo-spectral solver.
+ *
+ * Every entry point replaces one Fortran external of the reference (implicit
+ * interface, arrays `present` on the device) and keeps its argument meaning:
+ * the caller owns every field, passes DEVICE pointers to them (Fortran:
+ * `!$acc host_data use_device(z,...)`), and the library owns only its tables
+ * (wavenumbers, integrating factor, forcing list, twiddles).
+ *
+ * Memory layout of a field (identical to the reference):
+ *   spectral  complex(8) z(N/2+1, N)  -> C: double z[N][N/2+1][2], kx fastest
+ *   physical  real(8)    z(N+2, N)    -> C: double z[N][N+2], x fastest,
+ *                                        2 padding doubles per row
+ * Both views are the same NS = (N+2)*N doubles (src/modules.f90:4-9).
+ *
+ * Every function returns GT_OK (0) or a GT_ERR_* code; the message of the last
+ * failure is returned by gt_last_error(h) (or gt_last_error(NULL) for a failed
+ * gt_create). No C++ exception crosses this boundary.
+ *
+ * All work is enqueued on the handle's stream (gt_set_stream, default: the
+ * legacy default stream) and is asynchronous unless stated otherwise.
+ */
+#ifndef GTURBO_H
+#define GTURBO_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GT_OK 0
+#define GT_ERR_ARG 1      /* invalid argument or parameter                  */
+#define GT_ERR_CUDA 2     /* a CUDA runtime call failed                      */
+#define GT_ERR_NFORC 3    /* more forced modes than GT_NFORC ('NFORC too small !') */
+#define GT_ERR_STATE 4    /* wrong call order / handle state                 */
+#define GT_ERR_NOMEM 5    /* device or host allocation failed                */
+#define GT_ERR_NONFINITE 6 /* a diagnostic reduction found NaN/Inf           */
+
+/* Capacity of the forced-mode table: commforc NFORC (src/modules.f90:41). */
+#define GT_NFORC 2048
+
+/* Runtime parameters: the contents of params.dat (src/inieuler.f90:13-20)
+ * plus the compile-time grid size NX=NY (src/modules.f90:4). */
+typedef struct gt_params {
+  int32_t n;        /* NX = NY, a power of two in [16, 8192]                */
+  int32_t rko;      /* Runge-Kutta order, 2 or 4 (anything else -> 2, as inieuler.f90:241-243) */
+  int32_t truncate; /* 1 = 2/3-rule dealiasing (trunc), 0 = none           */
+  int32_t split;    /* -1 = derive as inieuler.f90:22-36; 0/1 = force     */
+  double xlx, xly;  /* box lengths                                          */
+  double nu, alpnu; /* hyperviscosity nu * k^(2 alpnu)                       */
+  double mu, alpmu; /* friction mu * k^(2 alpmu)                            */
+  double alpv;      /* alpha: psi_hat = -q_hat / |k|^alpha                  */
+  double dt;        /* time step                                            */
+  double rtrunc;    /* truncation radius as written in params.dat (unsquared) */
+  double famp, k1f, k2f; /* forcing amplitude and shell k1f < |k| <= k2f     */
+} gt_params;
+
+/* Derived quantities of a handle (read-only). */
+typedef struct gt_info {
+  int32_t n, nh;        /* N and N/2+1                                       */
+  int32_t nbin;         /* NBIN = N/2 (src/modules.f90:9)                    */
+  int32_t rko, split, truncate;
+  int32_t nf;           /* number of forced modes (iniforcing)              */
+  int32_t pad_;
+  int64_t field_doubles;/* NS = (N+2)*N                                      */
+  double dkx, dky;
+  double inpz, inpe;    /* mean enstrophy / energy input (iniforcing.f90:28-29) */
+  double fkxsmax, fkysmax, rtrunc2;
+} gt_info;
+
+typedef struct gt_handle gt_handle;
+
+/* ---- set-up ------------------------------------------------------------ */
+
+/* Replaces the set-up half of inieuler (src/inieuler.f90:22-87): derives
+ * split, dt2/dt3/dt6/sdt, runs defk (src/defk.f90:1-76) and iniforcing
+ * (src/iniforcing.f90:1-80), and uploads the tables to the current device.
+ * Returns GT_ERR_NFORC where the reference stops with 'NFORC too small !'. */
+int gt_create(const gt_params* p, gt_handle** out);
+int gt_destroy(gt_handle* h);
+/* Stream for all later work; NULL = legacy default stream. */
+int gt_set_stream(gt_handle* h, void* cuda_stream);
+int gt_get_info(const gt_handle* h, gt_info* info);
+/* Forced-mode table (iniforcing.f90: ikxf, ikyf; 0-based here). Host arrays
+ * of capacity GT_NFORC. */
+int gt_get_forcing_modes(const gt_handle* h, int32_t* ikxf, int32_t* ikyf, int32_t* nf);
+/* Message of the last failure on h (h == NULL: last gt_create failure). */
+const char* gt_last_error(const gt_handle* h);
+/* Synchronise the handle's stream; returns any pending asynchronous error. */
+int gt_sync(gt_handle* h);
+
+/* ---- spectral transforms (src/fft_dir.f90, src/fft_inv.f90) ------------ */
+
+/* In-place 2D real-to-complex FFT of the physical field followed by the
+ * division by NY*NX of every value, padding included (src/fft_dir.f90:11-21). */
+int gt_fft_dir(gt_handle* h, double* z);
+/* In-place unnormalised 2D complex-to-real FFT (src/fft_inv.f90:11-13). The
+ * imaginary parts of the kx=0 and kx=N/2 values after the y-transform are
+ * taken as zero (Hermitian input); the 2 padding doubles per row are zeroed. */
+int gt_fft_inv(gt_handle* h, double* z);
+/* 2/3-rule ellipse mask and zero mean, in place (src/trunc.f90:10-25). */
+int gt_trunc(gt_handle* h, double* z);
+/* Physical-space products u <- z*u, v <- z*v, padding zeroed (src/produ.f90:11-23). */
+int gt_produ(gt_handle* h, const double* z, double* u, double* v);
+
+/* ---- nonlinear term and time steppers ---------------------------------- */
+
+/* Nonlinear term (src/nlt.f90:1-66): on return z holds N_hat = -i k.(u q)^,
+ * truncated when truncate=1. z's input is destroyed as in the reference; u and
+ * v are scratch fields of NS doubles each. */
+int gt_nlt(gt_handle* h, double* z, double* u, double* v);
+/* Lawson RK2 step (src/rkstep.f90:2-76); znl, u, v are scratch. */
+int gt_step_rk2(gt_handle* h, double* z, double* znl, double* u, double* v);
+/* Lawson RK4 step (src/rkstep.f90:82-131); znl, znew, u, v are scratch. */
+int gt_step_rk4(gt_handle* h, double* z, double* znl, double* znew, double* u, double* v);
+
+/* ---- stochastic forcing (src/forcing.f90:1-51) -------------------------- */
+
+/* Adds one white-in-time random-phase kick to the nf forced modes. *seed is
+ * the caller's LCG state (host int32, as the Fortran `seed` variable):
+ * it is read, and on return holds the state after nf draws. The phases are
+ * bit-identical to the reference's serial rann() sequence. */
+int gt_forcing(gt_handle* h, double* z, int32_t* seed);
+/* The reference's rann (src/forcing.f90:40-51) on the host: advances *seed
+ * once and returns the real(4) draw. Exported for drivers and tests. */
+float gt_rann(int32_t* seed);
+
+/* ---- diagnostics (src/diagnostics.f90:5-179) --------------------------- */
+
+/* Shell spectra, fluxes and global budgets of z (and of znl = nlt(z) for the
+ * fluxes). z, znl: device fields. Outputs are HOST arrays of NBIN doubles:
+ *   sp, sz   energy / enstrophy spectra, already divided by dk (spectrum)
+ *   fle, flz energy / enstrophy flux Pi(k) = suffix sums (fluxes)
+ *   glob[6]  = { ee, zz, disz_nu, disz_mu, dise_nu, dise_mu } (glob)
+ * Any output pointer may be NULL to skip it. Synchronous (returns once the
+ * host arrays are filled). Reductions are deterministic (fixed order). */
+int gt_diag(gt_handle* h, const double* z, const double* znl,
+            double* sp, double* sz, double* fle, double* flz, double* glob);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GTURBO_H */

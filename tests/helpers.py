@@ -1,0 +1,31 @@
+"""Shared helpers of the test suite (fields, comparisons)."""
+import numpy as np
+
+from oracle.coracle import Oracle, spec
+
+
+def rand_field(orc: Oracle, seed: int, truncate: bool = True, hermitian: bool = True) -> np.ndarray:
+    """A random spectral field in the (N, N+2) layout, from the oracle's fft_dir of a real field."""
+    n = orc.n
+    rng = np.random.default_rng(seed)
+    a = np.zeros((n, n + 2))
+    a[:, :n] = rng.standard_normal((n, n))
+    orc.fft_dir(a)
+    if not hermitian:
+        s = spec(a)
+        s[:, 0] += 1e-3 * (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    if truncate:
+        orc.trunc(a)
+    return a
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
+
+
+def phys(a: np.ndarray) -> np.ndarray:
+    """The N x N physical values of an (N, N+2) field (padding dropped)."""
+    return a[:, : a.shape[0]]

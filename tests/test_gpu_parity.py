@@ -1,0 +1,230 @@
+"""Parity of every C-ABI routine against the CPU oracle (same seeded inputs).
+
+Tolerance: relative L2 <= 1e-12 (the single-step bound of the specification); integer and
+mask work (trunc, forcing's LCG state, forced-mode table) must match exactly.
+"""
+import numpy as np
+import pytest
+
+from gturbo_gb300.params import Params
+from oracle.coracle import Oracle, spec
+from tests.helpers import phys, rand_field, rel_l2
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+SIZES = [16, 32, 64, 128, 256, 512]
+
+
+def _solver(p):
+    from gturbo_gb300.solver import Solver
+    return Solver(p)
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def _params(n, **kw):
+    base = dict(n=n, alpv=2.0, rko=4, k1f=3.0, k2f=5.0, nu=1e-12, alpnu=4.0, mu=0.05, dt=1e-3)
+    base.update(kw)
+    return Params(**base)
+
+
+@pytest.mark.parametrize("n", SIZES + [1024, 2048])
+def test_fft_inv(n):
+    p = _params(n)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 1)
+    ref = a.copy()
+    orc.fft_inv(ref)
+    z = _dev(a)
+    sol.fft_inv(z)
+    out = _host(z)
+    assert rel_l2(phys(out), phys(ref)) < TOL
+    assert np.all(out[:, n:] == 0.0)
+
+
+@pytest.mark.parametrize("n", SIZES + [1024, 2048])
+def test_fft_dir(n):
+    p = _params(n)
+    orc, sol = Oracle(p), _solver(p)
+    rng = np.random.default_rng(2)
+    a = np.zeros((n, n + 2))
+    a[:, :n] = rng.standard_normal((n, n))
+    ref = a.copy()
+    orc.fft_dir(ref)
+    z = _dev(a)
+    sol.fft_dir(z)
+    assert rel_l2(_host(z), ref) < TOL
+
+
+@pytest.mark.parametrize("n", [16, 64, 256, 1024])
+def test_trunc_exact(n):
+    p = _params(n)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 3, truncate=False)
+    ref = a.copy()
+    orc.trunc(ref)
+    z = _dev(a)
+    sol.trunc(z)
+    assert np.array_equal(_host(z), ref)
+
+
+def test_produ_exact():
+    n = 64
+    p = _params(n)
+    orc, sol = Oracle(p), _solver(p)
+    rng = np.random.default_rng(4)
+    z, u, v = (rng.standard_normal((n, n + 2)) for _ in range(3))
+    ru, rv = u.copy(), v.copy()
+    orc.produ(z, ru, rv)
+    du, dv = _dev(u), _dev(v)
+    sol.produ(_dev(z), du, dv)
+    assert np.array_equal(_host(du), ru) and np.array_equal(_host(dv), rv)
+
+
+@pytest.mark.parametrize("n", SIZES + [1024])
+@pytest.mark.parametrize("alpv", [0.5, 1.0, 2.0, 3.0])
+def test_nlt(n, alpv):
+    p = _params(n, alpv=alpv)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 5)
+    ref = a.copy()
+    orc.nlt(ref)
+    z, u, v = _dev(a), sol.field(), sol.field()
+    sol.nlt(z, u, v)
+    assert rel_l2(_host(z), ref) < TOL
+
+
+@pytest.mark.parametrize("n", [32, 256])
+def test_nlt_untruncated_input(n):
+    """A field with modes outside the 2/3 ellipse must give the reference's result too."""
+    p = _params(n)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 6, truncate=False)
+    ref = a.copy()
+    orc.nlt(ref)
+    z, u, v = _dev(a), sol.field(), sol.field()
+    sol.nlt(z, u, v)
+    assert rel_l2(_host(z), ref) < TOL
+    # and a truncated field right after it (the flag must have been cleared)
+    b = rand_field(orc, 7)
+    ref = b.copy()
+    orc.nlt(ref)
+    z = _dev(b)
+    sol.nlt(z, u, v)
+    assert rel_l2(_host(z), ref) < TOL
+
+
+@pytest.mark.parametrize("n", [32, 256])
+def test_nlt_no_dealiasing(n):
+    p = _params(n, truncate=0)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 8, truncate=False)
+    ref = a.copy()
+    orc.nlt(ref)
+    z, u, v = _dev(a), sol.field(), sol.field()
+    sol.nlt(z, u, v)
+    assert rel_l2(_host(z), ref) < TOL
+
+
+@pytest.mark.parametrize("n,rko,alpv", [(32, 2, 1.0), (64, 4, 2.0), (256, 2, 1.0), (256, 4, 2.0),
+                                        (512, 4, 3.0), (1024, 2, 0.5)])
+def test_step(n, rko, alpv):
+    p = _params(n, rko=rko, alpv=alpv, dt=2e-3)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 9) * 50.0
+    ref = a.copy()
+    orc.rk_step(ref)
+    z = _dev(a)
+    sol.rk_step(z, sol.work())
+    assert rel_l2(_host(z), ref) < TOL
+
+
+def test_step_split_rk2():
+    """alpnu=1, alpmu=0, RK2: the split integrator emkx(i)*emky(j) (rkstep.f90:21-27, 51-57)."""
+    p = _params(128, rko=2, alpnu=1.0, alpmu=0.0, nu=1e-3)
+    orc, sol = Oracle(p), _solver(p)
+    assert orc.info.split == 1 and sol.info.split == 1
+    a = rand_field(orc, 10)
+    ref = a.copy()
+    orc.rk_step(ref)
+    z = _dev(a)
+    sol.rk_step(z, sol.work())
+    assert rel_l2(_host(z), ref) < TOL
+
+
+@pytest.mark.parametrize("n,k1,k2", [(64, 3.0, 5.0), (256, 10.0, 12.0), (2048, 20.0, 22.0)])
+def test_forcing(n, k1, k2):
+    p = _params(n, k1f=k1, k2f=k2, famp=0.7)
+    orc, sol = Oracle(p), _solver(p)
+    ik, jk = orc.forcing_modes()
+    gik, gjk = sol.forcing_modes()
+    assert np.array_equal(ik, gik) and np.array_equal(jk, gjk)
+    assert sol.info.nf == orc.info.nf and sol.info.inpe == pytest.approx(orc.info.inpe, rel=1e-15)
+    a = rand_field(orc, 11)
+    seed = 481929
+    ref = a.copy()
+    z = _dev(a)
+    for _ in range(3):
+        seed_ref = orc.forcing(ref, seed)
+        seed_gpu = sol.forcing(z, seed)
+        assert seed_ref == seed_gpu
+        seed = seed_ref
+    out = _host(z)
+    assert np.abs(out - ref).max() < 1e-14 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("n,alpv", [(64, 2.0), (256, 1.0), (512, 0.5)])
+def test_diag(n, alpv):
+    p = _params(n, alpv=alpv, nu=1e-20, alpnu=8.0)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 12)
+    b = a.copy()
+    orc.nlt(b)
+    ref = orc.diag(a, b)
+    out = sol.diag(_dev(a), _dev(b))
+    for k in ("sp", "sz", "glob"):
+        assert rel_l2(out[k], ref[k]) < 1e-13, k
+    for k in ("fle", "flz"):
+        scale = np.abs(ref[k]).max()
+        assert np.abs(out[k] - ref[k]).max() <= 1e-12 * scale, k
+
+
+def test_main_loop_10_steps():
+    """10 iterations of the main loop (step, diagnostics every 5, forcing) at 256^2, RK4."""
+    from gturbo_gb300.params import config
+    p = config("c1")
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 13)
+    ref = a.copy()
+    z = _dev(a)
+    work = sol.work()
+    s_ref = s_gpu = 481929
+    for it in range(1, 11):
+        s_ref, d_ref = orc.main_step(ref, s_ref, diag=(it % 5 == 0))
+        s_gpu, d_gpu = sol.main_step(z, s_gpu, work, diag=(it % 5 == 0))
+        assert s_ref == s_gpu
+        if d_ref is not None:
+            assert rel_l2(d_gpu["sp"], d_ref["sp"]) < 1e-11
+    assert rel_l2(_host(z), ref) < 1e-11
+
+
+def test_step_2048_rk2_headline():
+    """One RK2 step of the 2048^2 alpha=1 workload against the oracle."""
+    from gturbo_gb300.params import config
+    p = config("c2")
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 14) * 1e3
+    ref = a.copy()
+    orc.rk_step(ref)
+    z = _dev(a)
+    sol.rk_step(z, sol.work())
+    assert rel_l2(_host(z), ref) < TOL
