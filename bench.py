@@ -1,0 +1,435 @@
+#!/usr/bin/env python3
+"""Benchmark of the Gturbo time-stepping hot path on GB300.
+
+Workload (default ``--config c2``): the 2048^2 SQG-like run -- alpha=1, Lawson RK2, dt=2e-4,
+hyperviscosity (2/3 N/2)^-16 k^16, drag mu=0.1, stochastic forcing on 20 < |k| <= 22 with
+injection rate 1 (the reference's LCG, seed 481929), diagnostics (spectra, fluxes, budgets) every
+100 steps, random-phase initial field with E(k) ~ k^4 exp(-(k/10)^2), E=0.5. Inputs are synthetic
+and resident in HBM; the working set (4 fields + 2 tables, ~168 MB) exceeds the 126 MB L2, so no
+flush is needed between steps.
+
+A "step" is one iteration of the reference's main loop (src/main.f90:97-137): the RK step,
+the diagnostics when ipas % imix == 0, and the forcing kick.
+
+Arms:
+  default            the CUDA path (gturbo_gb300) -> one JSON line on rank 0
+  --impl reference   the reference's algorithm on the host cores (the C oracle, all threads)
+Multi-GPU (torchrun): every rank advances its own independent replica (no collective on the
+data path); the barrier + max-over-ranks timing gives the whole-job throughput.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "steps/s @2048² FP64 vs ref; batched member-steps/s vs plain; adjoint/fwd time"
+SEED = 481929  # src/seed.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU-baseline sample budget")
+    ap.add_argument("--no-extras", action="store_true", help="skip e2e / cpu / ref-equivalent legs")
+    return ap.parse_args()
+
+
+def workload(name):
+    from gturbo_gb300.params import IC_K0, config
+
+    p = config(name)
+    desc = (f"{name}: {p.n}^2 alpha={p.alpv:g} RK{p.rko} dt={p.dt:g} nu={p.nu:.3e} k^{2 * p.alpnu:g} "
+            f"mu={p.mu:g} forcing {p.k1f:g}<|k|<={p.k2f:g} eps=1 (famp={p.famp:.6f}) "
+            f"IC k0={IC_K0[name]:g} E=0.5, diagnostics every {p.imix} steps")
+    return p, IC_K0[name], desc
+
+
+# ---------------------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception as e:  # nvidia-smi missing: report no clocks
+            log("clock sampler unavailable:", e)
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------------------
+# CPU baseline: the C oracle (the reference's algorithm restated) on the host cores
+# ---------------------------------------------------------------------------------------
+def cpu_oracle_run(p, k0, steps, budget_s, threads=None):
+    """Times up to `steps` main-loop iterations of the oracle within ~budget_s seconds."""
+    import numpy as np
+
+    from gturbo_gb300.ic import random_phase_ic
+    from oracle import coracle
+
+    if threads:
+        coracle.set_num_threads(threads)
+    orc = coracle.Oracle(p)
+    z = random_phase_ic(p, k0, 0.5, seed=1)
+    work = [orc.zeros() for _ in range(4)]
+    seed = SEED
+    t0 = time.perf_counter()
+    seed, _ = orc.main_step(z, seed, work=work)  # warm-up + calibration
+    t1 = time.perf_counter() - t0
+    k = max(1, min(steps, int(budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    for ipas in range(1, k + 1):
+        seed, _ = orc.main_step(z, seed, diag=(ipas % p.imix == 0), work=work)
+    dt = time.perf_counter() - t0
+    assert np.isfinite(z).all()
+    return {"value": k / dt, "unit": "steps/s", "cores": coracle.num_threads(), "kind": "port",
+            "sample": f"{k} main-loop steps of the {p.n}^2 workload (RK{p.rko} + forcing"
+                      f"{', diagnostics every ' + str(p.imix) if k >= p.imix else ''}), "
+                      f"C oracle with OpenMP"}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    p, k0, desc = workload(args.config)
+    budget = max(10.0, min(120.0, args.cpu_seconds * 3))
+    res = cpu_oracle_run(p, k0, args.steps, budget)
+    line = {"metric": METRIC, "value": res["value"], "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / res["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": desc},
+            "cpu_baseline": res,
+            "e2e": {"value": res["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------------------
+# the CUDA path
+# ---------------------------------------------------------------------------------------
+def fp64_gemm_tflops(torch, dev):
+    """Measured FP64 peak proxy: cuBLAS DGEMM 4096^3, best of 3."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def pass_model(p, kind):
+    """Algorithmic FLOPs and HBM bytes of one launch of a pass of the nonlinear term.
+
+    FLOPs follow the FFT convention 5 L log2 L per complex length-L transform (2.5 L log2 L per
+    real one) and count the unpruned work of the reference's 5 cuFFT transforms per nlt.
+    Bytes count every field touched once (S = 16 N (N/2+1)): A reads q and writes 3 fields,
+    B reads 3 and writes 2, C reads 2 fields and the RK2 stage reads z and writes one field.
+    """
+    n = p.n
+    nh = n // 2 + 1
+    S = 16 * n * nh
+    lg = math.log2(n)
+    if kind == "nlt_colinv":
+        return 3 * nh * 5 * n * lg, 4 * S
+    if kind == "nlt_row":
+        return 5 * n * 2.5 * n * lg, 5 * S
+    if kind == "nlt_colfwd":
+        return 2 * nh * 5 * n * lg, 4 * S
+    return None, None
+
+
+def ours_arm(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from gturbo_gb300.ic import random_phase_ic
+    from gturbo_gb300.solver import Solver
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    p, k0, desc = workload(args.config)
+    K, W = args.steps, max(3, args.warmup)
+    sol = Solver(p, device=local)
+    stream = sol.stream
+    work = sol.work()
+    z0 = torch.from_numpy(random_phase_ic(p, k0, 0.5, seed=1 + rank)).to(dev)
+    z = z0.clone()
+    seed = SEED
+    # warm-up (including one diagnostics pass)
+    for it in range(W):
+        seed, _ = sol.main_step(z, seed, work, diag=(it == W - 1))
+    torch.cuda.synchronize()
+
+    # ---- timed region: K main-loop steps, diagnostics every imix ----------------------
+    z.copy_(z0)
+    seed = SEED
+    torch.cuda.synchronize()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    ndiag = 0
+    for ipas in range(1, K + 1):
+        d = ipas % p.imix == 0
+        ndiag += d
+        seed, out = sol.main_step(z, seed, work, diag=d)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3
+    t_all = t
+    if world > 1:
+        tt = torch.tensor([t], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_all = float(tt.item())
+        barrier()
+    finite = bool(torch.isfinite(z).all().item())
+    value = K * world / t_all
+    stages = 4 if p.rko == 4 else 2
+    launches = K * (3 * stages + 1) + ndiag * (3 + 5)
+
+    extras = {}
+    if rank == 0:
+        # ---- per-kernel CUDA-event timing (same workload, separate pass) ---------------
+        kp = min(K, 100)
+        sol.profile(True)
+        for ipas in range(1, kp + 1):
+            seed, _ = sol.main_step(z, seed, work, diag=(ipas % p.imix == 0))
+        prof = sol.profile_read()
+        sol.profile(False)
+        tot = sum(v[0] for v in prof.values())
+        kernels = {k: {"ms_per_launch": (v[0] / v[1]) if v[1] else None, "launches": v[1],
+                       "share": v[0] / tot if tot else None} for k, v in prof.items() if v[1]}
+        top = max(kernels, key=lambda k: kernels[k]["share"])
+        peaks, src = measured_peaks()
+        fp64 = fp64_gemm_tflops(torch, dev)
+        fl, by = pass_model(p, top)
+        ms = kernels[top]["ms_per_launch"]
+        roof = {"kernel": top, "bound": "fp64",
+                "achieved": fl / (ms / 1e3) / 1e12 if fl else None, "unit": "TFLOP/s",
+                "peak": fp64, "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
+                "(FP64 pipe; MEASURED_PEAKS.json has no FP64 figure)",
+                "traffic": None,
+                "hbm_achieved_gbs": by / (ms / 1e3) / 1e9 if by else None,
+                "hbm_peak_gbs": peaks.get("hbm_gbs"), "hbm_peak_source": src}
+        roof["frac"] = roof["achieved"] / fp64 if roof["achieved"] else None
+        if roof["hbm_achieved_gbs"] and roof["hbm_peak_gbs"]:
+            roof["hbm_frac"] = roof["hbm_achieved_gbs"] / roof["hbm_peak_gbs"]
+        extras["roofline"] = roof
+        extras["kernels"] = kernels
+        step_bytes = (26 if p.rko == 2 else 57) * 16 * p.n * (p.n // 2 + 1)
+        extras["step_hbm_gbs"] = step_bytes * value / world / 1e9
+
+        if not args.no_extras:
+            # ---- no-diagnostics throughput (the comparison with the cuFFT baseline) ----
+            z.copy_(z0)
+            torch.cuda.synchronize()
+            kn = min(K, 100)
+            e0.record(stream)
+            for _ in range(kn):
+                seed, _ = sol.main_step(z, seed, work, diag=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ours_nodiag = kn / (e0.elapsed_time(e1) / 1e3)
+
+            # ---- end to end through the public API, host buffers every step ------------
+            host = torch.from_numpy(random_phase_ic(p, k0, 0.5, seed=1)).pin_memory()
+            res_host = torch.empty_like(host).pin_memory()
+            ke = min(K, 100)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e0.record(stream)
+            for ipas in range(1, ke + 1):
+                with torch.cuda.stream(stream):
+                    z.copy_(host, non_blocking=True)
+                seed, _ = sol.main_step(z, seed, work, diag=(ipas % p.imix == 0))
+                with torch.cuda.stream(stream):
+                    res_host.copy_(z, non_blocking=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            te = max(e0.elapsed_time(e1) / 1e3, 0.0)
+            te_wall = time.perf_counter() - t0
+            nbytes = host.numel() * 8
+            extras["e2e"] = {"value": ke / max(te, te_wall), "unit": "steps/s",
+                             "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                             "steps": ke, "note": "per step: pinned H2D of the field, main-loop "
+                             "step through gturbo_gb300.Solver (C-ABI), D2H of the field"}
+
+            # ---- reference-equivalent GPU build (cuFFT + unfused kernels) --------------
+            try:
+                extras["ref_gpu_equivalent"] = refeq_run(p, k0, kn, W, dev, torch)
+                extras["ref_gpu_equivalent"]["ours_nodiag_steps_s"] = ours_nodiag
+                extras["ref_gpu_equivalent"]["speedup_nodiag"] = (
+                    ours_nodiag / extras["ref_gpu_equivalent"]["value"])
+            except Exception as e:  # reported, never fatal
+                extras["ref_gpu_equivalent"] = {"unavailable": str(e)[:200]}
+
+            # ---- CPU baseline (the oracle on the host cores) ---------------------------
+            try:
+                extras["cpu_baseline"] = cpu_oracle_run(p, k0, 10 ** 6, args.cpu_seconds)
+            except Exception as e:
+                extras["cpu_baseline"] = {"unavailable": str(e)[:200]}
+        if "e2e" not in extras:
+            extras["e2e"] = {"value": None, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                             "d2h_bytes_per_step": 0, "note": "skipped (--no-extras)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": K,
+                "warmup": W, "ms_per_step": 1e3 * t_all / K, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (random-phase IC, reference LCG forcing, seed 481929)",
+                "config": {"workload": desc, "n": p.n, "alpha": p.alpv, "rk": p.rko,
+                           "imix": p.imix, "diag_calls_timed": ndiag,
+                           "parallelism": f"replicas x{world}" if world > 1 else "single",
+                           "l2": "no flush: working set ~168 MB > 126 MB L2"},
+                "gpu_launches": launches, "finite": finite, "clocks": clk}
+        line.update(extras)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def refeq_run(p, k0, steps, warm, dev, torch):
+    """The reference-equivalent cuFFT build: steps/s of step + forcing (no diagnostics)."""
+    import ctypes
+
+    from baseline import build as bb
+    from gturbo_gb300.ic import random_phase_ic
+
+    lib = ctypes.CDLL(bb.build())
+    P = ctypes.c_void_p
+    lib.re_create.argtypes = [ctypes.c_void_p, ctypes.POINTER(P)]
+    lib.re_set_stream.argtypes = [P, P]
+    lib.re_step.argtypes = [P, P, P, P, P, P]
+    lib.re_forcing.argtypes = [P, P]
+    lib.re_set_seed.argtypes = [P, ctypes.c_int32]
+    lib.re_destroy.argtypes = [P]
+    cp = p.to_ctypes()
+    h = P()
+    rc = lib.re_create(ctypes.byref(cp), ctypes.byref(h))
+    if rc:
+        raise RuntimeError(f"re_create failed: {rc}")
+    stream = torch.cuda.current_stream(dev)
+    lib.re_set_stream(h, P(stream.cuda_stream))
+    z = torch.from_numpy(random_phase_ic(p, k0, 0.5, seed=1)).to(dev)
+    w = [torch.zeros_like(z) for _ in range(4)]
+    ptr = lambda t: P(t.data_ptr())  # noqa: E731
+    lib.re_set_seed(h, SEED)
+    for _ in range(warm):
+        lib.re_step(h, ptr(z), ptr(w[0]), ptr(w[1]), ptr(w[2]), ptr(w[3]))
+        lib.re_forcing(h, ptr(z))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        lib.re_step(h, ptr(z), ptr(w[0]), ptr(w[1]), ptr(w[2]), ptr(w[3]))
+        lib.re_forcing(h, ptr(z))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    finite = bool(torch.isfinite(z).all().item())
+    lib.re_destroy(h)
+    return {"value": steps / t, "unit": "steps/s", "steps": steps, "finite": finite,
+            "what": "cuFFT in-place D2Z/Z2D + one kernel per OpenACC region of the reference "
+                    "(no diagnostics), same GPU, same run"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return ours_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

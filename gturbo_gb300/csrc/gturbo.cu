@@ -60,6 +60,10 @@ struct gt_handle {
   double *d_part = nullptr, *d_rowsum = nullptr, *d_bins = nullptr, *d_fl = nullptr, *d_glob = nullptr;
   double* h_diag = nullptr;  // pinned: bins [nbin*4] + fl [nbin*2] + glob [6]
   cudaError_t (*dispatch)(const GtOp&) = nullptr;
+  // launch timing (gt_profile)
+  bool prof = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<int> ev_kind;  // kind of pair p = events 2p, 2p+1
 };
 
 namespace {
@@ -187,8 +191,37 @@ GtOp base_op(const gt_handle* h) {
   return op;
 }
 
+// Event pair around the next launch when profiling: prof_begin before, prof_end after.
+int prof_begin(gt_handle* h, int kind) {
+  if (!h->prof) return -1;
+  const size_t pair = h->ev_kind.size();
+  while (h->ev_pool.size() < 2 * (pair + 1)) {
+    cudaEvent_t ev;
+    if (cudaEventCreate(&ev) != cudaSuccess) return -1;
+    h->ev_pool.push_back(ev);
+  }
+  h->ev_kind.push_back(kind);
+  cudaEventRecord(h->ev_pool[2 * pair], h->stream);
+  return (int)pair;
+}
+
+void prof_end(gt_handle* h, int pair) {
+  if (pair >= 0) cudaEventRecord(h->ev_pool[2 * pair + 1], h->stream);
+}
+
+int op_class(int kind) {
+  switch (kind) {
+    case gt::OP_NLT_COLINV: return GT_PROF_NLT_COLINV;
+    case gt::OP_NLT_ROW: return GT_PROF_NLT_ROW;
+    case gt::OP_NLT_COLFWD: return GT_PROF_NLT_COLFWD;
+    default: return GT_PROF_OTHER;
+  }
+}
+
 int run(gt_handle* h, const GtOp& op) {
+  const int pair = prof_begin(h, op_class(op.kind));
   cudaError_t e = h->dispatch(op);
+  prof_end(h, pair);
   if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
   return GT_OK;
 }
@@ -392,6 +425,7 @@ int gt_create(const gt_params* p, gt_handle** out) {
 int gt_destroy(gt_handle* h) {
   if (!h) return GT_OK;
   cudaDeviceSynchronize();
+  for (cudaEvent_t ev : h->ev_pool) cudaEventDestroy(ev);
   free_device(h);
   delete h;
   return GT_OK;
@@ -520,9 +554,11 @@ int gt_forcing(gt_handle* h, double* z, int32_t* seed) {
   if (h->nf == 0) return GT_OK;
   const uint32_t x0 = (uint32_t)(*seed);
   const double sf = h->sdt * h->p.famp;
+  const int pair = prof_begin(h, GT_PROF_FORCING);
   gt::k_forcing<<<(h->nf + 127) / 128, 128, 0, h->stream>>>(
       reinterpret_cast<double2*>(z), h->NH, h->nf, h->d_ikxf, h->d_ikyf, h->d_jc, h->d_lcga,
       h->d_lcgb, h->d_ff, x0, sf);
+  prof_end(h, pair);
   GT_CUDA(h, cudaGetLastError());
   *seed = (int32_t)((h->lcga_nf * x0 + h->lcgb_nf) & 0x7FFFFFFFu);
   return GT_OK;
@@ -553,6 +589,7 @@ int gt_diag(gt_handle* h, const double* z, const double* znl, double* sp, double
   double* hf = hb + (size_t)nb * 4;
   double* hg = hf + (size_t)nb * 2;
   const bool want_bins = sp || sz || fle || flz;
+  const int pair = prof_begin(h, GT_PROF_DIAG);
   if (want_bins) {
     const int ngroups = (h->N + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
     const int nthr = ngroups * nb;
@@ -572,6 +609,7 @@ int gt_diag(gt_handle* h, const double* z, const double* znl, double* sp, double
     GT_CUDA(h, cudaGetLastError());
     GT_CUDA(h, cudaMemcpyAsync(hg, h->d_glob, sizeof(double) * 6, cudaMemcpyDeviceToHost, h->stream));
   }
+  prof_end(h, pair);
   GT_CUDA(h, cudaStreamSynchronize(h->stream));
   for (int b = 0; b < nb; ++b) {
     if (sp) sp[b] = hb[b * 4 + 0];
@@ -587,6 +625,29 @@ int gt_diag(gt_handle* h, const double* z, const double* znl, double* sp, double
     }
     if (!finite) return fail(h, GT_ERR_NONFINITE, "gt_diag: non-finite global budget");
   }
+  return GT_OK;
+}
+
+int gt_profile(gt_handle* h, int enable) {
+  if (!h) return fail(nullptr, GT_ERR_ARG, "gt_profile: null handle");
+  h->prof = enable != 0;
+  return GT_OK;
+}
+
+int gt_profile_read(gt_handle* h, double* ms, int64_t* launches) {
+  if (!h || !ms || !launches) return fail(h, GT_ERR_ARG, "gt_profile_read: null argument");
+  GT_CUDA(h, cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < GT_PROF_KINDS; ++k) {
+    ms[k] = 0.0;
+    launches[k] = 0;
+  }
+  for (size_t p = 0; p < h->ev_kind.size(); ++p) {
+    float t = 0.0f;
+    GT_CUDA(h, cudaEventElapsedTime(&t, h->ev_pool[2 * p], h->ev_pool[2 * p + 1]));
+    ms[h->ev_kind[p]] += t;
+    launches[h->ev_kind[p]] += 1;
+  }
+  h->ev_kind.clear();
   return GT_OK;
 }
 

@@ -100,6 +100,19 @@ class Solver:
     def sync(self) -> None:
         self._check(self.lib.gt_sync(self.h))
 
+    PROF_KINDS = ("nlt_colinv", "nlt_row", "nlt_colfwd", "forcing", "diag", "other")
+
+    def profile(self, enable: bool) -> None:
+        """Record CUDA events around every later launch (gt_profile)."""
+        self._check(self.lib.gt_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        """{kind: (total ms, launches)} since the last read (gt_profile_read)."""
+        ms = (ctypes.c_double * 6)()
+        cnt = (ctypes.c_int64 * 6)()
+        self._check(self.lib.gt_profile_read(self.h, ms, cnt))
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(self.PROF_KINDS)}
+
     # -- the reference's routines -----------------------------------------------------------
     def fft_dir(self, z: torch.Tensor) -> None:
         self._check(self.lib.gt_fft_dir(self.h, self._ptr(z)))

@@ -139,6 +139,26 @@ float gt_rann(int32_t* seed);
 int gt_diag(gt_handle* h, const double* z, const double* znl,
             double* sp, double* sz, double* fle, double* flz, double* glob);
 
+/* ---- launch timing (benchmarks) ---------------------------------------- */
+
+/* Kernel classes timed by gt_profile: the three passes of the nonlinear term, the forcing
+ * kick, the diagnostics, and everything else (transforms, trunc, produ). */
+#define GT_PROF_NLT_COLINV 0
+#define GT_PROF_NLT_ROW 1
+#define GT_PROF_NLT_COLFWD 2
+#define GT_PROF_FORCING 3
+#define GT_PROF_DIAG 4
+#define GT_PROF_OTHER 5
+#define GT_PROF_KINDS 6
+
+/* No counterpart in the reference (its only timer is a wall clock around the whole run,
+ * src/main.f90:191-193). enable=1: record a CUDA event pair on the handle's stream around
+ * every later kernel launch; enable=0: stop. */
+int gt_profile(gt_handle* h, int enable);
+/* Synchronises the stream, returns per class the summed kernel time (ms) and the number of
+ * launches since the last read, and resets both. ms, launches: GT_PROF_KINDS entries. */
+int gt_profile_read(gt_handle* h, double* ms, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -228,3 +228,29 @@ def test_step_2048_rk2_headline():
     z = _dev(a)
     sol.rk_step(z, sol.work())
     assert rel_l2(_host(z), ref) < TOL
+
+
+@pytest.mark.parametrize("cfg", ["c1", "c2"])
+def test_spectra_50_step_horizon(cfg):
+    """Spectra, fluxes and budgets within 1e-9 after 50 main-loop steps (forcing from the
+    reference's LCG and seed), from the workload's random-phase initial field."""
+    from gturbo_gb300.ic import random_phase_ic
+    from gturbo_gb300.params import IC_K0, config
+    p = config(cfg)
+    orc, sol = Oracle(p), _solver(p)
+    a = random_phase_ic(p, IC_K0[cfg], 0.5, seed=1)
+    ref = a.copy()
+    z = _dev(a)
+    work = sol.work()
+    owork = [orc.zeros() for _ in range(4)]
+    s_ref = s_gpu = 481929
+    for it in range(1, 51):
+        s_ref, d_ref = orc.main_step(ref, s_ref, diag=(it == 50), work=owork)
+        s_gpu, d_gpu = sol.main_step(z, s_gpu, work, diag=(it == 50))
+    assert s_ref == s_gpu
+    assert np.isfinite(ref).all()
+    for k in ("sp", "sz", "glob"):
+        assert rel_l2(d_gpu[k], d_ref[k]) < 1e-9, k
+    for k in ("fle", "flz"):
+        assert np.abs(d_gpu[k] - d_ref[k]).max() <= 1e-9 * np.abs(d_ref[k]).max(), k
+    assert rel_l2(_host(z), ref) < 1e-10
