@@ -66,6 +66,7 @@ def load(path: str | None = None):
         "gt_forcing": ([P, D, I32P], ctypes.c_int),
         "gt_rann": ([I32P], ctypes.c_float),
         "gt_diag": ([P, D, D, H, H, H, H, H], ctypes.c_int),
+        "gt_diag_static": ([ctypes.POINTER(GtParams), D, D, D, D, D, D, D, P], ctypes.c_int),
         "gt_profile": ([P, ctypes.c_int], ctypes.c_int),
         "gt_profile_read": ([P, H, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     }

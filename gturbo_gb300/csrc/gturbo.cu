@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -652,3 +653,128 @@ int gt_profile_read(gt_handle* h, double* ms, int64_t* launches) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// gt_diag_static: the diagnostics without any device allocation.
+//
+// For callers that cannot allocate device memory: a driver whose device arrays all live in
+// OpenACC data regions (the reference's main program) or in another runtime's memory pool,
+// sized to fill the GPU, and host code that must not call cudaMalloc/cudaFree between time
+// steps, because those calls synchronise the whole device. Such a caller has no gt_handle
+// (gt_create allocates the tables) and passes only its fields and output arrays.
+//
+// The scratch (partial shell sums, per-row budgets, the k^2 tables) is this file-scope device
+// array, present on every GPU that loads the library until the process exits. Host code
+// reaches it only through the address that cudaGetSymbolAddress returns for the current
+// device; the first call on each device looks that address up, so that first call should be
+// made before any stream capture. Every call rewrites all the scratch it reads, so nothing
+// has to start at zero; calls that overlap on the GPU (other streams, other threads) share
+// the array and race.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+constexpr int kStaticMaxN = GT_DIAG_STATIC_MAX_N;
+constexpr int kStaticMaxNH = kStaticMaxN / 2 + 1;
+constexpr int kStaticMaxBin = kStaticMaxN / 2;
+constexpr int kStaticGroups = (kStaticMaxN + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
+constexpr size_t kOffFkxs = 0;
+constexpr size_t kOffFkys = kOffFkxs + ((kStaticMaxNH + 31) / 32) * 32;
+constexpr size_t kOffPart = kOffFkys + kStaticMaxN;
+constexpr size_t kOffRows = kOffPart + (size_t)kStaticGroups * kStaticMaxBin * 4;
+constexpr size_t kOffBins = kOffRows + (size_t)kStaticMaxN * 6;
+constexpr size_t kOffFl = kOffBins + (size_t)kStaticMaxBin * 4;
+constexpr size_t kStaticDoubles = kOffFl + (size_t)kStaticMaxBin * 2;
+
+static __device__ __align__(256) double g_diag_scratch[kStaticDoubles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+double* g_static_ptr[kMaxDevices] = {nullptr};
+
+// (i dkx)^2 and (fky(j))^2 exactly as defk.f90:27-43 forms them.
+__global__ void k_static_k2(double* fkxs, double* fkys, int n, double dkx, double dky) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n / 2 + 1) {
+    const double kx = (double)t * dkx;
+    fkxs[t] = kx * kx;
+  }
+  if (t < n) {
+    const double ky = (double)(t <= n / 2 ? t : t - n) * dky;
+    fkys[t] = ky * ky;
+  }
+}
+
+__global__ void k_static_scatter(const double* bins, const double* fl, double* sp, double* sz,
+                                 double* fle, double* flz, int nbin) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbin) return;
+  if (sp) sp[b] = bins[b * 4 + 0];
+  if (sz) sz[b] = bins[b * 4 + 1];
+  if (fle) fle[b] = fl[b * 2 + 0];
+  if (flz) flz[b] = fl[b * 2 + 1];
+}
+
+}  // namespace
+
+extern "C" int gt_diag_static(const gt_params* p, const double* z, const double* znl, double* sp,
+                              double* sz, double* fle, double* flz, double* glob,
+                              void* cuda_stream) {
+  if (!p || !z) return fail(nullptr, GT_ERR_ARG, "gt_diag_static: null argument");
+  const int n = p->n;
+  if (n < 16 || (n & (n - 1)) || n > kStaticMaxN)
+    return fail(nullptr, GT_ERR_ARG,
+                "gt_diag_static: n must be a power of two in [16, GT_DIAG_STATIC_MAX_N=2048]");
+  if ((fle || flz) && !znl) return fail(nullptr, GT_ERR_ARG, "gt_diag_static: fluxes need znl");
+  if (!(p->xlx > 0.0) || !(p->xly > 0.0))
+    return fail(nullptr, GT_ERR_ARG, "gt_diag_static: xlx and xly must be positive");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "gt_diag_static: cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(nullptr, GT_ERR_ARG, "gt_diag_static: device index");
+  double* base;
+  {
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[dev]) {
+      void* ptr = nullptr;
+      e = cudaGetSymbolAddress(&ptr, g_diag_scratch);
+      if (e != cudaSuccess) return cuda_fail(nullptr, e, "gt_diag_static: cudaGetSymbolAddress");
+      g_static_ptr[dev] = static_cast<double*>(ptr);
+    }
+    base = g_static_ptr[dev];
+  }
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  const int nh = n / 2 + 1, nb = n / 2;
+  gt::DiagArgs D;
+  D.z = reinterpret_cast<const double2*>(z);
+  D.znl = reinterpret_cast<const double2*>(znl);
+  D.fkxs = base + kOffFkxs;
+  D.fkys = base + kOffFkys;
+  D.n = n;
+  D.nh = nh;
+  D.nbin = nb;
+  D.dk = 2.0 * 3.14159265358979323846 / p->xlx;
+  D.alpv = p->alpv;
+  D.nu = p->nu;
+  D.mu = p->mu;
+  D.alpnu = p->alpnu;
+  D.alpmu = p->alpmu;
+  D.part = base + kOffPart;
+  D.rowsum = base + kOffRows;
+  const double dky = 2.0 * 3.14159265358979323846 / p->xly;
+  k_static_k2<<<(n + 127) / 128, 128, 0, s>>>(base + kOffFkxs, base + kOffFkys, n, D.dk, dky);
+  if (sp || sz || fle || flz) {
+    const int ngroups = (n + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
+    gt::k_diag_bins<<<(ngroups * nb + 127) / 128, 128, 0, s>>>(D);
+    gt::k_diag_bins_final<<<(nb + 127) / 128, 128, 0, s>>>(D, base + kOffBins);
+    if (znl) gt::k_diag_suffix<<<(nb + 127) / 128, 128, 0, s>>>(base + kOffBins, base + kOffFl, nb);
+    k_static_scatter<<<(nb + 127) / 128, 128, 0, s>>>(base + kOffBins, base + kOffFl, sp, sz,
+                                                       znl ? fle : nullptr, znl ? flz : nullptr, nb);
+  }
+  if (glob) {
+    gt::k_diag_glob_rows<<<n, 256, 0, s>>>(D);
+    gt::k_diag_glob_final<<<1, 32, 0, s>>>(D, glob);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "gt_diag_static: launch");
+  return GT_OK;
+}

@@ -139,6 +139,28 @@ float gt_rann(int32_t* seed);
 int gt_diag(gt_handle* h, const double* z, const double* znl,
             double* sp, double* sz, double* fle, double* flz, double* glob);
 
+/* Largest grid size gt_diag_static accepts (its scratch is sized for it). */
+#define GT_DIAG_STATIC_MAX_N 2048
+
+/* gt_diag for callers that cannot allocate device memory. No counterpart in
+ * the reference. It serves a driver whose device arrays all live in OpenACC
+ * data regions or in another runtime's memory pool sized to fill the GPU, and
+ * host code that must not call cudaMalloc/cudaFree between steps (they
+ * synchronise the whole device). It needs no gt_handle, allocates nothing and
+ * keeps its scratch (~2.3 MB) in a static device array that every GPU loading
+ * the library holds until the process exits.
+ *   p        the run parameters (n <= GT_DIAG_STATIC_MAX_N, else GT_ERR_ARG)
+ *   z, znl   device fields as for gt_diag
+ *   sp..glob DEVICE output arrays (NBIN doubles; glob 6), any may be NULL
+ *   stream   CUDA stream of the work (NULL = legacy default stream)
+ * Asynchronous: returns after enqueueing. No NaN/Inf check. The first call on
+ * a device looks up the scratch address there, so make it before any stream
+ * capture. All calls share the scratch: calls that overlap on the GPU race.
+ * Errors are reported through gt_last_error(NULL). */
+int gt_diag_static(const gt_params* p, const double* z, const double* znl,
+                   double* sp, double* sz, double* fle, double* flz, double* glob,
+                   void* cuda_stream);
+
 /* ---- launch timing (benchmarks) ---------------------------------------- */
 
 /* Kernel classes timed by gt_profile: the three passes of the nonlinear term, the forcing
