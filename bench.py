@@ -219,6 +219,7 @@ def ours_arm(args):
     import torch.distributed as dist
 
     from gturbo_gb300.ic import random_phase_ic
+    from gturbo_gb300.replicas import replica_ic_seed, whole_job_rate
     from gturbo_gb300.solver import Solver
 
     rank = int(os.environ.get("RANK", "0"))
@@ -238,7 +239,7 @@ def ours_arm(args):
     sol = Solver(p, device=local)
     stream = sol.stream
     work = sol.work()
-    z0 = torch.from_numpy(random_phase_ic(p, k0, 0.5, seed=1 + rank)).to(dev)
+    z0 = torch.from_numpy(random_phase_ic(p, k0, 0.5, seed=replica_ic_seed(rank))).to(dev)
     z = z0.clone()
     seed = SEED
     # warm-up (including one diagnostics pass)
@@ -266,14 +267,9 @@ def ours_arm(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     t = e0.elapsed_time(e1) / 1e3
-    t_all = t
-    if world > 1:
-        tt = torch.tensor([t], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_all = float(tt.item())
-        barrier()
+    _, t_all, value = whole_job_rate(K, t)
+    barrier()
     finite = bool(torch.isfinite(z).all().item())
-    value = K * world / t_all
     stages = 4 if p.rko == 4 else 2
     launches = K * (3 * stages + 1) + ndiag * (3 + 5)
 

@@ -20,8 +20,12 @@ def rand_field(orc: Oracle, seed: int, truncate: bool = True, hermitian: bool = 
 
 
 def rel_l2(a, b) -> float:
-    a = np.asarray(a, dtype=np.float64).ravel()
-    b = np.asarray(b, dtype=np.float64).ravel()
+    a = np.asarray(a).ravel()
+    b = np.asarray(b).ravel()
+    if np.iscomplexobj(a) or np.iscomplexobj(b):
+        a, b = a.astype(np.complex128), b.astype(np.complex128)
+    else:
+        a, b = a.astype(np.float64), b.astype(np.float64)
     nb = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
 

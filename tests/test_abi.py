@@ -1,0 +1,102 @@
+"""CPU tests of the C-ABI boundary: the library loads, exports every function declared in
+include/gturbo.h, its structs have the layout of the header, and the host-only entry points
+behave like the reference (no GPU work is launched here)."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from gturbo_gb300 import _lib, build
+from gturbo_gb300.params import GtInfo, GtParams, Params
+from oracle.coracle import rann
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def test_library_exports_every_header_function(lib):
+    names = _lib.header_functions()
+    assert len(names) >= 20
+    out = subprocess.run(["nm", "-D", "--defined-only", build.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    for n in names:
+        assert hasattr(lib, n)
+
+
+def _c_layout(struct, fields):
+    src = ["#include <stdio.h>", "#include <stddef.h>", '#include "gturbo.h"', "int main(void){",
+           f'printf("%zu\\n", sizeof({struct}));']
+    src += [f'printf("%zu\\n", offsetof({struct}, {f}));' for f in fields]
+    src.append("return 0;}")
+    tmp = os.path.join(build.BUILD, f"layout_{struct}")
+    os.makedirs(build.BUILD, exist_ok=True)
+    with open(tmp + ".c", "w") as f:
+        f.write("\n".join(src))
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), tmp + ".c", "-o", tmp], check=True)
+    vals = [int(x) for x in subprocess.run([tmp], capture_output=True, text=True, check=True).stdout.split()]
+    return vals[0], vals[1:]
+
+
+@pytest.mark.parametrize("ctype,cname", [(GtParams, "gt_params"), (GtInfo, "gt_info")])
+def test_struct_layout_matches_header(ctype, cname):
+    fields = [f for f, _ in ctype._fields_]
+    size, offs = _c_layout(cname, fields)
+    assert size == ctypes.sizeof(ctype)
+    assert offs == [getattr(ctype, f).offset for f in fields]
+
+
+def test_gt_rann_is_the_reference_lcg(lib):
+    s = ctypes.c_int32(481929)
+    got = np.array([lib.gt_rann(ctypes.byref(s)) for _ in range(500)], np.float32)
+    ref, last = rann(481929, 500)
+    assert np.array_equal(got, ref) and s.value == last
+
+
+def test_create_rejects_bad_grid_size(lib):
+    h = ctypes.c_void_p()
+    cp = Params(n=100).to_ctypes()
+    assert lib.gt_create(ctypes.byref(cp), ctypes.byref(h)) == 1
+    assert b"power of two" in lib.gt_last_error(None)
+
+
+def test_create_reports_nforc_overflow(lib):
+    """More than NFORC=2048 forced modes: the reference stops with 'NFORC too small !'
+    (src/iniforcing.f90:22); the C-ABI returns GT_ERR_NFORC before touching the device."""
+    h = ctypes.c_void_p()
+    cp = Params(n=512, k1f=0.0, k2f=60.0).to_ctypes()
+    assert lib.gt_create(ctypes.byref(cp), ctypes.byref(h)) == 3
+    assert b"NFORC" in lib.gt_last_error(None)
+
+
+def test_null_arguments_are_errors_not_crashes(lib):
+    assert lib.gt_create(None, None) == 1
+    assert lib.gt_fft_dir(None, None) == 1
+    assert lib.gt_step_rk2(None, None, None, None, None) == 1
+    assert lib.gt_diag(None, None, None, None, None, None, None, None) == 1
+
+
+def test_read_params_dat_format():
+    from gturbo_gb300.params import read_params_dat
+    text = """6.2831853071795864769d0\t6.2831853071795864769d0
+4.5d-46\t8.0d0\t0.1d0\t0.0d0\t1.0d0
+2.0d-5\t2
+2000\t100000\t100
+0.6666666666666666667d0\t1
+0.4d0\t20.0d0\t22.0d0
+
+xlx   yly
+"""
+    p = read_params_dat(text, 2048)
+    assert p.n == 2048 and p.rko == 2 and p.truncate == 1 and p.imix == 100
+    assert p.nu == 4.5e-46 and p.alpnu == 8.0 and p.alpv == 1.0 and p.dt == 2e-5
+    assert p.xlx == 2 * np.pi and p.k1f == 20.0 and p.famp == 0.4

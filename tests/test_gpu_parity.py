@@ -254,3 +254,50 @@ def test_spectra_50_step_horizon(cfg):
     for k in ("fle", "flz"):
         assert np.abs(d_gpu[k] - d_ref[k]).max() <= 1e-9 * np.abs(d_ref[k]).max(), k
     assert rel_l2(_host(z), ref) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["n32_a2_rk4", "n64_a1_rk2", "n64_a05_rk2_split"])
+def test_against_golden_vectors(name):
+    """The CUDA path against the committed vectors of the numpy restatement."""
+    import os
+    from tests.golden.make_golden import CASES
+    p, _ = CASES[name]
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{name}.npz"))
+    sol = _solver(p)
+    n = p.n
+    a = np.zeros((n, n + 2))
+    a[:, :n] = g["phys_in"]
+    z = _dev(a)
+    sol.fft_dir(z)
+    assert rel_l2(_host(z), g["fft_dir"]) < TOL
+    z = _dev(g["spec_in"])
+    sol.fft_inv(z)
+    assert rel_l2(_host(z)[:, :n], g["fft_inv"]) < TOL
+    z, u, v = _dev(g["spec_in"]), sol.field(), sol.field()
+    sol.nlt(z, u, v)
+    assert rel_l2(_host(z), g["nlt"]) < TOL
+    z = _dev(g["spec_in"])
+    sol.rk_step(z, sol.work())
+    assert rel_l2(_host(z), g["step"]) < TOL
+    z = _dev(g["spec_in"])
+    s = 481929
+    for _ in range(3):
+        s = sol.forcing(z, s)
+    assert s == int(g["forcing3_seed"][0])
+    assert np.abs(_host(z) - g["forcing3"]).max() < 1e-14
+    ik, jk = sol.forcing_modes()
+    assert np.array_equal(ik, g["ikxf"]) and np.array_equal(jk, g["ikyf"])
+
+
+def test_single_mode_decay_on_gpu():
+    p = _params(64, rko=2, alpv=1.0, nu=1e-6, alpnu=2.0, mu=0.3)
+    orc, sol = Oracle(p), _solver(p)
+    a = orc.zeros()
+    spec(a)[5, 3] = 0.7 - 0.2j
+    z, u, v = _dev(a), sol.field(), sol.field()
+    sol.nlt(z, u, v)
+    assert np.abs(_host(z)).max() < 1e-15
+    z = _dev(a)
+    sol.rk_step(z, sol.work())
+    e = orc.emk()[5, 3]
+    assert spec(_host(z))[5, 3] == pytest.approx(e * e * (0.7 - 0.2j), rel=1e-14)
