@@ -39,7 +39,7 @@ def load(path: str | None = None):
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("GTURBO_LIB") or LIB_PATH
     if not os.path.exists(path):
         raise ImportError(f"gturbo_gb300 CUDA library not built: {path} is missing "
                           "(run gturbo_gb300.build.build())")
@@ -67,6 +67,18 @@ def load(path: str | None = None):
         "gt_rann": ([I32P], ctypes.c_float),
         "gt_diag": ([P, D, D, H, H, H, H, H], ctypes.c_int),
         "gt_diag_static": ([ctypes.POINTER(GtParams), D, D, D, D, D, D, D, P], ctypes.c_int),
+        "gt_forcing_philox": ([P, D, ctypes.c_uint64, ctypes.c_uint64], ctypes.c_int),
+        "gt_ens_create": ([ctypes.POINTER(GtParams), ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64),
+                           ctypes.POINTER(P)], ctypes.c_int),
+        "gt_ens_destroy": ([P], ctypes.c_int),
+        "gt_ens_set_stream": ([P, P], ctypes.c_int),
+        "gt_ens_set_fields": ([P, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P),
+                               ctypes.POINTER(P), ctypes.POINTER(P)], ctypes.c_int),
+        "gt_ens_set_step": ([P, ctypes.c_uint64], ctypes.c_int),
+        "gt_ens_get_step": ([P, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+        "gt_ens_use_graph": ([P, ctypes.c_int], ctypes.c_int),
+        "gt_ens_step": ([P, ctypes.c_int32], ctypes.c_int),
+        "gt_ens_last_error": ([P], ctypes.c_char_p),
         "gt_profile": ([P, ctypes.c_int], ctypes.c_int),
         "gt_profile_read": ([P, H, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     }

@@ -30,7 +30,8 @@ def _nvcc() -> str:
 
 def sources() -> list[str]:
     units = sorted(f for f in os.listdir(CSRC) if f.startswith("gt_inst_") and f.endswith(".cu"))
-    return [os.path.join(CSRC, f) for f in units] + [os.path.join(CSRC, "gturbo.cu")]
+    return [os.path.join(CSRC, f) for f in units] + [os.path.join(CSRC, "gturbo.cu"),
+                                                      os.path.join(CSRC, "gt_ens.cu")]
 
 
 def _deps() -> list[str]:
@@ -49,19 +50,27 @@ def _stale(target: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
-    """Compile (if stale) and link the library; returns its path."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, jobs: int | None = None,
+          out_dir: str | None = None, extra_flags: list[str] | None = None) -> str:
+    """Compile (if stale) and link the library; returns its path.
+
+    ``out_dir`` and ``extra_flags`` (e.g. ``["-DGT_ROW_MINB=3"]``) build a variant elsewhere;
+    the environment variable GTURBO_NVCC_FLAGS adds flags to every build.
+    """
+    bdir = out_dir or BUILD
+    lib_path = os.path.join(bdir, LIB_NAME)
+    os.makedirs(bdir, exist_ok=True)
     deps = _deps()
-    if not force and not _stale(LIB_PATH, deps):
-        return LIB_PATH
+    if not force and not _stale(lib_path, deps):
+        return lib_path
     nvcc = _nvcc()
     srcs = sources()
-    objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in srcs]
+    objs = [os.path.join(bdir, os.path.basename(s)[:-3] + ".o") for s in srcs]
+    flags = list(NVCC_FLAGS) + list(extra_flags or []) + os.environ.get("GTURBO_NVCC_FLAGS", "").split()
 
     def compile_one(pair):
         src, obj = pair
-        cmd = [nvcc, *NVCC_FLAGS, "-c", src, "-o", obj]
+        cmd = [nvcc, *flags, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n{r.stderr}")
@@ -72,13 +81,13 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     jobs = jobs or min(len(srcs), max(2, os.cpu_count() or 2))
     with cf.ThreadPoolExecutor(jobs) as ex:
         list(ex.map(compile_one, zip(srcs, objs)))
-    tmp = LIB_PATH + ".tmp"
+    tmp = lib_path + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

@@ -1,0 +1,39 @@
+// gt_internal.h -- host helpers shared by the C-ABI translation units (not part of the ABI).
+#pragma once
+
+#include "../../include/gturbo.h"
+#include "gt_kernels.cuh"
+
+namespace gt {
+
+// Arguments of one nonlinear-term evaluation of a field with the tables of handle h
+// (epilogue defaults: EPI_NLT with h's integrating factor and time steps).
+NltArgs handle_nlt_args(const gt_handle* h, const double* zin, double* q, double* u, double* v,
+                        int* flag);
+
+}  // namespace gt
+
+namespace gt {
+
+// Forced-mode table of a handle (device pointers) and its kick amplitude sqrt(dt)*famp.
+struct ForcingView {
+  const int* ikx;
+  const int* iky;
+  const int* jc;
+  int nf;
+  int nh;
+  double sf;
+};
+ForcingView handle_forcing(const gt_handle* h);
+
+// Grid size, RK order and the parameters a handle was created with.
+const gt_params* handle_params(const gt_handle* h);
+int handle_rko(const gt_handle* h);
+// Records msg as h's last error (h == NULL: the thread's create/no-handle error); returns code.
+int set_error(gt_handle* h, int code, const char* msg);
+
+}  // namespace gt
+
+namespace gt {
+cudaStream_t handle_stream(const gt_handle* h);
+}  // namespace gt

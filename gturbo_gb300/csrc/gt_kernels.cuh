@@ -106,7 +106,10 @@ template <int N>
 struct Shape {
   static constexpr int NH = N / 2 + 1;
   static constexpr int T = N / 16;
-  static constexpr int COLS = (N >= 4096) ? 1 : (N == 2048) ? 2 : (128 / T > 16 ? 16 : 128 / T);
+  // One column per CTA from N=1024 up: the 2/3 rule leaves ~N/3 active columns, and small
+  // CTAs let the block scheduler spread them evenly over the 152 SMs (the FP64 pipe is
+  // shared by the resident CTAs, so an SM's time is its number of columns).
+  static constexpr int COLS = (N >= 1024) ? 1 : (128 / T > 16 ? 16 : 128 / T);
   static constexpr int COL_THREADS = COLS * T;
   static constexpr int COL_CTAS = (NH + COLS - 1) / COLS;
   static constexpr size_t COL_SMEM = (size_t)padded(N) * COLS * sizeof(double2);
@@ -118,97 +121,124 @@ struct Shape {
 
 __device__ __forceinline__ double2 czero() { return make_double2(0.0, 0.0); }
 
-// ---------------------------------------------------------------------------------------
-// Pass A: inverse y-transforms of u, v and q (in that order: zin may alias qo, as the
-// reference destroys z, so q is re-read from zin before the q column is overwritten).
-// ---------------------------------------------------------------------------------------
+// Minimum resident CTAs per SM requested from ptxas (register budget) for N >= 1024.
+#ifndef GT_ROW_MINB
+#define GT_ROW_MINB 2
+#endif
+#ifndef GT_COL_MINB
+#define GT_COL_MINB 3
+#endif
 template <int N>
-__global__ void __launch_bounds__(Shape<N>::COL_THREADS)
-k_nlt_colinv(const double2* zin, double2* qo, double2* __restrict__ uo, double2* __restrict__ vo,
-             const double* __restrict__ kainv, const double* __restrict__ fkx,
-             const double* __restrict__ fky, const double2* __restrict__ tw, int kxlim, int* flag) {
-  using S = Shape<N>;
-  constexpr int T = S::T, C = S::COLS, NH = S::NH;
+struct MinBlocks {
+  static constexpr int ROW = N >= 1024 ? GT_ROW_MINB : 1;
+  static constexpr int COL = N >= 1024 ? GT_COL_MINB : 1;
+};
+
+// ---------------------------------------------------------------------------------------
+// The three passes as tile functions. A tile is one CTA's work: C adjacent columns (passes
+// A and C) or ROWS rows (pass B) of one field. The single-field kernels run tile = blockIdx.x;
+// the ensemble kernels read (member, tile) from a work list, so members of different sizes
+// share one launch (every variant uses 128-thread CTAs from N = 128 to 2048).
+// ---------------------------------------------------------------------------------------
+
+// One nonlinear-term evaluation of one field.
+struct NltArgs {
+  int n;                 // grid size (dispatch key of the ensemble kernels)
+  const double2* zin;    // pass A input (may alias q)
+  double2* q;            // transformed q (pass A out, pass B in)
+  double2* u;            // pass A out / pass B in-out / pass C in
+  double2* v;
+  const double* kainv;   // 1/|k|^alpha [N][NH]
+  const double* fkx;
+  const double* fky;
+  const int* kcut;       // largest kept |ky| per column
+  const double2* tw;     // exp(-2 pi i k / N)
+  int kxlim, kin, kout, truncate;
+  int* flag;             // untruncated-input flag of this field
+  EpiArgs epi;
+};
+
+// Pass A: inverse y-transforms of u, v and q (in that order: zin may alias q, as the
+// reference destroys z, so q is re-read from zin before the q column is overwritten).
+template <int N, int C>
+__device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
+  constexpr int T = N / 16, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
   const int c = threadIdx.x % C, t = threadIdx.x / C;
-  const int i = blockIdx.x * C + c;
+  const int i = tile * C + c;
   const bool valid = i < NH;
   const int ic = valid ? i : NH - 1;
   double2* sm = smem + c;
+  const double2* zin = a.zin;
   double2 v[16];
 #pragma unroll
   for (int s = 0; s < 16; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
   // A column beyond the 2/3 ellipse (i > kxlim) carries data only if the caller passed an
-  // untruncated field: then raise the flag so that pass B reads every column. A block made
+  // untruncated field: then raise the flag so that pass B reads every column. A tile made
   // only of such columns is skipped when all of them are zero.
   int nz = 0;
-  if (valid && i > kxlim) {
+  if (valid && i > a.kxlim) {
 #pragma unroll
     for (int s = 0; s < 16; ++s) nz |= (v[s].x != 0.0) | (v[s].y != 0.0);
   }
-  if (blockIdx.x * C > kxlim) {
+  if (tile * C > a.kxlim) {
     if (!__syncthreads_or(nz)) return;
   }
-  if (nz) atomicExch(flag, 1);
-  const double kx = __ldg(&fkx[ic]);
+  if (nz) atomicExch(a.flag, 1);
+  const double kx = __ldg(&a.fkx[ic]);
   // u = i ky/|k|^a q  (nlt.f90:29-32)
 #pragma unroll
   for (int s = 0; s < 16; ++s) {
     const int j = t + s * T;
-    const double m = __ldg(&fky[j]) * __ldg(&kainv[(size_t)j * NH + ic]);
+    const double m = __ldg(&a.fky[j]) * __ldg(&a.kainv[(size_t)j * NH + ic]);
     v[s] = make_double2(-m * v[s].y, m * v[s].x);
   }
-  fft_regs<N, 16, true, C>(v, sm, t, tw, 0);
+  fft_regs<N, 16, true, C>(v, sm, t, a.tw, 0);
   if (valid) {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) uo[(size_t)(t + s * T) * NH + i] = v[s];
+    for (int s = 0; s < 16; ++s) a.u[(size_t)(t + s * T) * NH + i] = v[s];
   }
   // v = -i kx/|k|^a q  (nlt.f90:33-34)
 #pragma unroll
   for (int s = 0; s < 16; ++s) {
     const int j = t + s * T;
     const double2 q = valid ? zin[(size_t)j * NH + ic] : czero();
-    const double m = kx * __ldg(&kainv[(size_t)j * NH + ic]);
+    const double m = kx * __ldg(&a.kainv[(size_t)j * NH + ic]);
     v[s] = make_double2(m * q.y, -m * q.x);
   }
   __syncthreads();
-  fft_regs<N, 16, true, C>(v, sm, t, tw, 0);
+  fft_regs<N, 16, true, C>(v, sm, t, a.tw, 0);
   if (valid) {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) vo[(size_t)(t + s * T) * NH + i] = v[s];
+    for (int s = 0; s < 16; ++s) a.v[(size_t)(t + s * T) * NH + i] = v[s];
   }
   // q (nlt.f90:41)
 #pragma unroll
   for (int s = 0; s < 16; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
   __syncthreads();
-  fft_regs<N, 16, true, C>(v, sm, t, tw, 0);
+  fft_regs<N, 16, true, C>(v, sm, t, a.tw, 0);
   if (valid) {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) qo[(size_t)(t + s * T) * NH + i] = v[s];
+    for (int s = 0; s < 16; ++s) a.q[(size_t)(t + s * T) * NH + i] = v[s];
   }
 }
 
-// ---------------------------------------------------------------------------------------
 // Pass B: per row y, C2R of q (half-length packing) and of u+iv (one complex transform of
 // length N), p = (u+iv) q, R2C of p, then A = P[k] + conj P[N-k] = 2 FFT(uq)[k] and
 // B = -i (P[k] - conj P[N-k]) = 2 FFT(vq)[k] written over U and V for k <= kout.
-// Inputs beyond column kin are taken as zero unless *flag says pass A wrote them.
-// ---------------------------------------------------------------------------------------
-template <int N>
-__global__ void __launch_bounds__(Shape<N>::ROW_THREADS)
-k_nlt_row(const double2* __restrict__ qf, double2* uf, double2* vf, const double2* __restrict__ tw,
-          int kin, int kout, const int* __restrict__ flag) {
-  using S = Shape<N>;
-  constexpr int T = S::T, NH = S::NH, M = N / 2;
+// Inputs beyond column kin are taken as zero unless the flag says pass A wrote them.
+template <int N, int ROWS>
+__device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
+  constexpr int T = N / 16, NH = N / 2 + 1, M = N / 2;
   extern __shared__ double2 smem[];
   const int r = threadIdx.x / T, t = threadIdx.x % T;
-  const int y = blockIdx.x * S::ROWS + r;
+  const int y = tile * ROWS + r;
   double2* cs = smem + (size_t)r * (padded(N) + padded(M));
   double2* zs = cs + padded(N);
-  const int kl = (*flag) ? M : kin;
-  const double2* qrow = qf + (size_t)y * NH;
-  const double2* urow = uf + (size_t)y * NH;
-  const double2* vrow = vf + (size_t)y * NH;
+  const int kl = (*a.flag) ? M : a.kin;
+  const double2* qrow = a.q + (size_t)y * NH;
+  const double2* urow = a.u + (size_t)y * NH;
+  const double2* vrow = a.v + (size_t)y * NH;
   // C[k] = U[k] + i V[k], C[N-k] = conj U[k] + i conj V[k]; Im of U, V at k=0, N/2 dropped
 #pragma unroll
   for (int s = 0; s <= 8; ++s) {
@@ -228,12 +258,12 @@ k_nlt_row(const double2* __restrict__ qf, double2* uf, double2* vf, const double
 #pragma unroll
   for (int s = 0; s < 8; ++s) {
     const int k = t + s * T;
-    double2 a = (k <= kl) ? qrow[k] : czero();
+    double2 p = (k <= kl) ? qrow[k] : czero();
     double2 b = (M - k <= kl) ? qrow[M - k] : czero();
-    if (k == 0) { a.y = 0.0; b.y = 0.0; }
-    const double2 sm_ = make_double2(a.x + b.x, a.y - b.y);
-    const double2 d = make_double2(a.x - b.x, a.y + b.y);
-    const double2 w = __ldg(&tw[k]);
+    if (k == 0) { p.y = 0.0; b.y = 0.0; }
+    const double2 sm_ = make_double2(p.x + b.x, p.y - b.y);
+    const double2 d = make_double2(p.x - b.x, p.y + b.y);
+    const double2 w = __ldg(&a.tw[k]);
     const double2 tt = twmul<true>(d, w);  // W^-k d
     zs[padix(k)] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
   }
@@ -244,7 +274,7 @@ k_nlt_row(const double2* __restrict__ qf, double2* uf, double2* vf, const double
 #pragma unroll
     for (int s = 0; s < 8; ++s) h[s] = zs[padix(t + s * T)];
     __syncthreads();
-    fft_regs<M, 8, true, 1>(h, zs, t, tw, 1);
+    fft_regs<M, 8, true, 1>(h, zs, t, a.tw, 1);
     __syncthreads();
 #pragma unroll
     for (int s = 0; s < 8; ++s) zs[padix(t + s * T)] = h[s];
@@ -254,7 +284,7 @@ k_nlt_row(const double2* __restrict__ qf, double2* uf, double2* vf, const double
 #pragma unroll
   for (int s = 0; s < 16; ++s) v[s] = cs[padix(t + s * T)];
   __syncthreads();
-  fft_regs<N, 16, true, 1>(v, cs, t, tw, 0);
+  fft_regs<N, 16, true, 1>(v, cs, t, a.tw, 0);
   __syncthreads();
   // p = (u + i v) q  (produ.f90:18-19); q[2m] = Re z[m], q[2m+1] = Im z[m]
 #pragma unroll
@@ -264,17 +294,17 @@ k_nlt_row(const double2* __restrict__ qf, double2* uf, double2* vf, const double
     const double q = (x & 1) ? zq.y : zq.x;
     v[s] = make_double2(v[s].x * q, v[s].y * q);
   }
-  fft_regs<N, 16, false, 1>(v, cs, t, tw, 0);
+  fft_regs<N, 16, false, 1>(v, cs, t, a.tw, 0);
   __syncthreads();
 #pragma unroll
   for (int s = 0; s < 16; ++s) cs[padix(t + s * T)] = v[s];
   __syncthreads();
-  double2* urw = uf + (size_t)y * NH;
-  double2* vrw = vf + (size_t)y * NH;
+  double2* urw = a.u + (size_t)y * NH;
+  double2* vrw = a.v + (size_t)y * NH;
 #pragma unroll
   for (int s = 0; s <= 8; ++s) {
     const int k = t + s * T;
-    if (k <= kout) {
+    if (k <= a.kout) {
       const double2 P = cs[padix(k)];
       const double2 Q = cs[padix((N - k) & (N - 1))];
       urw[k] = make_double2(P.x + Q.x, P.y - Q.y);
@@ -283,38 +313,34 @@ k_nlt_row(const double2* __restrict__ qf, double2* uf, double2* vf, const double
   }
 }
 
-// ---------------------------------------------------------------------------------------
 // Pass C: forward y-transforms of A and B, N = -i (kx A + ky B) / (2 N^2), the 2/3 mask
 // (row j of column i is kept iff min(j, N-j) <= kcut[i]) and the stage epilogue.
-// ---------------------------------------------------------------------------------------
-template <int N>
-__global__ void __launch_bounds__(Shape<N>::COL_THREADS)
-k_nlt_colfwd(double2* af, const double2* __restrict__ bf, const double* __restrict__ fkx,
-             const double* __restrict__ fky, const int* __restrict__ kcut,
-             const double2* __restrict__ tw, int kxlim, int truncate, int* flag, EpiArgs E) {
-  using S = Shape<N>;
-  constexpr int T = S::T, C = S::COLS, NH = S::NH;
+template <int N, int C>
+__device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
+  constexpr int T = N / 16, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
-  if (blockIdx.x == 0 && threadIdx.x == 0) *flag = 0;  // pass B of this nlt is complete
+  if (tile == 0 && threadIdx.x == 0) *a.flag = 0;  // pass B of this nlt is complete
   const int c = threadIdx.x % C, t = threadIdx.x / C;
-  const int i = blockIdx.x * C + c;
+  const int i = tile * C + c;
   const bool valid = i < NH;
   const int ic = valid ? i : NH - 1;
-  if (blockIdx.x * C > kxlim) {
-    // no retained mode in this block of columns: N = 0
+  if (tile * C > a.kxlim) {
+    // no retained mode in this tile: N = 0
     if (valid) {
 #pragma unroll
-      for (int s = 0; s < 16; ++s) epilogue(E, i, t + s * T, NH, czero());
+      for (int s = 0; s < 16; ++s) epilogue(a.epi, i, t + s * T, NH, czero());
     }
     return;
   }
   double2* sm = smem + c;
+  double2* af = a.u;
+  const double2* bf = a.v;
   const double scale = 0.5 / ((double)N * (double)N);
-  const double kxs = __ldg(&fkx[ic]) * scale;
+  const double kxs = __ldg(&a.fkx[ic]) * scale;
   double2 v[16];
 #pragma unroll
   for (int s = 0; s < 16; ++s) v[s] = valid ? af[(size_t)(t + s * T) * NH + ic] : czero();
-  fft_regs<N, 16, false, C>(v, sm, t, tw, 0);
+  fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
   // keep kx*FA in place of A (the same thread re-reads it below)
   if (valid) {
 #pragma unroll
@@ -324,21 +350,57 @@ k_nlt_colfwd(double2* af, const double2* __restrict__ bf, const double* __restri
 #pragma unroll
   for (int s = 0; s < 16; ++s) v[s] = valid ? bf[(size_t)(t + s * T) * NH + ic] : czero();
   __syncthreads();
-  fft_regs<N, 16, false, C>(v, sm, t, tw, 0);
+  fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
   if (!valid) return;
-  const int kc = truncate ? __ldg(&kcut[i]) : N;
+  const int kc = a.truncate ? __ldg(&a.kcut[i]) : N;
 #pragma unroll
   for (int s = 0; s < 16; ++s) {
     const int j = t + s * T;
-    const double kys = __ldg(&fky[j]) * scale;
-    const double2 a = af[(size_t)j * NH + i];
+    const double kys = __ldg(&a.fky[j]) * scale;
+    const double2 fa = af[(size_t)j * NH + i];
     // N = -i (kx A + ky B): re = kx Im A + ky Im B, im = -(kx Re A + ky Re B)
-    double2 nh = make_double2(fma(kys, v[s].y, a.y), -fma(kys, v[s].x, a.x));
+    double2 nh = make_double2(fma(kys, v[s].y, fa.y), -fma(kys, v[s].x, fa.x));
     const int aj = min(j, N - j);
-    if (aj > kc || (i == 0 && j == 0 && truncate)) nh = czero();
-    epilogue(E, i, j, NH, nh);
+    if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
+    epilogue(a.epi, i, j, NH, nh);
   }
 }
+
+// ---- single-field kernels ---------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
+k_nlt_colinv(NltArgs a) {
+  colinv_tile<N, Shape<N>::COLS>(a, blockIdx.x);
+}
+
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::ROW_THREADS, MinBlocks<N>::ROW)
+k_nlt_row(NltArgs a) {
+  row_tile<N, Shape<N>::ROWS>(a, blockIdx.x);
+}
+
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
+k_nlt_colfwd(NltArgs a) {
+  colfwd_tile<N, Shape<N>::COLS>(a, blockIdx.x);
+}
+
+// ---- ensemble kernels: one launch per pass for every member ------------------------------
+// CTA b works on tile tiles[b] = (member, tile) of the member's field; members may differ in
+// size (N = 128 ... 2048), alpha, dt and tables. All variants use 128-thread CTAs and the same
+// shared memory (C * N = 2048 columns-values, ROWS * N = 2048 row-values).
+constexpr int kEnsThreads = 128;
+constexpr size_t kEnsColSmem = (size_t)padded(2048) * sizeof(double2);
+constexpr size_t kEnsRowSmem = (size_t)(padded(2048) + padded(1024)) * sizeof(double2);
+
+struct EnsTile {
+  int member;
+  int tile;
+};
+
+// Tiles per field of each ensemble pass (128-thread CTAs).
+__host__ __device__ constexpr int ens_col_tiles(int n) { return (n / 2 + 1 + (2048 / n) - 1) / (2048 / n); }
+__host__ __device__ constexpr int ens_row_tiles(int n) { return n / (2048 / n); }
 
 // ---------------------------------------------------------------------------------------
 // Standalone transforms (fft_inv.f90, fft_dir.f90) and elementwise routines.

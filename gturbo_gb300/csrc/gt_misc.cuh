@@ -80,12 +80,23 @@ struct DiagArgs {
   const double2* znl;   // may be null: no fluxes
   const double* fkxs;
   const double* fkys;
+  const double* kainv;  // 1/|k|^alpha table [n][nh] or null (then pow per mode)
   int n, nh, nbin;
+  int unit_k;           // 1: dkx = dky = 1 (box 2 pi), integer wavenumbers -> integer bins
   double dk, alpv;
   double nu, mu, alpnu, alpmu;
   double* part;         // [ngroups][nbin][4]: sp, sz, flem, flzm
   double* rowsum;       // [n][6]
 };
+
+// smallest s >= 0 with s*s >= x (x < 2^52)
+__device__ __forceinline__ int isqrt_ceil(long long x) {
+  if (x <= 0) return 0;
+  long long s = (long long)sqrtf((float)x);
+  while (s * s < x) ++s;
+  while (s > 0 && (s - 1) * (s - 1) >= x) --s;
+  return (int)s;
+}
 
 __device__ __forceinline__ int diag_bin(const DiagArgs& D, int i, int j) {
   const double k = sqrt(__ldg(&D.fkxs[i]) + __ldg(&D.fkys[j]));
@@ -102,31 +113,46 @@ __global__ void k_diag_bins(DiagArgs D) {
     const int j0 = g * kDiagRowGroup, j1 = min(D.n, j0 + kDiagRowGroup);
     for (int j = j0; j < j1; ++j) {
       const double fkys = __ldg(&D.fkys[j]);
-      // The bin index is non-decreasing in i along a row. Start from the analytic estimate of
-      // the first i with bin >= b and correct it with the exact bin function.
-      const double kb = (double)b * D.dk;
-      const double rem = kb * kb - fkys;
-      int lo = rem > 0.0 ? (int)ceil(sqrt(rem) / D.dk) : 0;
-      lo = min(max(lo, 0), D.nh);
-      while (lo > 0 && diag_bin(D, lo - 1, j) >= b) --lo;
-      while (lo < D.nh && diag_bin(D, lo, j) < b) ++lo;
-      for (int i = lo; i < D.nh; ++i) {
-        if (diag_bin(D, i, j) != b) break;
+      // The bin index is non-decreasing in i along a row: bin b is a segment [lo, hi).
+      int lo, hi;
+      if (D.unit_k) {
+        // integer wavenumbers: int(sqrt(k2)) = floor(sqrt(i^2 + ky^2)) exactly (k2 < 2^52),
+        // so b^2 <= i^2 + ky^2 < (b+1)^2 gives the segment in integer arithmetic
+        const long long ky = min(j, D.n - j);
+        lo = isqrt_ceil((long long)b * b - ky * ky);
+        hi = isqrt_ceil((long long)(b + 1) * (b + 1) - ky * ky);
+        lo = min(lo, D.nh);
+        hi = min(hi, D.nh);
+      } else {
+        // start from the analytic estimate of the first i with bin >= b and correct it with
+        // the exact bin function
+        const double kb = (double)b * D.dk;
+        const double rem = kb * kb - fkys;
+        lo = rem > 0.0 ? (int)ceil(sqrt(rem) / D.dk) : 0;
+        lo = min(max(lo, 0), D.nh);
+        while (lo > 0 && diag_bin(D, lo - 1, j) >= b) --lo;
+        while (lo < D.nh && diag_bin(D, lo, j) < b) ++lo;
+        hi = lo;
+        while (hi < D.nh && diag_bin(D, hi, j) == b) ++hi;
+      }
+      for (int i = lo; i < hi; ++i) {
         if (i == 0 && j == 0) continue;
-        const double2 q = D.z[(size_t)j * D.nh + i];
-        const double k2 = __ldg(&D.fkxs[i]) + fkys;
-        const double ka = pow(k2, D.alpv / 2.0);
-        double a2 = hypot(q.x, q.y);
-        a2 = a2 * a2;
+        const size_t o = (size_t)j * D.nh + i;
+        const double2 q = D.z[o];
+        // 1/|k|^alpha from the table when the handle has one (a few FP64 instructions per
+        // mode instead of a pow: the bin segments are uneven, so warps diverge here)
+        const double ikv = D.kainv ? __ldg(&D.kainv[o])
+                                   : 1.0 / pow(__ldg(&D.fkxs[i]) + fkys, D.alpv / 2.0);
+        const double a2 = q.x * q.x + q.y * q.y;
         const double fac = (i == 0 || i == D.nh - 1) ? 0.5 : 1.0;
-        sp = sp + fac * a2 / ka;
+        sp = sp + fac * a2 * ikv;
         sz = sz + fac * a2;
         if (D.znl) {
-          const double2 w = D.znl[(size_t)j * D.nh + i];
+          const double2 w = D.znl[o];
           const double ff = (i == 0 || i == D.nh - 1) ? 1.0 : 2.0;
           const double f = q.x * w.x + q.y * w.y;
           fz = fz + ff * f;
-          fe = fe + ff * (f / ka);
+          fe = fe + ff * (f * ikv);
         }
       }
     }
@@ -169,18 +195,25 @@ __global__ void k_diag_glob_rows(DiagArgs D) {
   const double fkys = __ldg(&D.fkys[j]);
   for (int i = threadIdx.x; i < D.nh; i += blockDim.x) {
     if (i == 0 && j == 0) continue;
-    const double2 q = D.z[(size_t)j * D.nh + i];
+    const size_t o = (size_t)j * D.nh + i;
+    const double2 q = D.z[o];
     const double k2 = __ldg(&D.fkxs[i]) + fkys;
-    const double ka = pow(k2, D.alpv / 2.0);
-    double a2 = hypot(q.x, q.y);
-    a2 = a2 * a2;
+    const double ikv = D.kainv ? __ldg(&D.kainv[o]) : 1.0 / pow(k2, D.alpv / 2.0);
+    const double a2 = q.x * q.x + q.y * q.y;
     const double fac = (i == 0 || i == D.nh - 1) ? 0.5 : 1.0;
-    acc[0] += fac * a2 / ka;
-    acc[1] += fac * a2;
-    acc[2] += 2.0 * fac * D.nu * pow(k2, D.alpnu) * a2;
-    acc[3] += 2.0 * fac * D.mu * pow(k2, D.alpmu) * a2;
-    acc[4] += 2.0 * fac * D.nu * pow(k2, D.alpnu - D.alpv / 2.0) * a2;
-    acc[5] += 2.0 * fac * D.mu * pow(k2, D.alpmu - D.alpv / 2.0) * a2;
+    // k2^alpnu, k2^alpmu from one log (pow costs ~2x log + exp in FP64); the alpha-shifted
+    // powers of diagnostics.f90:160-161 are these divided by ka
+    const double lk = log(k2);
+    const double knu = exp(D.alpnu * lk);
+    const double kmu = D.alpmu == 0.0 ? 1.0 : exp(D.alpmu * lk);
+    const double fa = fac * a2;
+    const double fai = fa * ikv;
+    acc[0] += fai;
+    acc[1] += fa;
+    acc[2] += 2.0 * D.nu * knu * fa;
+    acc[3] += 2.0 * D.mu * kmu * fa;
+    acc[4] += 2.0 * D.nu * knu * fai;
+    acc[5] += 2.0 * D.mu * kmu * fai;
   }
   __shared__ double red[6][256];
   for (int q = 0; q < 6; ++q) red[q][threadIdx.x] = acc[q];

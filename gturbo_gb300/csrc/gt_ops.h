@@ -22,19 +22,10 @@ enum OpKind : int {
 struct GtOp {
   int kind;
   cudaStream_t stream;
-  const double2* zin;
-  double2* a;
-  double2* b;
-  double2* c;
-  const double* kainv;
-  const double* fkx;
-  const double* fky;
-  const int* kcut;
+  NltArgs nlt;        // passes A, B, C
+  double2* a;         // field of the standalone transforms
   const double2* tw;
-  int kxlim, kin, kout, truncate;
-  int* flag;
   double scale;
-  EpiArgs epi;
 };
 
 // Per-N entry points (defined in gt_inst_<N>.cu).

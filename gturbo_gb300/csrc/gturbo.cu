@@ -16,6 +16,7 @@
 #include "../../include/gturbo.h"
 #include "gt_misc.cuh"
 #include "gt_ops.h"
+#include "gt_internal.h"
 
 using gt::GtOp;
 
@@ -67,6 +68,55 @@ struct gt_handle {
   std::vector<int> ev_kind;  // kind of pair p = events 2p, 2p+1
 };
 
+namespace gt {
+
+NltArgs handle_nlt_args(const gt_handle* h, const double* zin, double* q, double* u, double* v,
+                        int* flag) {
+  NltArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.n = h->N;
+  a.zin = reinterpret_cast<const double2*>(zin);
+  a.q = reinterpret_cast<double2*>(q);
+  a.u = reinterpret_cast<double2*>(u);
+  a.v = reinterpret_cast<double2*>(v);
+  a.kainv = h->d_kainv;
+  a.fkx = h->d_fkx;
+  a.fky = h->d_fky;
+  a.kcut = h->d_kcut;
+  a.tw = h->d_tw;
+  a.truncate = h->truncate;
+  a.kxlim = h->truncate ? h->kxlim : h->N / 2;
+  a.kin = a.kxlim;
+  a.kout = a.kxlim;
+  a.flag = flag;
+  a.epi.split = h->split;
+  a.epi.emk = h->d_emk;
+  a.epi.emkx = h->d_emkx;
+  a.epi.emky = h->d_emky;
+  a.epi.dt = h->p.dt;
+  a.epi.dt2 = h->dt2;
+  a.epi.dt3 = h->dt3;
+  a.epi.dt6 = h->dt6;
+  return a;
+}
+
+ForcingView handle_forcing(const gt_handle* h) {
+  ForcingView f;
+  f.ikx = h->d_ikxf;
+  f.iky = h->d_ikyf;
+  f.jc = h->d_jc;
+  f.nf = h->nf;
+  f.nh = h->NH;
+  f.sf = h->sdt * h->p.famp;
+  return f;
+}
+
+const gt_params* handle_params(const gt_handle* h) { return &h->p; }
+int handle_rko(const gt_handle* h) { return h->rko; }
+cudaStream_t handle_stream(const gt_handle* h) { return h->stream; }
+
+}  // namespace gt
+
 namespace {
 
 int fail(gt_handle* h, int code, const std::string& msg) {
@@ -74,6 +124,12 @@ int fail(gt_handle* h, int code, const std::string& msg) {
   else g_create_error = msg;
   return code;
 }
+
+}  // namespace
+
+int gt::set_error(gt_handle* h, int code, const char* msg) { return fail(h, code, msg); }
+
+namespace {
 
 int cuda_fail(gt_handle* h, cudaError_t e, const char* what) {
   return fail(h, GT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -171,24 +227,8 @@ GtOp base_op(const gt_handle* h) {
   GtOp op;
   std::memset(&op, 0, sizeof(op));
   op.stream = h->stream;
-  op.kainv = h->d_kainv;
-  op.fkx = h->d_fkx;
-  op.fky = h->d_fky;
-  op.kcut = h->d_kcut;
   op.tw = h->d_tw;
-  op.truncate = h->truncate;
-  op.kxlim = h->truncate ? h->kxlim : h->N / 2;
-  op.kin = op.kxlim;
-  op.kout = op.kxlim;
-  op.flag = h->d_flag;
-  op.epi.split = 0;
-  op.epi.emk = h->d_emk;
-  op.epi.emkx = h->d_emkx;
-  op.epi.emky = h->d_emky;
-  op.epi.dt = h->p.dt;
-  op.epi.dt2 = h->dt2;
-  op.epi.dt3 = h->dt3;
-  op.epi.dt6 = h->dt6;
+  op.nlt = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, h->d_flag);
   return op;
 }
 
@@ -232,24 +272,20 @@ int run(gt_handle* h, const GtOp& op) {
 int nlt_passes(gt_handle* h, const double* zin, double* qbuf, double* u, double* v,
                const gt::EpiArgs& epi) {
   GtOp op = base_op(h);
+  op.nlt = gt::handle_nlt_args(h, zin, qbuf, u, v, h->d_flag);
+  op.nlt.epi = epi;
   op.kind = gt::OP_NLT_COLINV;
-  op.zin = reinterpret_cast<const double2*>(zin);
-  op.a = reinterpret_cast<double2*>(qbuf);
-  op.b = reinterpret_cast<double2*>(u);
-  op.c = reinterpret_cast<double2*>(v);
   int rc = run(h, op);
   if (rc) return rc;
   op.kind = gt::OP_NLT_ROW;
-  op.zin = reinterpret_cast<const double2*>(qbuf);
   rc = run(h, op);
   if (rc) return rc;
   op.kind = gt::OP_NLT_COLFWD;
-  op.epi = epi;
   return run(h, op);
 }
 
 gt::EpiArgs make_epi(const gt_handle* h, int mode, double* out, double* znew, const double* z) {
-  gt::EpiArgs E = base_op(h).epi;
+  gt::EpiArgs E = base_op(h).nlt.epi;
   E.mode = mode;
   E.out = reinterpret_cast<double2*>(out);
   E.znew = reinterpret_cast<double2*>(znew);
@@ -527,7 +563,6 @@ int gt_step_rk2(gt_handle* h, double* z, double* znl, double* u, double* v) {
   if (!h || !z || !znl || !u || !v) return fail(h, GT_ERR_ARG, "gt_step_rk2: null argument");
   gt::EpiArgs E1 = make_epi(h, gt::EPI_RK2A, znl, nullptr, z);
   gt::EpiArgs E2 = make_epi(h, gt::EPI_RK2B, z, nullptr, z);
-  E1.split = E2.split = h->split;
   int rc = nlt_passes(h, z, znl, u, v, E1);
   if (rc) return rc;
   return nlt_passes(h, znl, znl, u, v, E2);
@@ -574,10 +609,12 @@ int gt_diag(gt_handle* h, const double* z, const double* znl, double* sp, double
   D.znl = reinterpret_cast<const double2*>(znl);
   D.fkxs = h->d_fkxs;
   D.fkys = h->d_fkys;
+  D.kainv = h->d_kainv;
   D.n = h->N;
   D.nh = h->NH;
   D.nbin = h->NBIN;
   D.dk = h->dkx;
+  D.unit_k = (h->dkx == 1.0 && h->dky == 1.0) ? 1 : 0;
   D.alpv = h->p.alpv;
   D.nu = h->p.nu;
   D.mu = h->p.mu;
@@ -749,6 +786,7 @@ extern "C" int gt_diag_static(const gt_params* p, const double* z, const double*
   D.znl = reinterpret_cast<const double2*>(znl);
   D.fkxs = base + kOffFkxs;
   D.fkys = base + kOffFkys;
+  D.kainv = nullptr;
   D.n = n;
   D.nh = nh;
   D.nbin = nb;
@@ -761,6 +799,7 @@ extern "C" int gt_diag_static(const gt_params* p, const double* z, const double*
   D.part = base + kOffPart;
   D.rowsum = base + kOffRows;
   const double dky = 2.0 * 3.14159265358979323846 / p->xly;
+  D.unit_k = (D.dk == 1.0 && dky == 1.0) ? 1 : 0;
   k_static_k2<<<(n + 127) / 128, 128, 0, s>>>(base + kOffFkxs, base + kOffFkys, n, D.dk, dky);
   if (sp || sz || fle || flz) {
     const int ngroups = (n + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;

@@ -150,6 +150,10 @@ class Solver:
         self._check(self.lib.gt_forcing(self.h, self._ptr(z), ctypes.byref(s)))
         return s.value
 
+    def forcing_philox(self, z, key: int, step: int) -> None:
+        """The kick with counter-based Philox phases (gt_forcing_philox)."""
+        self._check(self.lib.gt_forcing_philox(self.h, self._ptr(z), int(key), int(step)))
+
     def diag(self, z, znl=None) -> dict:
         """spectrum / fluxes / glob of src/diagnostics.f90 (synchronous)."""
         nb = self.n // 2

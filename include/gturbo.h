@@ -127,6 +127,40 @@ int gt_forcing(gt_handle* h, double* z, int32_t* seed);
  * once and returns the real(4) draw. Exported for drivers and tests. */
 float gt_rann(int32_t* seed);
 
+/* Counter-based forcing, no counterpart in the reference (its LCG is serial):
+ * the same kick as gt_forcing, with the phase of forced mode k at step `step`
+ * equal to 2*pi*u, u = top 53 bits of Philox4x64-10(counter = (step, k, 0, 0),
+ * key = (key, 0)) word 0. Independent streams per key; every mode is drawn in
+ * parallel and the result does not depend on call order. */
+int gt_forcing_philox(gt_handle* h, double* z, uint64_t key, uint64_t step);
+
+/* ---- batched ensembles (no counterpart in the reference) ---------------- */
+
+/* An ensemble advances nmembers independent fields in one launch per pass:
+ * members may differ in grid size (powers of two in [128, 2048]), alpha,
+ * dt, dissipation and forcing shell, but share the RK order. Member m has the
+ * parameters members[m] and the Philox forcing stream keys[m]. One step of
+ * every member is the RK step (gt_step_rk2/gt_step_rk4) followed by
+ * gt_forcing_philox at the ensemble's step counter, which then advances. */
+typedef struct gt_ens gt_ens;
+int gt_ens_create(const gt_params* members, int32_t nmembers, const uint64_t* keys, gt_ens** out);
+int gt_ens_destroy(gt_ens* e);
+/* Stream the ensemble's work is ordered after / before (NULL = legacy default). */
+int gt_ens_set_stream(gt_ens* e, void* cuda_stream);
+/* Device fields of every member (host arrays of nmembers device pointers, each
+ * field NS doubles of that member's size); znew may be NULL for RK2. */
+int gt_ens_set_fields(gt_ens* e, double* const* z, double* const* znl, double* const* znew,
+                      double* const* u, double* const* v);
+/* Philox step counter of the next forcing (synchronous). */
+int gt_ens_set_step(gt_ens* e, uint64_t step);
+int gt_ens_get_step(gt_ens* e, uint64_t* step);
+/* 1 (default): capture one ensemble step as a CUDA graph on first use and replay
+ * it; 0: launch the kernels directly every step. */
+int gt_ens_use_graph(gt_ens* e, int enable);
+/* Advance every member by nsteps steps (asynchronous on the ensemble's stream). */
+int gt_ens_step(gt_ens* e, int32_t nsteps);
+const char* gt_ens_last_error(const gt_ens* e);
+
 /* ---- diagnostics (src/diagnostics.f90:5-179) --------------------------- */
 
 /* Shell spectra, fluxes and global budgets of z (and of znl = nlt(z) for the

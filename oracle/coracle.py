@@ -55,6 +55,9 @@ def _load():
     lib.or_forcing.argtypes = [P, D, I32]
     lib.or_diag.argtypes = [P, D, D, D, D, D, D, D]
     lib.or_main_step.argtypes = [P, D, D, D, D, D, I32, ctypes.c_int, D, D, D, D, D]
+    U64 = ctypes.POINTER(ctypes.c_uint64)
+    lib.or_philox4x64_10.argtypes = [U64, U64, U64]
+    lib.or_forcing_philox.argtypes = [P, D, ctypes.c_uint64, ctypes.c_uint64]
     lib.or_num_threads.restype = ctypes.c_int
     lib.or_set_num_threads.argtypes = [ctypes.c_int]
     _lib = lib
@@ -72,6 +75,16 @@ def spec(a: np.ndarray) -> np.ndarray:
     """Complex (N, N/2+1) view of an (N, N+2) float64 field."""
     n = a.shape[0]
     return a.view(np.complex128).reshape(n, n // 2 + 1)
+
+
+def philox4x64_10(counter, key):
+    """Philox4x64-10 block of the oracle (4 uint64 counter words, 2 key words)."""
+    lib = _load()
+    c = (ctypes.c_uint64 * 4)(*counter)
+    k = (ctypes.c_uint64 * 2)(*key)
+    o = (ctypes.c_uint64 * 4)()
+    lib.or_philox4x64_10(c, k, o)
+    return [int(x) for x in o]
 
 
 def set_num_threads(n: int) -> None:
@@ -167,6 +180,9 @@ class Oracle:
         s = ctypes.c_int32(seed)
         self.lib.or_forcing(self.h, _dp(z), ctypes.byref(s))
         return s.value
+
+    def forcing_philox(self, z, key: int, step: int) -> None:
+        self.lib.or_forcing_philox(self.h, _dp(z), ctypes.c_uint64(key), ctypes.c_uint64(step))
 
     def diag(self, z, znl=None):
         nb = self.n // 2

@@ -670,3 +670,49 @@ void or_set_num_threads(int n) {
   (void)n;
 #endif
 }
+
+/* ------------------------------------------------------------------------ */
+/* Counter-based forcing (no counterpart in the reference): Philox4x64-10    */
+/* (Salmon et al., SC'11), the generator numpy calls Philox.                 */
+/* ------------------------------------------------------------------------ */
+
+void or_philox4x64_10(const uint64_t ctr_in[4], const uint64_t key[2], uint64_t out[4]) {
+  uint64_t x0 = ctr_in[0], x1 = ctr_in[1], x2 = ctr_in[2], x3 = ctr_in[3];
+  uint64_t k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; r++) {
+    if (r > 0) {
+      k0 += 0x9E3779B97F4A7C15ull;
+      k1 += 0xBB67AE8584CAA73Bull;
+    }
+    unsigned __int128 p0 = (unsigned __int128)0xD2E7470EE14C6C93ull * x0;
+    unsigned __int128 p1 = (unsigned __int128)0xCA5A826395121157ull * x2;
+    uint64_t hi0 = (uint64_t)(p0 >> 64), lo0 = (uint64_t)p0;
+    uint64_t hi1 = (uint64_t)(p1 >> 64), lo1 = (uint64_t)p1;
+    uint64_t y0 = hi1 ^ x1 ^ k0, y1 = lo1, y2 = hi0 ^ x3 ^ k1, y3 = lo0;
+    x0 = y0; x1 = y1; x2 = y2; x3 = y3;
+  }
+  out[0] = x0; out[1] = x1; out[2] = x2; out[3] = x3;
+}
+
+/* The forcing kick with phase 2 pi u, u = top 53 bits of Philox((step, k, 0, 0), (key, 0))[0]. */
+void or_forcing_philox(const or_ctx* c, double* z, uint64_t key, uint64_t step) {
+  const int NH = c->NH;
+  const double sf = c->sdt * c->p.famp;
+  const uint64_t kk[2] = {key, 0};
+  for (int k = 0; k < c->nf; k++) {
+    uint64_t ctr[4] = {step, (uint64_t)k, 0, 0}, o[4];
+    or_philox4x64_10(ctr, kk, o);
+    double u = (double)(o[0] >> 11) * (1.0 / 9007199254740992.0);
+    double te = 2.0 * 3.14159265358979323846 * u;
+    double cc = cos(te), cs = sin(te);
+    int i = c->ikxf[k], j = c->ikyf[k];
+    size_t o2 = 2 * ((size_t)j * NH + i);
+    z[o2] = z[o2] + sf * c->ff[k][0] * cc;
+    z[o2 + 1] = z[o2 + 1] + sf * c->ff[k][1] * cs;
+    if (i == 0 || i == NH - 1) {
+      size_t oc = 2 * ((size_t)c->jc[j] * NH + i);
+      z[oc] = z[oc] + sf * c->ff[k][0] * cc;
+      z[oc + 1] = z[oc + 1] - sf * c->ff[k][1] * cs;
+    }
+  }
+}

@@ -181,3 +181,50 @@ def test_fft_round_trip_and_trunc_idempotent():
     b = a.copy()
     o.trunc(b)
     assert np.array_equal(a, b)
+
+
+def test_oracle_philox_matches_numpy_philox():
+    """The oracle's Philox4x64-10 block equals numpy.random.Philox (whose first draw uses the
+    counter + 1)."""
+    from oracle.coracle import philox4x64_10
+    M = 2 ** 64
+    for ctr, key in [((0, 0, 0, 0), (0, 0)), ((7, 3, 0, 1), (123456789, 42)),
+                     ((M - 1, M - 1, 5, 6), (M - 1, 1)), ((M - 1, M - 1, M - 1, M - 1), (5, M - 3))]:
+        c = sum(x << (64 * i) for i, x in enumerate(ctr))
+        k = sum(x << (64 * i) for i, x in enumerate(key))
+        ref = [int(x) for x in np.random.Philox(counter=c, key=k).random_raw(4)]
+        v = (c + 1) % 2 ** 256
+        assert philox4x64_10([(v >> (64 * i)) & (M - 1) for i in range(4)], key) == ref
+
+
+def test_philox_forcing_is_order_free_and_hermitian():
+    p = _p(64, k1f=0.0, k2f=6.0)
+    o = Oracle(p)
+    a = o.zeros()
+    o.forcing_philox(a, 7, 3)
+    b = o.zeros()
+    o.forcing_philox(b, 7, 3)
+    assert np.array_equal(a, b)
+    c = o.zeros()
+    o.forcing_philox(c, 8, 3)
+    assert not np.array_equal(a, c)
+    s = spec(a)
+    for col in (0, 32):
+        for j in range(1, 32):
+            assert s[64 - j, col] == pytest.approx(np.conj(s[j, col]), abs=1e-15)
+    # unit-modulus kicks of size sqrt(dt) famp on every forced mode
+    ik, jk = o.forcing_modes()
+    amp = np.abs(s[jk, ik])
+    assert np.allclose(amp[ik > 0], np.sqrt(p.dt) * p.famp, rtol=1e-14)
+
+
+def test_ensemble_c4_members():
+    from gturbo_gb300.ensemble import ensemble_c4
+    ms = ensemble_c4()
+    assert len(ms) == 64
+    assert [m.params.n for m in ms].count(256) == 32 and [m.params.n for m in ms].count(1024) == 8
+    assert set(m.params.alpv for m in ms) <= {0.5, 1.0, 2.0, 3.0}
+    assert len(set(m.key for m in ms)) == 64
+    for m in ms[::9]:
+        assert Oracle(m.params).info.inpe == pytest.approx(1.0, rel=1e-12)
+        assert m.params.dt == pytest.approx(0.25 / m.params.n)
