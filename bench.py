@@ -356,6 +356,12 @@ def ours_arm(args):
             except Exception as e:
                 extras["ensemble"] = {"unavailable": str(e)[:300]}
 
+            # ---- adjoint gradient (1024^2, 200 steps, checkpoints) vs the forward run ---
+            try:
+                extras["adjoint"] = adjoint_run(torch)
+            except Exception as e:
+                extras["adjoint"] = {"unavailable": str(e)[:300]}
+
             # ---- CPU baseline (the oracle on the host cores) ---------------------------
             try:
                 extras["cpu_baseline"] = cpu_oracle_run(p, k0, 10 ** 6, args.cpu_seconds)
@@ -380,6 +386,48 @@ def ours_arm(args):
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def adjoint_run(torch):
+    """The 1024^2 gradient workload: 200 RK2 steps with the LCG kick (alpha=1, dt=5e-5), J =
+    energy in the shells 4 <= |k| <= 8 at the final time, gradients with respect to the initial
+    field and famp by the checkpointed adjoint (checkpoint every 20 steps). Reports the backward
+    sweep against the plain forward run, and checks the gradient against the tangent-linear
+    model (dot-product test) and a central finite difference along one random direction."""
+    from gturbo_gb300.adjoint import forward_objective, gradient, tlm_run
+    from gturbo_gb300.ic import random_phase_ic
+    from gturbo_gb300.params import IC_K0, config
+    from gturbo_gb300.solver import Solver
+
+    p = config("c5")
+    nsteps, K, kmin, kmax = 200, 20, 4.0, 8.0
+    sol = Solver(p)
+    z0 = torch.from_numpy(random_phase_ic(p, IC_K0["c5"], 0.5, seed=1)).cuda()
+    forward_objective(sol, z0, 3, SEED, kmin, kmax)  # warm-up
+    torch.cuda.synchronize()
+    s = sol.stream
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    J_fwd = forward_objective(sol, z0, nsteps, SEED, kmin, kmax)
+    e1.record(s)
+    torch.cuda.synchronize()
+    t_fwd = e0.elapsed_time(e1)
+    gradient(sol, z0, 2, SEED, kmin, kmax, checkpoint=K)  # warm-up
+    J, gz, gf, _, (tf, tb) = gradient(sol, z0, nsteps, SEED, kmin, kmax, checkpoint=K)
+    g = torch.Generator(device="cpu").manual_seed(3)
+    dz = torch.randn(z0.shape, generator=g, dtype=torch.float64).cuda() * (z0.abs().max() / 4)
+    _, dJ = tlm_run(sol, z0, dz, 0.0, nsteps, SEED, kmin, kmax)
+    adj = float((gz * dz).sum().item())
+    h = 1e-6
+    fd = (forward_objective(sol, z0 + h * dz, nsteps, SEED, kmin, kmax)
+          - forward_objective(sol, z0 - h * dz, nsteps, SEED, kmin, kmax)) / (2 * h)
+    return {"workload": f"{p.n}^2 alpha={p.alpv:g} RK2 dt={p.dt:g}, {nsteps} steps, LCG kick, "
+                        f"J = energy in {kmin:g}<=|k|<={kmax:g}, checkpoint every {K}",
+            "forward_ms": t_fwd, "adjoint_forward_sweep_ms": tf, "adjoint_backward_sweep_ms": tb,
+            "backward_over_forward": tb / t_fwd, "gradient_over_forward": (tf + tb) / t_fwd,
+            "J": J, "J_plain_forward": J_fwd, "dJdfamp": gf,
+            "dot_test_rel": abs(adj - dJ) / abs(dJ), "fd_vs_tlm_rel": abs(fd - dJ) / abs(dJ),
+            "fd_step": h}
 
 
 def ensemble_run(steps, warm, torch):

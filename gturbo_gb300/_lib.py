@@ -68,6 +68,14 @@ def load(path: str | None = None):
         "gt_diag": ([P, D, D, H, H, H, H, H], ctypes.c_int),
         "gt_diag_static": ([ctypes.POINTER(GtParams), D, D, D, D, D, D, D, P], ctypes.c_int),
         "gt_forcing_philox": ([P, D, ctypes.c_uint64, ctypes.c_uint64], ctypes.c_int),
+        "gt_objective": ([P, D, ctypes.c_double, ctypes.c_double, H, D], ctypes.c_int),
+        "gt_tlm_step_rk2": ([P, D, D, ctypes.c_double, I32P, ctypes.POINTER(P)], ctypes.c_int),
+        "gt_adj_stage": ([P, D, D, ctypes.POINTER(P)], ctypes.c_int),
+        "gt_adj_step_rk2": ([P, D, D, D, ctypes.c_int32, H, ctypes.POINTER(P)], ctypes.c_int),
+        "gt_adj_gradient": ([P, D, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                             ctypes.c_double, H, D, H, D, H], ctypes.c_int),
+        "gt_tlm_run": ([P, D, D, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                        ctypes.c_double, H, H], ctypes.c_int),
         "gt_ens_create": ([ctypes.POINTER(GtParams), ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64),
                            ctypes.POINTER(P)], ctypes.c_int),
         "gt_ens_destroy": ([P], ctypes.c_int),

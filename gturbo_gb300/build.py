@@ -31,7 +31,8 @@ def _nvcc() -> str:
 def sources() -> list[str]:
     units = sorted(f for f in os.listdir(CSRC) if f.startswith("gt_inst_") and f.endswith(".cu"))
     return [os.path.join(CSRC, f) for f in units] + [os.path.join(CSRC, "gturbo.cu"),
-                                                      os.path.join(CSRC, "gt_ens.cu")]
+                                                      os.path.join(CSRC, "gt_ens.cu"),
+                                                      os.path.join(CSRC, "gt_adj.cu")]
 
 
 def _deps() -> list[str]:

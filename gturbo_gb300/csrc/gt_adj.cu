@@ -1,0 +1,491 @@
+// gt_adj.cu -- tangent-linear model, discrete adjoint and the checkpointed gradient driver of
+// the Lawson RK2 step with the LCG forcing kick (no counterpart in the reference).
+//
+// Objective: J(z) = sum over kmin <= |k| <= kmax of fac |z|^2 / |k|^alpha, the reference's
+// energy weights (fac = 1/2 on the kx=0 and Nyquist columns, src/diagnostics.f90:150-156).
+// Parameters: the state entries (real and imaginary parts of the stored half-spectrum) and the
+// forcing amplitude famp; the forcing phases are the reference's LCG sequence from a seed.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gturbo.h"
+#include "gt_internal.h"
+#include "gt_ops.h"
+
+namespace gt {
+
+// per-row partial sums of J (and its gradient), fixed-order tree reduction
+__global__ void k_objective_rows(const double2* __restrict__ z, const double* __restrict__ fkxs,
+                                 const double* __restrict__ fkys, const double* __restrict__ kainv,
+                                 int nh, double k2lo, double k2hi, double* rowsum, double2* grad) {
+  const int j = blockIdx.x;
+  double acc = 0.0;
+  const double ky2 = fkys[j];
+  for (int i = threadIdx.x; i < nh; i += blockDim.x) {
+    const size_t o = (size_t)j * nh + i;
+    const double k2 = fkxs[i] + ky2;
+    const bool in = k2 >= k2lo && k2 <= k2hi && !(i == 0 && j == 0);
+    const double fac = (i == 0 || i == nh - 1) ? 0.5 : 1.0;
+    const double2 q = z[o];
+    const double w = in ? fac * kainv[o] : 0.0;
+    acc += w * (q.x * q.x + q.y * q.y);
+    if (grad) grad[o] = make_double2(2.0 * w * q.x, 2.0 * w * q.y);
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) rowsum[j] = red[0];
+}
+
+// <a, b> = sum Re(conj a b) per row
+__global__ void k_dot_rows(const double2* __restrict__ a, const double2* __restrict__ b, int nh,
+                           double* rowsum) {
+  const int j = blockIdx.x;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nh; i += blockDim.x) {
+    const size_t o = (size_t)j * nh + i;
+    acc += a[o].x * b[o].x + a[o].y * b[o].y;
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) rowsum[j] = red[0];
+}
+
+__global__ void k_sum_in_order(const double* __restrict__ x, int n, double* out) {
+  if (threadIdx.x != 0) return;
+  double s = 0.0;
+  for (int k = 0; k < n; ++k) s += x[k];
+  *out = s;
+}
+
+// <lam, g> for the unit-amplitude kick g of the LCG state seed0 (forcing.f90:16-33 with famp
+// factored out): sdt (cos te, sin te) on each forced mode, sdt (cos te, -sin te) on the
+// conjugate partner of the kx=0 and Nyquist modes.
+__global__ void k_forcing_dot(const double2* __restrict__ lam, int nh, int nf, const int* __restrict__ ikx,
+                              const int* __restrict__ iky, const int* __restrict__ jc,
+                              const uint32_t* __restrict__ lcga, const uint32_t* __restrict__ lcgb,
+                              uint32_t seed0, double sdt, double* out) {
+  const double pi2 = 2.0 * 3.14159265358979;
+  double acc = 0.0;
+  for (int k = threadIdx.x; k < nf; k += blockDim.x) {
+    const uint32_t x = (lcga[k] * seed0 + lcgb[k]) & 0x7FFFFFFFu;
+    const float rr = (float)((double)x / 2147483647.0);
+    double cs, cc;
+    sincos(pi2 * (double)rr, &cs, &cc);
+    const int i = ikx[k], j = iky[k];
+    const double2 l = lam[(size_t)j * nh + i];
+    acc += sdt * (l.x * cc + l.y * cs);
+    if (i == 0 || i == nh - 1) {
+      const double2 lc = lam[(size_t)jc[j] * nh + i];
+      acc += sdt * (lc.x * cc - lc.y * cs);
+    }
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+}  // namespace gt
+
+namespace {
+
+int afail(gt_handle* h, int code, const std::string& msg) { return gt::set_error(h, code, msg.c_str()); }
+
+int acuda(gt_handle* h, cudaError_t e, const char* what) {
+  return afail(h, GT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define GA_CUDA(h, call)                                 \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return acuda(h, e_, #call);   \
+  } while (0)
+
+int check_adj(gt_handle* h) {
+  if (!h) return afail(nullptr, GT_ERR_ARG, "null handle");
+  const gt_params* p = gt::handle_params(h);
+  if (p->n > GT_ADJ_MAX_N) return afail(h, GT_ERR_ARG, "adjoint / tangent-linear: n must be <= GT_ADJ_MAX_N (4096)");
+  if (gt::handle_rko(h) != 2) return afail(h, GT_ERR_ARG, "adjoint / tangent-linear: RK2 only");
+  return GT_OK;
+}
+
+gt::GtOp op_of(const gt_handle* h, int kind) {
+  gt::GtOp op;
+  std::memset(&op, 0, sizeof(op));
+  op.kind = kind;
+  op.stream = gt::handle_stream(h);
+  return op;
+}
+
+int run3(gt_handle* h, gt::GtOp op, int k0) {
+  for (int k = 0; k < 3; ++k) {
+    op.kind = k0 + k;
+    const cudaError_t e = gt::handle_dispatch(h, op);
+    if (e != cudaSuccess) return acuda(h, e, "adjoint launch");
+  }
+  return GT_OK;
+}
+
+size_t field_bytes(const gt_handle* h) {
+  const int n = gt::handle_params(h)->n;
+  return sizeof(double) * (size_t)(n + 2) * n;
+}
+
+// objective into d_out (device double), gradient into grad (device, may be null)
+int objective_dev(gt_handle* h, const double* z, double kmin, double kmax, double* grad,
+                  double* d_rows, double* d_out) {
+  const gt_params* p = gt::handle_params(h);
+  const int n = p->n, nh = n / 2 + 1;
+  const double *fkxs, *fkys;
+  gt::handle_k2(h, &fkxs, &fkys);
+  const gt::NltArgs t = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, nullptr);
+  cudaStream_t s = gt::handle_stream(h);
+  gt::k_objective_rows<<<n, 256, 0, s>>>(reinterpret_cast<const double2*>(z), fkxs, fkys, t.kainv, nh,
+                                         kmin * kmin, kmax * kmax, d_rows, reinterpret_cast<double2*>(grad));
+  gt::k_sum_in_order<<<1, 32, 0, s>>>(d_rows, n, d_out);
+  GA_CUDA(h, cudaGetLastError());
+  return GT_OK;
+}
+
+int forcing_dot_dev(gt_handle* h, const double* lam, uint32_t seed0, double* d_out) {
+  const gt::ForcingView f = gt::handle_forcing(h);
+  if (f.nf == 0) {
+    GA_CUDA(h, cudaMemsetAsync(d_out, 0, sizeof(double), gt::handle_stream(h)));
+    return GT_OK;
+  }
+  gt::k_forcing_dot<<<1, 256, 0, gt::handle_stream(h)>>>(reinterpret_cast<const double2*>(lam), f.nh, f.nf,
+                                                         f.ikx, f.iky, f.jc, f.lcga, f.lcgb, seed0, f.sdt, d_out);
+  GA_CUDA(h, cudaGetLastError());
+  return GT_OK;
+}
+
+// w = P0 e (z + dt/2 N(z)): the forward stage A with the fused passes (work: 3 fields)
+int stage_a(gt_handle* h, const double* z, double* w, double* const* work) {
+  gt::GtOp op = op_of(h, gt::OP_NLT_COLINV);
+  op.nlt = gt::handle_nlt_args(h, z, work[0], work[1], work[2], gt::handle_flag(h));
+  op.nlt.epi.mode = gt::EPI_RK2A;
+  op.nlt.epi.out = reinterpret_cast<double2*>(w);
+  op.nlt.epi.z = reinterpret_cast<const double2*>(z);
+  return run3(h, op, gt::OP_NLT_COLINV);
+}
+
+// z_next = P0 e (e z + dt N(w)) written to `out` (may alias z) (work: 3 fields)
+int stage_b(gt_handle* h, const double* w, double* out, double* const* work) {
+  gt::GtOp op = op_of(h, gt::OP_NLT_COLINV);
+  op.nlt = gt::handle_nlt_args(h, w, work[0], work[1], work[2], gt::handle_flag(h));
+  op.nlt.epi.mode = gt::EPI_RK2B;
+  op.nlt.epi.out = reinterpret_cast<double2*>(out);
+  op.nlt.epi.z = reinterpret_cast<const double2*>(out);
+  return run3(h, op, gt::OP_NLT_COLINV);
+}
+
+gt::TlmArgs tlm_args(const gt_handle* h) {
+  const gt::NltArgs t = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, nullptr);
+  gt::TlmArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.n = t.n;
+  a.kainv = t.kainv;
+  a.fkx = t.fkx;
+  a.fky = t.fky;
+  a.kcut = t.kcut;
+  a.tw = t.tw;
+  a.truncate = t.truncate;
+  a.emk = t.epi.emk;
+  a.emkx = t.epi.emkx;
+  a.emky = t.epi.emky;
+  a.split = t.epi.split;
+  a.dt = t.epi.dt;
+  a.dt2 = t.epi.dt2;
+  return a;
+}
+
+gt::AdjArgs adj_args(const gt_handle* h) {
+  const gt::TlmArgs t = tlm_args(h);
+  gt::AdjArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.n = t.n;
+  a.kainv = t.kainv;
+  a.fkx = t.fkx;
+  a.fky = t.fky;
+  a.kcut = t.kcut;
+  a.tw = t.tw;
+  a.truncate = t.truncate;
+  a.emk = t.emk;
+  a.emkx = t.emkx;
+  a.emky = t.emky;
+  a.split = t.split;
+  a.dt = t.dt;
+  a.dt2 = t.dt2;
+  return a;
+}
+
+// one adjoint step (without the forcing dot), work: q, u, v, a, b, rho
+int adj_step(gt_handle* h, const double* z, const double* w, double* lam, double* const* work) {
+  gt::GtOp op = op_of(h, gt::OP_ADJ_COLINV);
+  gt::AdjArgs a = adj_args(h);
+  a.q = reinterpret_cast<double2*>(work[0]);
+  a.u = reinterpret_cast<double2*>(work[1]);
+  a.v = reinterpret_cast<double2*>(work[2]);
+  a.a = reinterpret_cast<double2*>(work[3]);
+  a.b = reinterpret_cast<double2*>(work[4]);
+  a.rho = reinterpret_cast<double2*>(work[5]);
+  a.lam = reinterpret_cast<double2*>(lam);
+  // second half of the step: linearised at w, input l'
+  a.mode = gt::ADJ_STAGE_B;
+  a.x = reinterpret_cast<const double2*>(w);
+  a.lin = reinterpret_cast<const double2*>(lam);
+  op.adj = a;
+  int rc = run3(h, op, gt::OP_ADJ_COLINV);
+  if (rc) return rc;
+  // first half: linearised at z, input rho
+  a.mode = gt::ADJ_STAGE_A;
+  a.x = reinterpret_cast<const double2*>(z);
+  a.lin = a.rho;
+  op.adj = a;
+  return run3(h, op, gt::OP_ADJ_COLINV);
+}
+
+struct DevPool {
+  std::vector<void*> ptrs;
+  ~DevPool() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  double* field(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    return static_cast<double*>(p);
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int gt_objective(gt_handle* h, const double* z, double kmin, double kmax, double* J, double* grad) {
+  if (!h || !z || !J) return afail(h, GT_ERR_ARG, "gt_objective: null argument");
+  DevPool pool;
+  const int n = gt::handle_params(h)->n;
+  double* rows = pool.field(sizeof(double) * (n + 1));
+  if (!rows) return afail(h, GT_ERR_NOMEM, "gt_objective: cudaMalloc");
+  int rc = objective_dev(h, z, kmin, kmax, grad, rows, rows + n);
+  if (rc) return rc;
+  GA_CUDA(h, cudaMemcpyAsync(J, rows + n, sizeof(double), cudaMemcpyDeviceToHost, gt::handle_stream(h)));
+  GA_CUDA(h, cudaStreamSynchronize(gt::handle_stream(h)));
+  return GT_OK;
+}
+
+int gt_tlm_step_rk2(gt_handle* h, double* z, double* dz, double dfamp, int32_t* seed, double* const* work) {
+  int rc = check_adj(h);
+  if (rc) return rc;
+  if (!z || !dz || !seed || !work) return afail(h, GT_ERR_ARG, "gt_tlm_step_rk2: null argument");
+  for (int k = 0; k < 8; ++k)
+    if (!work[k]) return afail(h, GT_ERR_ARG, "gt_tlm_step_rk2: null work field");
+  gt::GtOp op = op_of(h, gt::OP_TLM_COLINV);
+  gt::TlmArgs a = tlm_args(h);
+  a.q = reinterpret_cast<double2*>(work[2]);
+  a.u = reinterpret_cast<double2*>(work[3]);
+  a.v = reinterpret_cast<double2*>(work[4]);
+  a.dq = reinterpret_cast<double2*>(work[5]);
+  a.du = reinterpret_cast<double2*>(work[6]);
+  a.dv = reinterpret_cast<double2*>(work[7]);
+  a.z = reinterpret_cast<double2*>(z);
+  a.dz = reinterpret_cast<double2*>(dz);
+  a.w = reinterpret_cast<double2*>(work[0]);
+  a.dw = reinterpret_cast<double2*>(work[1]);
+  a.mode = gt::TLM_STAGE_A;
+  a.x = a.z;
+  a.dx = a.dz;
+  op.tlm = a;
+  rc = run3(h, op, gt::OP_TLM_COLINV);
+  if (rc) return rc;
+  a.mode = gt::TLM_STAGE_B;
+  a.x = a.w;
+  a.dx = a.dw;
+  op.tlm = a;
+  rc = run3(h, op, gt::OP_TLM_COLINV);
+  if (rc) return rc;
+  const uint32_t s0 = (uint32_t)(*seed);
+  GA_CUDA(h, gt::forcing_amp(h, z, s0, gt::handle_params(h)->famp));
+  GA_CUDA(h, gt::forcing_amp(h, dz, s0, dfamp));
+  const gt::ForcingView f = gt::handle_forcing(h);
+  if (f.nf > 0) *seed = (int32_t)((f.lcga_nf * s0 + f.lcgb_nf) & 0x7FFFFFFFu);
+  return GT_OK;
+}
+
+int gt_adj_stage(gt_handle* h, const double* z, double* w, double* const* work) {
+  int rc = check_adj(h);
+  if (rc) return rc;
+  if (!z || !w || !work || !work[0] || !work[1] || !work[2]) return afail(h, GT_ERR_ARG, "gt_adj_stage: null argument");
+  return stage_a(h, z, w, work);
+}
+
+int gt_adj_step_rk2(gt_handle* h, const double* z, const double* w, double* lam, int32_t seed,
+                    double* gfamp, double* const* work) {
+  int rc = check_adj(h);
+  if (rc) return rc;
+  if (!z || !w || !lam || !work) return afail(h, GT_ERR_ARG, "gt_adj_step_rk2: null argument");
+  for (int k = 0; k < 6; ++k)
+    if (!work[k]) return afail(h, GT_ERR_ARG, "gt_adj_step_rk2: null work field");
+  if (gfamp) {
+    DevPool pool;
+    double* d = pool.field(sizeof(double));
+    if (!d) return afail(h, GT_ERR_NOMEM, "gt_adj_step_rk2: cudaMalloc");
+    rc = forcing_dot_dev(h, lam, (uint32_t)seed, d);
+    if (rc) return rc;
+    double v = 0.0;
+    GA_CUDA(h, cudaMemcpyAsync(&v, d, sizeof(double), cudaMemcpyDeviceToHost, gt::handle_stream(h)));
+    GA_CUDA(h, cudaStreamSynchronize(gt::handle_stream(h)));
+    *gfamp += v;
+  }
+  return adj_step(h, z, w, lam, work);
+}
+
+int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed, int32_t K, double kmin,
+                    double kmax, double* J, double* grad_z0, double* grad_famp, double* zT, double* times_ms) {
+  int rc = check_adj(h);
+  if (rc) return rc;
+  if (!z0 || !J || !grad_z0 || nsteps < 1 || K < 1) return afail(h, GT_ERR_ARG, "gt_adj_gradient: bad argument");
+  cudaStream_t s = gt::handle_stream(h);
+  const size_t fb = field_bytes(h);
+  const int n = gt::handle_params(h)->n;
+  const int ncp = (nsteps + K - 1) / K;
+  DevPool pool;
+  std::vector<double*> cp(ncp), zs(K), ws(K), work(6);
+  for (auto& p : cp) p = pool.field(fb);
+  for (auto& p : zs) p = pool.field(fb);
+  for (auto& p : ws) p = pool.field(fb);
+  for (auto& p : work) p = pool.field(fb);
+  double* z = pool.field(fb);
+  double* lam = pool.field(fb);
+  double* scal = pool.field(sizeof(double) * ((size_t)nsteps + n + 2));
+  if (pool.ptrs.size() != (size_t)(ncp + 2 * K + 6 + 3))
+    return afail(h, GT_ERR_NOMEM, "gt_adj_gradient: cudaMalloc of the checkpoint storage failed");
+  double* dots = scal;           // [nsteps]
+  double* rows = scal + nsteps;  // [n + 1], objective scratch + result
+  cudaEvent_t e0, e1, e2;
+  GA_CUDA(h, cudaEventCreate(&e0));
+  GA_CUDA(h, cudaEventCreate(&e1));
+  GA_CUDA(h, cudaEventCreate(&e2));
+  std::vector<int32_t> seeds(nsteps);
+  GA_CUDA(h, cudaEventRecord(e0, s));
+  // forward sweep, checkpoint every K steps
+  GA_CUDA(h, cudaMemcpyAsync(z, z0, fb, cudaMemcpyDeviceToDevice, s));
+  int32_t sd = seed;
+  for (int st = 0; st < nsteps; ++st) {
+    if (st % K == 0) GA_CUDA(h, cudaMemcpyAsync(cp[st / K], z, fb, cudaMemcpyDeviceToDevice, s));
+    seeds[st] = sd;
+    rc = stage_a(h, z, ws[0], work.data());
+    if (!rc) rc = stage_b(h, ws[0], z, work.data());
+    if (!rc) rc = gt_forcing(h, z, &sd);
+    if (rc) return rc;
+  }
+  if (zT) GA_CUDA(h, cudaMemcpyAsync(zT, z, fb, cudaMemcpyDeviceToDevice, s));
+  rc = objective_dev(h, z, kmin, kmax, lam, rows, rows + n);
+  if (rc) return rc;
+  GA_CUDA(h, cudaEventRecord(e1, s));
+  // backward sweep: per segment, recompute and store (z_s, w_s), then run the adjoint back
+  for (int c = ncp - 1; c >= 0; --c) {
+    const int s0 = c * K, s1 = (s0 + K < nsteps) ? s0 + K : nsteps;
+    GA_CUDA(h, cudaMemcpyAsync(zs[0], cp[c], fb, cudaMemcpyDeviceToDevice, s));
+    for (int st = s0; st < s1; ++st) {
+      const int r = st - s0;
+      rc = stage_a(h, zs[r], ws[r], work.data());
+      if (rc) return rc;
+      if (st + 1 < s1) {
+        GA_CUDA(h, cudaMemcpyAsync(zs[r + 1], zs[r], fb, cudaMemcpyDeviceToDevice, s));
+        rc = stage_b(h, ws[r], zs[r + 1], work.data());
+        int32_t sk = seeds[st];
+        if (!rc) rc = gt_forcing(h, zs[r + 1], &sk);
+        if (rc) return rc;
+      }
+    }
+    for (int st = s1 - 1; st >= s0; --st) {
+      const int r = st - s0;
+      rc = forcing_dot_dev(h, lam, (uint32_t)seeds[st], dots + st);
+      if (!rc) rc = adj_step(h, zs[r], ws[r], lam, work.data());
+      if (rc) return rc;
+    }
+  }
+  GA_CUDA(h, cudaEventRecord(e2, s));
+  GA_CUDA(h, cudaMemcpyAsync(grad_z0, lam, fb, cudaMemcpyDeviceToDevice, s));
+  std::vector<double> host(nsteps + 1);
+  GA_CUDA(h, cudaMemcpyAsync(host.data(), dots, sizeof(double) * nsteps, cudaMemcpyDeviceToHost, s));
+  GA_CUDA(h, cudaMemcpyAsync(host.data() + nsteps, rows + n, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GA_CUDA(h, cudaStreamSynchronize(s));
+  *J = host[nsteps];
+  if (grad_famp) {
+    double g = 0.0;
+    for (int st = 0; st < nsteps; ++st) g += host[st];
+    *grad_famp = g;
+  }
+  if (times_ms) {
+    float f = 0.f, b = 0.f;
+    cudaEventElapsedTime(&f, e0, e1);
+    cudaEventElapsedTime(&b, e1, e2);
+    times_ms[0] = f;
+    times_ms[1] = b;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  return GT_OK;
+}
+
+int gt_tlm_run(gt_handle* h, const double* z0, const double* dz0, double dfamp, int32_t nsteps, int32_t seed,
+               double kmin, double kmax, double* J, double* dJ) {
+  int rc = check_adj(h);
+  if (rc) return rc;
+  if (!z0 || !dz0 || !J || !dJ || nsteps < 0) return afail(h, GT_ERR_ARG, "gt_tlm_run: bad argument");
+  cudaStream_t s = gt::handle_stream(h);
+  const size_t fb = field_bytes(h);
+  const int n = gt::handle_params(h)->n;
+  DevPool pool;
+  double* z = pool.field(fb);
+  double* dz = pool.field(fb);
+  double* grad = pool.field(fb);
+  std::vector<double*> work(8);
+  for (auto& p : work) p = pool.field(fb);
+  double* rows = pool.field(sizeof(double) * (2 * (size_t)n + 2));
+  if (pool.ptrs.size() != 12) return afail(h, GT_ERR_NOMEM, "gt_tlm_run: cudaMalloc failed");
+  GA_CUDA(h, cudaMemcpyAsync(z, z0, fb, cudaMemcpyDeviceToDevice, s));
+  GA_CUDA(h, cudaMemcpyAsync(dz, dz0, fb, cudaMemcpyDeviceToDevice, s));
+  int32_t sd = seed;
+  for (int st = 0; st < nsteps; ++st) {
+    rc = gt_tlm_step_rk2(h, z, dz, dfamp, &sd, work.data());
+    if (rc) return rc;
+  }
+  rc = objective_dev(h, z, kmin, kmax, grad, rows, rows + n);
+  if (rc) return rc;
+  gt::k_dot_rows<<<n, 256, 0, s>>>(reinterpret_cast<const double2*>(grad), reinterpret_cast<const double2*>(dz),
+                                   n / 2 + 1, rows + n + 1);
+  gt::k_sum_in_order<<<1, 32, 0, s>>>(rows + n + 1, n, rows + 2 * n + 1);
+  GA_CUDA(h, cudaGetLastError());
+  double out[2];
+  GA_CUDA(h, cudaMemcpyAsync(&out[0], rows + n, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GA_CUDA(h, cudaMemcpyAsync(&out[1], rows + 2 * n + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GA_CUDA(h, cudaStreamSynchronize(s));
+  *J = out[0];
+  *dJ = out[1];
+  return GT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,519 @@
+// gt_adjoint.cuh -- tangent-linear and discrete adjoint of the nonlinear term and of the Lawson
+// RK2 step (no counterpart in the reference). Same three-pass structure and FFT engine as
+// the forward passes; N <= 4096 (the row passes keep 3 length-N rows in shared memory).
+//
+// Notation: F(q) = T o R[-i kx (u q) - i ky (v q)] with q, u, v = C2R(q^), C2R(Mu q^), C2R(Mv q^),
+// Mu = i ky/|k|^a, Mv = -i kx/|k|^a, R = D2Z/N^2 (normalised forward) and T the 2/3 mask.
+// The state space is the stored half-spectrum with the real inner product
+// <a, b> = sum Re(conj(a) b); there C2R^T = c o D2Z (c = 2 on interior columns, 1 on the kx=0
+// and Nyquist columns) and R^T = C2R(w o .)/N^2 (w = 1/2 interior, 1 on those two columns), so
+//   dF(q; dq)   = T o R[-i kx (du q + u dq) - i ky (dv q + v dq)]
+//   dF(q)^T l   = c o D2Z[u a + v b] + conj(Mu) c o D2Z[q a] + conj(Mv) c o D2Z[q b],
+//                 a, b = C2R(w o i kx T l)/N^2, C2R(w o i ky T l)/N^2.
+#pragma once
+
+#include "gt_kernels.cuh"
+
+namespace gt {
+
+// ---------------------------------------------------------------------------------------
+// Tangent-linear: the forward nonlinear term and its derivative in one pass sequence.
+// ---------------------------------------------------------------------------------------
+enum TlmMode : int {
+  TLM_STAGE_A = 0,  // w = P0 e (z + dt/2 N),      dw = P0 e (dz + dt/2 dN)
+  TLM_STAGE_B = 1,  // z = P0 e (e z + dt N),       dz = P0 e (e dz + dt dN)   (in place)
+};
+
+struct TlmArgs {
+  int n;
+  const double2* x;   // stage input (state)
+  const double2* dx;  // stage input (tangent)
+  double2 *q, *u, *v, *dq, *du, *dv;  // scratch; A, B, dA, dB leave in u, v, du, dv
+  const double* kainv;
+  const double* fkx;
+  const double* fky;
+  const int* kcut;
+  const double2* tw;
+  int truncate;
+  int mode;
+  double2* z;         // step-start state (read; written by stage B)
+  double2* dz;        // step-start tangent (read; written by stage B)
+  double2* w;         // stage A outputs
+  double2* dw;
+  const double* emk;
+  const double* emkx;
+  const double* emky;
+  int split;
+  double dt, dt2;
+};
+
+__device__ __forceinline__ double stage_e(const double* emk, const double* emkx, const double* emky,
+                                          int split, int i, int j, int NH) {
+  return split ? __ldg(&emkx[i]) * __ldg(&emky[j]) : __ldg(&emk[(size_t)j * NH + i]);
+}
+
+template <int N, int C>
+__device__ __forceinline__ void tlm_colinv_tile(const TlmArgs& a, int tile) {
+  constexpr int T = N / 16, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  const int i = tile * C + c;
+  const bool valid = i < NH;
+  const int ic = valid ? i : NH - 1;
+  double2* sm = smem + c;
+  const double kx = __ldg(&a.fkx[ic]);
+  double2 v[16];
+  for (int f = 0; f < 6; ++f) {
+    const double2* src = f < 3 ? a.x : a.dx;
+    double2* dst = f == 0 ? a.q : f == 1 ? a.u : f == 2 ? a.v : f == 3 ? a.dq : f == 4 ? a.du : a.dv;
+    const int kind = f % 3;  // 0: q, 1: Mu q, 2: Mv q
+#pragma unroll
+    for (int s = 0; s < 16; ++s) {
+      const int j = t + s * T;
+      const size_t o = (size_t)j * NH + ic;
+      const double2 q = valid ? src[o] : czero();
+      if (kind == 0) {
+        v[s] = q;
+      } else if (kind == 1) {
+        const double m = __ldg(&a.fky[j]) * __ldg(&a.kainv[o]);
+        v[s] = make_double2(-m * q.y, m * q.x);
+      } else {
+        const double m = kx * __ldg(&a.kainv[o]);
+        v[s] = make_double2(m * q.y, -m * q.x);
+      }
+    }
+    __syncthreads();
+    fft_regs<N, 16, true, C>(v, sm, t, a.tw, 0);
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < 16; ++s) dst[(size_t)(t + s * T) * NH + i] = v[s];
+    }
+  }
+}
+
+// X + iY as one complex spectrum of length N from two half spectra (Im at k=0, N/2 dropped)
+template <int N>
+__device__ __forceinline__ void pair_spectrum(double2* cs, const double2* xrow, const double2* yrow, int t) {
+  constexpr int T = N / 16, M = N / 2;
+#pragma unroll
+  for (int s = 0; s <= 8; ++s) {
+    const int k = t + s * T;
+    if (k <= M) {
+      const double2 X = xrow[k], Y = yrow[k];
+      if (k == 0 || k == M) {
+        cs[padix(k)] = make_double2(X.x, Y.x);
+      } else {
+        cs[padix(k)] = make_double2(X.x - Y.y, X.y + Y.x);
+        cs[padix(N - k)] = make_double2(X.x + Y.y, Y.x - X.y);
+      }
+    }
+  }
+}
+
+// split P (length N, in smem) into 2 FFT(Re p)[k] -> xrow, 2 FFT(Im p)[k] -> yrow, k <= N/2
+template <int N>
+__device__ __forceinline__ void split_spectrum(const double2* cs, double2* xrow, double2* yrow, int t) {
+  constexpr int T = N / 16, M = N / 2;
+#pragma unroll
+  for (int s = 0; s <= 8; ++s) {
+    const int k = t + s * T;
+    if (k <= M) {
+      const double2 P = cs[padix(k)];
+      const double2 Q = cs[padix((N - k) & (N - 1))];
+      xrow[k] = make_double2(P.x + Q.x, P.y - Q.y);
+      yrow[k] = make_double2(P.y + Q.y, Q.x - P.x);
+    }
+  }
+}
+
+template <int N, int ROWS>
+__device__ __forceinline__ void tlm_row_tile(const TlmArgs& a, int tile) {
+  constexpr int T = N / 16, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  const int r = threadIdx.x / T, t = threadIdx.x % T;
+  const int y = tile * ROWS + r;
+  double2* c1 = smem + (size_t)r * 3 * padded(N);
+  double2* c2 = c1 + padded(N);
+  double2* c3 = c2 + padded(N);
+  const size_t ro = (size_t)y * NH;
+  pair_spectrum<N>(c1, a.u + ro, a.v + ro, t);    // u + i v
+  pair_spectrum<N>(c2, a.du + ro, a.dv + ro, t);  // du + i dv
+  pair_spectrum<N>(c3, a.q + ro, a.dq + ro, t);   // q + i dq
+  __syncthreads();
+  double2 v[16];
+  double2* bufs[3] = {c1, c2, c3};
+  for (int b = 0; b < 3; ++b) {
+#pragma unroll
+    for (int s = 0; s < 16; ++s) v[s] = bufs[b][padix(t + s * T)];
+    __syncthreads();
+    fft_regs<N, 16, true, 1>(v, bufs[b], t, a.tw, 0);
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 16; ++s) bufs[b][padix(t + s * T)] = v[s];
+  }
+  __syncthreads();
+  // products: p = (u + i v) q, dp = (du + i dv) q + (u + i v) dq
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    const int x = padix(t + s * T);
+    const double2 uv = c1[x], duv = c2[x], qq = c3[x];
+    c1[x] = make_double2(uv.x * qq.x, uv.y * qq.x);
+    c2[x] = make_double2(fma(duv.x, qq.x, uv.x * qq.y), fma(duv.y, qq.x, uv.y * qq.y));
+  }
+  __syncthreads();
+  for (int b = 0; b < 2; ++b) {
+#pragma unroll
+    for (int s = 0; s < 16; ++s) v[s] = bufs[b][padix(t + s * T)];
+    __syncthreads();
+    fft_regs<N, 16, false, 1>(v, bufs[b], t, a.tw, 0);
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 16; ++s) bufs[b][padix(t + s * T)] = v[s];
+  }
+  __syncthreads();
+  split_spectrum<N>(c1, a.u + ro, a.v + ro, t);
+  split_spectrum<N>(c2, a.du + ro, a.dv + ro, t);
+}
+
+template <int N, int C>
+__device__ __forceinline__ void tlm_colfwd_tile(const TlmArgs& a, int tile) {
+  constexpr int T = N / 16, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  const int i = tile * C + c;
+  const bool valid = i < NH;
+  const int ic = valid ? i : NH - 1;
+  double2* sm = smem + c;
+  const double scale = 0.5 / ((double)N * (double)N);
+  const double kxs = __ldg(&a.fkx[ic]) * scale;
+  const int kc = a.truncate ? (valid ? __ldg(&a.kcut[i]) : -1) : N;
+  double2 v[16];
+  for (int pr = 0; pr < 2; ++pr) {
+    double2* af = pr == 0 ? a.u : a.du;
+    const double2* bf = pr == 0 ? a.v : a.dv;
+#pragma unroll
+    for (int s = 0; s < 16; ++s) v[s] = valid ? af[(size_t)(t + s * T) * NH + ic] : czero();
+    __syncthreads();
+    fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < 16; ++s)
+        af[(size_t)(t + s * T) * NH + i] = make_double2(kxs * v[s].x, kxs * v[s].y);
+    }
+#pragma unroll
+    for (int s = 0; s < 16; ++s) v[s] = valid ? bf[(size_t)(t + s * T) * NH + ic] : czero();
+    __syncthreads();
+    fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < 16; ++s) {
+        const int j = t + s * T;
+        const size_t o = (size_t)j * NH + i;
+        const double kys = __ldg(&a.fky[j]) * scale;
+        const double2 fa = af[o];
+        double2 nh = make_double2(fma(kys, v[s].y, fa.y), -fma(kys, v[s].x, fa.x));
+        if (min(j, N - j) > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
+        af[o] = nh;  // N (pr = 0) or dN (pr = 1) in place of A / dA
+      }
+    }
+  }
+  if (!valid) return;
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    const int j = t + s * T;
+    const size_t o = (size_t)j * NH + i;
+    const double e = stage_e(a.emk, a.emkx, a.emky, a.split, i, j, NH);
+    const bool origin = (i == 0 && j == 0);
+    const double2 nh = a.u[o], dn = a.du[o];
+    const double2 z = a.z[o], dz = a.dz[o];
+    if (a.mode == TLM_STAGE_A) {
+      a.w[o] = origin ? czero() : make_double2(e * (z.x + a.dt2 * nh.x), e * (z.y + a.dt2 * nh.y));
+      a.dw[o] = origin ? czero() : make_double2(e * (dz.x + a.dt2 * dn.x), e * (dz.y + a.dt2 * dn.y));
+    } else {
+      a.z[o] = origin ? czero() : make_double2(e * (e * z.x + a.dt * nh.x), e * (e * z.y + a.dt * nh.y));
+      a.dz[o] = origin ? czero() : make_double2(e * (e * dz.x + a.dt * dn.x), e * (e * dz.y + a.dt * dn.y));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Adjoint of the RK2 step, in two halves (each one transposed nonlinear term):
+//   ADJ_STAGE_B: input lin = l' (gradient after the step), linearisation point x = w:
+//       lw  = dF(w)^T (dt e P0 l')
+//       lam = e e P0 l' + e P0 lw          rho = dt/2 e P0 lw
+//   ADJ_STAGE_A: input lin = rho, linearisation point x = z:
+//       lam += dF(z)^T rho
+// ---------------------------------------------------------------------------------------
+enum AdjMode : int {
+  ADJ_STAGE_B = 0,
+  ADJ_STAGE_A = 1,
+};
+
+struct AdjArgs {
+  int n;
+  const double2* x;    // linearisation point
+  const double2* lin;  // adjoint input (l' or rho)
+  double2 *q, *u, *v, *a, *b;  // scratch; S1, S2, S3 leave in q, u, v
+  const double* kainv;
+  const double* fkx;
+  const double* fky;
+  const int* kcut;
+  const double2* tw;
+  int truncate;
+  int mode;
+  double2* lam;        // output / accumulator
+  double2* rho;        // ADJ_STAGE_B second output
+  const double* emk;
+  const double* emkx;
+  const double* emky;
+  int split;
+  double dt, dt2;
+};
+
+template <int N, int C>
+__device__ __forceinline__ void adj_colinv_tile(const AdjArgs& a, int tile) {
+  constexpr int T = N / 16, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  const int i = tile * C + c;
+  const bool valid = i < NH;
+  const int ic = valid ? i : NH - 1;
+  double2* sm = smem + c;
+  const double kx = __ldg(&a.fkx[ic]);
+  const int kc = a.truncate ? __ldg(&a.kcut[ic]) : N;
+  const double wcol = (ic == 0 || ic == NH - 1) ? 1.0 : 0.5;
+  double2 v[16];
+  for (int f = 0; f < 5; ++f) {
+    double2* dst = f == 0 ? a.q : f == 1 ? a.u : f == 2 ? a.v : f == 3 ? a.a : a.b;
+#pragma unroll
+    for (int s = 0; s < 16; ++s) {
+      const int j = t + s * T;
+      const size_t o = (size_t)j * NH + ic;
+      if (f < 3) {
+        const double2 q = valid ? a.x[o] : czero();
+        if (f == 0) {
+          v[s] = q;
+        } else if (f == 1) {
+          const double m = __ldg(&a.fky[j]) * __ldg(&a.kainv[o]);
+          v[s] = make_double2(-m * q.y, m * q.x);
+        } else {
+          const double m = kx * __ldg(&a.kainv[o]);
+          v[s] = make_double2(m * q.y, -m * q.x);
+        }
+      } else {
+        double2 l = valid ? a.lin[o] : czero();
+        if (a.mode == ADJ_STAGE_B) {
+          const double e = stage_e(a.emk, a.emkx, a.emky, a.split, ic, j, NH) * a.dt;
+          l = (ic == 0 && j == 0) ? czero() : make_double2(e * l.x, e * l.y);
+        }
+        if (min(j, N - j) > kc || (ic == 0 && j == 0 && a.truncate)) l = czero();
+        // w o (i k) l
+        const double k = (f == 3 ? kx : __ldg(&a.fky[j])) * wcol;
+        v[s] = make_double2(-k * l.y, k * l.x);
+      }
+    }
+    __syncthreads();
+    fft_regs<N, 16, true, C>(v, sm, t, a.tw, 0);
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < 16; ++s) dst[(size_t)(t + s * T) * NH + i] = v[s];
+    }
+  }
+}
+
+template <int N, int ROWS>
+__device__ __forceinline__ void adj_row_tile(const AdjArgs& a, int tile) {
+  constexpr int T = N / 16, NH = N / 2 + 1, M = N / 2;
+  extern __shared__ double2 smem[];
+  const int r = threadIdx.x / T, t = threadIdx.x % T;
+  const int y = tile * ROWS + r;
+  double2* c1 = smem + (size_t)r * (2 * padded(N) + padded(M));
+  double2* c2 = c1 + padded(N);
+  double2* zs = c2 + padded(N);
+  const size_t ro = (size_t)y * NH;
+  pair_spectrum<N>(c1, a.u + ro, a.v + ro, t);  // u + i v
+  pair_spectrum<N>(c2, a.a + ro, a.b + ro, t);  // a + i b
+  const double2* qrow = a.q + ro;
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {  // half-length C2R packing of q
+    const int k = t + s * T;
+    double2 p = qrow[k], b = qrow[M - k];
+    if (k == 0) { p.y = 0.0; b.y = 0.0; }
+    const double2 sm_ = make_double2(p.x + b.x, p.y - b.y);
+    const double2 d = make_double2(p.x - b.x, p.y + b.y);
+    const double2 tt = twmul<true>(d, __ldg(&a.tw[k]));
+    zs[padix(k)] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
+  }
+  __syncthreads();
+  {
+    double2 h[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) h[s] = zs[padix(t + s * T)];
+    __syncthreads();
+    fft_regs<M, 8, true, 1>(h, zs, t, a.tw, 1);
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 8; ++s) zs[padix(t + s * T)] = h[s];
+  }
+  double2 v[16];
+  double2* bufs[2] = {c1, c2};
+  for (int b = 0; b < 2; ++b) {
+#pragma unroll
+    for (int s = 0; s < 16; ++s) v[s] = bufs[b][padix(t + s * T)];
+    __syncthreads();
+    fft_regs<N, 16, true, 1>(v, bufs[b], t, a.tw, 0);
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 16; ++s) bufs[b][padix(t + s * T)] = v[s];
+  }
+  __syncthreads();
+  // s1 = u a + v b (into zs, as packed pairs), s2 + i s3 = q (a + i b) (into c2); a, b / N^2
+  const double inv = 1.0 / ((double)N * (double)N);
+  double s1v[16];
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    const int x = t + s * T;
+    const double2 uv = c1[padix(x)];
+    const double2 ab = c2[padix(x)];
+    const double2 zq = zs[padix(x >> 1)];
+    const double q = (x & 1) ? zq.y : zq.x;
+    const double ax = ab.x * inv, bx = ab.y * inv;
+    s1v[s] = fma(uv.x, ax, uv.y * bx);
+    c2[padix(x)] = make_double2(q * ax, q * bx);
+  }
+  __syncthreads();
+  // repack s1 as z[m] = s1[2m] + i s1[2m+1] in zs (x even -> .x, odd -> .y)
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    const int x = t + s * T;
+    double* zd = reinterpret_cast<double*>(zs + padix(x >> 1));
+    zd[x & 1] = s1v[s];
+  }
+  __syncthreads();
+  // forward transforms: s2 + i s3 (length N), s1 (half length)
+#pragma unroll
+  for (int s = 0; s < 16; ++s) v[s] = c2[padix(t + s * T)];
+  __syncthreads();
+  fft_regs<N, 16, false, 1>(v, c2, t, a.tw, 0);
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < 16; ++s) c2[padix(t + s * T)] = v[s];
+  {
+    double2 h[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) h[s] = zs[padix(t + s * T)];
+    __syncthreads();
+    fft_regs<M, 8, false, 1>(h, zs, t, a.tw, 1);
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 8; ++s) zs[padix(t + s * T)] = h[s];
+  }
+  __syncthreads();
+  split_spectrum<N>(c2, a.u + ro, a.v + ro, t);  // 2 FFT(s2), 2 FFT(s3)
+  // 2 FFT(s1)[k] = (Z[k] + conj Z[M-k]) - i W^k (Z[k] - conj Z[M-k]), k in [0, M]
+  double2* s1row = a.q + ro;
+#pragma unroll
+  for (int s = 0; s <= 8; ++s) {
+    const int k = t + s * T;
+    if (k <= M) {
+      const double2 p = zs[padix(k & (M - 1))];
+      const double2 b = zs[padix((M - k) & (M - 1))];
+      const double2 sm_ = make_double2(p.x + b.x, p.y - b.y);
+      const double2 d = make_double2(p.x - b.x, p.y + b.y);
+      const double2 tt = twmul<false>(d, __ldg(&a.tw[k]));
+      s1row[k] = make_double2(sm_.x + tt.y, sm_.y - tt.x);
+    }
+  }
+}
+
+template <int N, int C>
+__device__ __forceinline__ void adj_colfwd_tile(const AdjArgs& a, int tile) {
+  constexpr int T = N / 16, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  const int i = tile * C + c;
+  const bool valid = i < NH;
+  const int ic = valid ? i : NH - 1;
+  double2* sm = smem + c;
+  const double kx = __ldg(&a.fkx[ic]);
+  // c o (.)/2: the row pass delivered 2 FFT(s); c = 1 on kx=0 and Nyquist, 2 inside
+  const double cw = (ic == 0 || ic == NH - 1) ? 0.5 : 1.0;
+  double2 v[16];
+  for (int f = 0; f < 3; ++f) {
+    const double2* src = f == 0 ? a.q : f == 1 ? a.u : a.v;
+#pragma unroll
+    for (int s = 0; s < 16; ++s) v[s] = valid ? src[(size_t)(t + s * T) * NH + ic] : czero();
+    __syncthreads();
+    fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < 16; ++s) {
+        const int j = t + s * T;
+        const size_t o = (size_t)j * NH + i;
+        double2 acc;
+        if (f == 0) {
+          acc = make_double2(cw * v[s].x, cw * v[s].y);
+        } else {
+          // conj(Mu) = -i ky/|k|^a, conj(Mv) = +i kx/|k|^a
+          const double m = (f == 1 ? -__ldg(&a.fky[j]) : kx) * __ldg(&a.kainv[o]) * cw;
+          const double2 prev = a.q[o];
+          acc = make_double2(fma(-m, v[s].y, prev.x), fma(m, v[s].x, prev.y));
+        }
+        a.q[o] = acc;
+      }
+    }
+  }
+  if (!valid) return;
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    const int j = t + s * T;
+    const size_t o = (size_t)j * NH + i;
+    const double2 g = a.q[o];
+    if (a.mode == ADJ_STAGE_B) {
+      const double e = stage_e(a.emk, a.emkx, a.emky, a.split, i, j, NH);
+      const bool origin = (i == 0 && j == 0);
+      const double2 l = a.lin[o];
+      a.lam[o] = origin ? czero() : make_double2(e * (e * l.x + g.x), e * (e * l.y + g.y));
+      a.rho[o] = origin ? czero() : make_double2(a.dt2 * e * g.x, a.dt2 * e * g.y);
+    } else {
+      const double2 l = a.lam[o];
+      a.lam[o] = make_double2(l.x + g.x, l.y + g.y);
+    }
+  }
+}
+
+// ---- kernels ------------------------------------------------------------------------------
+template <int N>
+struct AdjShape {
+  static constexpr size_t TLM_ROW_SMEM = (size_t)3 * padded(N) * Shape<N>::ROWS * sizeof(double2);
+  static constexpr size_t ADJ_ROW_SMEM =
+      (size_t)(2 * padded(N) + padded(N / 2)) * Shape<N>::ROWS * sizeof(double2);
+  static constexpr bool OK = (N <= 4096);
+};
+
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::COL_THREADS) k_tlm_colinv(TlmArgs a) {
+  if constexpr (AdjShape<N>::OK) tlm_colinv_tile<N, Shape<N>::COLS>(a, blockIdx.x);
+}
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::ROW_THREADS) k_tlm_row(TlmArgs a) {
+  if constexpr (AdjShape<N>::OK) tlm_row_tile<N, Shape<N>::ROWS>(a, blockIdx.x);
+}
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::COL_THREADS) k_tlm_colfwd(TlmArgs a) {
+  if constexpr (AdjShape<N>::OK) tlm_colfwd_tile<N, Shape<N>::COLS>(a, blockIdx.x);
+}
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::COL_THREADS) k_adj_colinv(AdjArgs a) {
+  if constexpr (AdjShape<N>::OK) adj_colinv_tile<N, Shape<N>::COLS>(a, blockIdx.x);
+}
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::ROW_THREADS) k_adj_row(AdjArgs a) {
+  if constexpr (AdjShape<N>::OK) adj_row_tile<N, Shape<N>::ROWS>(a, blockIdx.x);
+}
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::COL_THREADS) k_adj_colfwd(AdjArgs a) {
+  if constexpr (AdjShape<N>::OK) adj_colfwd_tile<N, Shape<N>::COLS>(a, blockIdx.x);
+}
+
+}  // namespace gt

@@ -23,8 +23,21 @@ struct ForcingView {
   int nf;
   int nh;
   double sf;
+  const uint32_t* lcga;  // LCG jump-ahead of the (k+1)-th draw
+  const uint32_t* lcgb;
+  uint32_t lcga_nf, lcgb_nf;  // jump-ahead of a whole kick (nf draws)
+  double sdt;
 };
 ForcingView handle_forcing(const gt_handle* h);
+// Launch one kernel of the handle's grid size.
+cudaError_t handle_dispatch(const gt_handle* h, const struct GtOp& op);
+// The LCG kick of gt_forcing with amplitude famp (the handle's own famp in gt_forcing);
+// seed0 is the LCG state before the kick.
+cudaError_t forcing_amp(gt_handle* h, double* z, uint32_t seed0, double famp);
+// k^2 tables of the handle
+void handle_k2(const gt_handle* h, const double** fkxs, const double** fkys);
+// the handle's untruncated-input flag (used by its single-field nonlinear-term passes)
+int* handle_flag(const gt_handle* h);
 
 // Grid size, RK order and the parameters a handle was created with.
 const gt_params* handle_params(const gt_handle* h);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "gt_adjoint.cuh"
 #include "gt_kernels.cuh"
 
 namespace gt {
@@ -17,12 +18,20 @@ enum OpKind : int {
   OP_COL_FWD = 4,     // column forward transform, scaled (fft_dir, second half)
   OP_ROW_C2R = 5,     // row C2R (fft_inv, second half)
   OP_ROW_R2C = 6,     // row R2C (fft_dir, first half)
+  OP_TLM_COLINV = 7,  // tangent-linear passes (N <= 4096)
+  OP_TLM_ROW = 8,
+  OP_TLM_COLFWD = 9,
+  OP_ADJ_COLINV = 10, // adjoint passes (N <= 4096)
+  OP_ADJ_ROW = 11,
+  OP_ADJ_COLFWD = 12,
 };
 
 struct GtOp {
   int kind;
   cudaStream_t stream;
   NltArgs nlt;        // passes A, B, C
+  TlmArgs tlm;
+  AdjArgs adj;
   double2* a;         // field of the standalone transforms
   const double2* tw;
   double scale;

@@ -108,8 +108,30 @@ ForcingView handle_forcing(const gt_handle* h) {
   f.nf = h->nf;
   f.nh = h->NH;
   f.sf = h->sdt * h->p.famp;
+  f.lcga = h->d_lcga;
+  f.lcgb = h->d_lcgb;
+  f.lcga_nf = h->lcga_nf;
+  f.lcgb_nf = h->lcgb_nf;
+  f.sdt = h->sdt;
   return f;
 }
+
+cudaError_t handle_dispatch(const gt_handle* h, const GtOp& op) { return h->dispatch(op); }
+
+cudaError_t forcing_amp(gt_handle* h, double* z, uint32_t seed0, double famp) {
+  if (h->nf == 0) return cudaSuccess;
+  k_forcing<<<(h->nf + 127) / 128, 128, 0, h->stream>>>(
+      reinterpret_cast<double2*>(z), h->NH, h->nf, h->d_ikxf, h->d_ikyf, h->d_jc, h->d_lcga,
+      h->d_lcgb, h->d_ff, seed0, h->sdt * famp);
+  return cudaGetLastError();
+}
+
+void handle_k2(const gt_handle* h, const double** fkxs, const double** fkys) {
+  *fkxs = h->d_fkxs;
+  *fkys = h->d_fkys;
+}
+
+int* handle_flag(const gt_handle* h) { return h->d_flag; }
 
 const gt_params* handle_params(const gt_handle* h) { return &h->p; }
 int handle_rko(const gt_handle* h) { return h->rko; }

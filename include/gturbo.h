@@ -161,6 +161,43 @@ int gt_ens_use_graph(gt_ens* e, int enable);
 int gt_ens_step(gt_ens* e, int32_t nsteps);
 const char* gt_ens_last_error(const gt_ens* e);
 
+/* ---- tangent-linear model and discrete adjoint (no counterpart in the reference) ----
+ * For the Lawson RK2 step (split or not) followed by the LCG kick, on grids
+ * n <= GT_ADJ_MAX_N. The state space is the stored half-spectrum with the real
+ * inner product <a, b> = sum Re(conj(a) b); the parameters are the state and
+ * the forcing amplitude famp (the phases follow the reference's LCG). */
+#define GT_ADJ_MAX_N 4096
+
+/* J(z) = sum over kmin <= |k| <= kmax of fac |z|^2 / |k|^alpha (fac = 1/2 on
+ * the kx=0 and Nyquist columns, the weights of src/diagnostics.f90:150-156).
+ * J: host; grad: device dJ/dz or NULL. Synchronous. */
+int gt_objective(gt_handle* h, const double* z, double kmin, double kmax, double* J, double* grad);
+/* One tangent-linear step: z advances exactly as gt_step_rk2 + gt_forcing(z, seed);
+ * dz advances by the derivative of that step plus dfamp times the kick pattern
+ * of the same LCG draws. *seed advances as in gt_forcing. work: 8 device fields. */
+int gt_tlm_step_rk2(gt_handle* h, double* z, double* dz, double dfamp, int32_t* seed, double* const* work);
+/* Stage state w = P0 e (z + dt/2 N(z)) of the RK2 step from z (work: 3 fields). */
+int gt_adj_stage(gt_handle* h, const double* z, double* w, double* const* work);
+/* Adjoint of one RK2 step + kick: z = state at the step start, w = its stage
+ * state (gt_adj_stage), lam = dJ/d(state after the kick) on entry and dJ/dz on
+ * return; when gfamp != NULL, dJ/dfamp of this kick (LCG state `seed` before it)
+ * is added to *gfamp (host; synchronous). work: 6 device fields. */
+int gt_adj_step_rk2(gt_handle* h, const double* z, const double* w, double* lam, int32_t seed,
+                    double* gfamp, double* const* work);
+/* Gradient of J(z after nsteps of RK2 + kick from seed) with respect to z0 and
+ * famp: a forward sweep that stores a checkpoint every K steps, then a backward
+ * sweep that recomputes each segment's (z_s, w_s) from its checkpoint and runs
+ * gt_adj_step_rk2 back over it. Outputs: J and *grad_famp (host), grad_z0 and
+ * zT (device; zT may be NULL), times_ms[2] = forward / backward sweep times
+ * (may be NULL). Allocates ceil(nsteps/K) + 2K + 8 fields with cudaMalloc for
+ * the duration of the call. Synchronous. */
+int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed, int32_t K,
+                    double kmin, double kmax, double* J, double* grad_z0, double* grad_famp,
+                    double* zT, double* times_ms);
+/* Tangent-linear run: J and its derivative dJ along (dz0, dfamp) after nsteps. */
+int gt_tlm_run(gt_handle* h, const double* z0, const double* dz0, double dfamp, int32_t nsteps,
+               int32_t seed, double kmin, double kmax, double* J, double* dJ);
+
 /* ---- diagnostics (src/diagnostics.f90:5-179) --------------------------- */
 
 /* Shell spectra, fluxes and global budgets of z (and of znl = nlt(z) for the

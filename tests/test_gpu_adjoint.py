@@ -1,0 +1,120 @@
+"""Tangent-linear model and discrete adjoint of the RK2 step + LCG kick, on the GPU.
+
+Checks, for J = energy in the shells 4 <= |k| <= 8 of the final field:
+  * dot-product test: <dJ/dz0, dz0> + dJ/dfamp dfamp == the tangent-linear dJ (same discrete
+    map, both exact derivatives: agreement to roundoff);
+  * FP64 central finite differences (relative step 1e-6) along random directions agree with
+    the tangent-linear dJ to 1e-6;
+  * the adjoint's J equals the plain forward path's J;
+  * a torch.autograd.Function wrapping the C-ABI gradient (test harness only) passes
+    torch.autograd.gradcheck-style directional checks.
+"""
+import numpy as np
+import pytest
+
+from gturbo_gb300.params import Params
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+KMIN, KMAX = 4.0, 8.0
+SEED = 481929
+
+
+def _setup(n=128, nsteps=12):
+    from gturbo_gb300.ic import random_phase_ic
+    from gturbo_gb300.params import famp_for_injection, nu8_scaled
+    from gturbo_gb300.solver import Solver
+    p = Params(n=n, alpv=1.0, rko=2, dt=5e-4, nu=nu8_scaled(n), alpnu=8.0, mu=0.1, k1f=10.0, k2f=12.0)
+    p = p.replace(famp=famp_for_injection(p, 1.0))
+    sol = Solver(p)
+    z0 = torch.from_numpy(random_phase_ic(p, 6.0, 0.5, seed=5)).cuda()
+    return p, sol, z0, nsteps
+
+
+def _direction(z0, seed, truncated_only=False):
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    d = torch.randn(z0.shape, generator=g, dtype=torch.float64).cuda()
+    if truncated_only:
+        d = d * (z0 != 0).to(torch.float64)
+    return d * (z0.abs().max() / d.abs().max())
+
+
+def test_adjoint_forward_matches_plain_forward():
+    from gturbo_gb300.adjoint import forward_objective, gradient
+    p, sol, z0, ns = _setup()
+    J_plain = forward_objective(sol, z0, ns, SEED, KMIN, KMAX)
+    J, gz, gf, zT, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=5)
+    assert J == pytest.approx(J_plain, rel=1e-14)
+    assert torch.isfinite(gz).all()
+
+
+@pytest.mark.parametrize("k", [1, 5, 12])
+def test_dot_product_adjoint_vs_tlm(k):
+    from gturbo_gb300.adjoint import gradient, tlm_run
+    p, sol, z0, ns = _setup()
+    J, gz, gf, _, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=k)
+    for seed in (1, 2):
+        dz = _direction(z0, seed)
+        dfamp = 0.3 * seed
+        J2, dJ = tlm_run(sol, z0, dz, dfamp, ns, SEED, KMIN, KMAX)
+        adj = float((gz * dz).sum().item()) + gf * dfamp
+        assert J2 == pytest.approx(J, rel=1e-14)
+        assert adj == pytest.approx(dJ, rel=1e-11, abs=1e-14 * abs(J))
+
+
+def test_tlm_against_central_differences():
+    from gturbo_gb300.adjoint import forward_objective, tlm_run
+    p, sol, z0, ns = _setup()
+    for seed in range(1, 9):
+        dz = _direction(z0, 100 + seed, truncated_only=(seed % 2 == 0))
+        dfamp = 0.0 if seed % 3 else 0.5
+        _, dJ = tlm_run(sol, z0, dz, dfamp, ns, SEED, KMIN, KMAX)
+        h = 1e-6
+        if dfamp:
+            from gturbo_gb300.solver import Solver
+            sp = Solver(p.replace(famp=p.famp + h * dfamp))
+            sm = Solver(p.replace(famp=p.famp - h * dfamp))
+            Jp = forward_objective(sp, z0 + h * dz, ns, SEED, KMIN, KMAX)
+            Jm = forward_objective(sm, z0 - h * dz, ns, SEED, KMIN, KMAX)
+        else:
+            Jp = forward_objective(sol, z0 + h * dz, ns, SEED, KMIN, KMAX)
+            Jm = forward_objective(sol, z0 - h * dz, ns, SEED, KMIN, KMAX)
+        fd = (Jp - Jm) / (2 * h)
+        assert fd == pytest.approx(dJ, rel=1e-6, abs=1e-9 * abs(Jp)), seed
+
+
+class _AdjointJ(torch.autograd.Function):
+    """J(z0) after nsteps, with the C-ABI adjoint as its backward (test harness only)."""
+
+    @staticmethod
+    def forward(ctx, z0, sol, nsteps, seed):
+        from gturbo_gb300.adjoint import gradient
+        J, gz, gf, _, _ = gradient(sol, z0.detach(), nsteps, seed, KMIN, KMAX, checkpoint=4)
+        ctx.save_for_backward(gz)
+        return torch.tensor(J, dtype=torch.float64, device=z0.device)
+
+    @staticmethod
+    def backward(ctx, gout):
+        (gz,) = ctx.saved_tensors
+        return gout * gz, None, None, None
+
+
+def test_autograd_function_wrapper():
+    from gturbo_gb300.adjoint import tlm_run
+    p, sol, z0, ns = _setup(n=128, nsteps=6)
+    z = z0.clone().requires_grad_(True)
+    J = _AdjointJ.apply(z, sol, ns, SEED)
+    J.backward()
+    dz = _direction(z0, 7)
+    _, dJ = tlm_run(sol, z0, dz, 0.0, ns, SEED, KMIN, KMAX)
+    assert float((z.grad * dz).sum()) == pytest.approx(dJ, rel=1e-11)
+
+
+def test_adjoint_limits():
+    from gturbo_gb300 import _lib
+    from gturbo_gb300.adjoint import gradient
+    from gturbo_gb300.solver import Solver
+    sol = Solver(Params(n=64, rko=4))
+    with pytest.raises(_lib.GturboError):
+        gradient(sol, sol.field(), 2, SEED, KMIN, KMAX)
