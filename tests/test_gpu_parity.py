@@ -217,6 +217,19 @@ def test_main_loop_10_steps():
     assert rel_l2(_host(z), ref) < 1e-11
 
 
+@pytest.mark.parametrize("n,rko", [(4096, 2), (8192, 4)])
+def test_step_large_grids(n, rko):
+    """One step at the largest grids (512-thread CTAs, the 8192^2 roofline workload's RK4)."""
+    p = _params(n, rko=rko, alpv=2.0, k1f=40.0, k2f=44.0, nu=1e-50, alpnu=8.0, dt=5e-5)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 15) * 1e4
+    ref = a.copy()
+    orc.rk_step(ref)
+    z = _dev(a)
+    sol.rk_step(z, sol.work())
+    assert rel_l2(_host(z), ref) < TOL
+
+
 def test_step_2048_rk2_headline():
     """One RK2 step of the 2048^2 alpha=1 workload against the oracle."""
     from gturbo_gb300.params import config
