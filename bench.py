@@ -211,6 +211,8 @@ def pass_model(p, kind):
         return 5 * n * 2.5 * n * lg, 5 * S
     if kind == "nlt_colfwd":
         return 2 * nh * 5 * n * lg, 4 * S
+    if kind == "nlt_colfwd_inv":  # pass C of a stage + pass A of the next
+        return 5 * nh * 5 * n * lg, 7 * S
     return None, None
 
 
@@ -272,7 +274,10 @@ def ours_arm(args):
     barrier()
     finite = bool(torch.isfinite(z).all().item())
     stages = 4 if p.rko == 4 else 2
-    launches = K * (3 * stages + 1) + ndiag * (3 + 5)
+    # per step: pass A of stage 1, then per stage pass B and pass C (fused with the next
+    # stage's pass A) -> 2 * stages + 1, plus the forcing kick; a diagnostics call adds one
+    # nonlinear term (3 passes) and 5 reduction kernels
+    launches = K * (2 * stages + 1 + 1) + ndiag * (3 + 5)
 
     extras = {}
     if rank == 0:

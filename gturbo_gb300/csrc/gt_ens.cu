@@ -64,6 +64,23 @@ k_ens_colfwd(const NltArgs* __restrict__ args, const EnsTile* __restrict__ tiles
   }
 }
 
+// pass C of stage cur[m] fused with pass A of stage next[m] (same tiles)
+__global__ void __launch_bounds__(kEnsThreads)
+k_ens_colfwd_inv(const NltArgs* __restrict__ cur, const NltArgs* __restrict__ next,
+                 const EnsTile* __restrict__ tiles) {
+  const EnsTile w = tiles[blockIdx.x];
+  const NltArgs a = cur[w.member];
+  const NltArgs b = next[w.member];
+  switch (a.n) {
+    case 128: colfwd_colinv_tile<128, 16>(a, b, w.tile); break;
+    case 256: colfwd_colinv_tile<256, 8>(a, b, w.tile); break;
+    case 512: colfwd_colinv_tile<512, 4>(a, b, w.tile); break;
+    case 1024: colfwd_colinv_tile<1024, 2>(a, b, w.tile); break;
+    case 2048: colfwd_colinv_tile<2048, 1>(a, b, w.tile); break;
+    default: break;
+  }
+}
+
 struct ForceMember {
   double2* z;
   const int* ikx;
@@ -195,11 +212,15 @@ void free_ens(gt_ens* e) {
 bool valid_ens_n(int n) { return n >= 128 && n <= 2048 && (n & (n - 1)) == 0; }
 
 int enqueue_step(gt_ens* e, cudaStream_t s) {
+  // pass A of stage 0, then per stage: pass B, and pass C fused with the next stage's pass A
+  gt::k_ens_colinv<<<e->ncol, gt::kEnsThreads, gt::kEnsColSmem, s>>>(e->d_args, e->d_col);
   for (int st = 0; st < e->stages; ++st) {
     const NltArgs* a = e->d_args + (size_t)st * e->nm;
-    gt::k_ens_colinv<<<e->ncol, gt::kEnsThreads, gt::kEnsColSmem, s>>>(a, e->d_col);
     gt::k_ens_row<<<e->nrow, gt::kEnsThreads, gt::kEnsRowSmem, s>>>(a, e->d_row);
-    gt::k_ens_colfwd<<<e->ncol, gt::kEnsThreads, gt::kEnsColSmem, s>>>(a, e->d_col);
+    if (st + 1 < e->stages)
+      gt::k_ens_colfwd_inv<<<e->ncol, gt::kEnsThreads, gt::kEnsColSmem, s>>>(a, a + e->nm, e->d_col);
+    else
+      gt::k_ens_colfwd<<<e->ncol, gt::kEnsThreads, gt::kEnsColSmem, s>>>(a, e->d_col);
   }
   if (e->nmodes > 0)
     gt::k_forcing_philox_ens<<<(e->nmodes + 127) / 128, 128, 0, s>>>(e->d_fm, e->d_modes, e->nmodes,
@@ -280,13 +301,14 @@ int gt_ens_create(const gt_params* members, int32_t nmembers, const uint64_t* ke
   up((void**)&e->d_col, col.data(), sizeof(EnsTile) * col.size());
   up((void**)&e->d_row, row.data(), sizeof(EnsTile) * row.size());
   up((void**)&e->d_modes, modes.data(), sizeof(int2) * modes.size());
-  up((void**)&e->d_flags, nullptr, sizeof(int) * nmembers);
+  up((void**)&e->d_flags, nullptr, sizeof(int) * 2 * nmembers);  // even / odd stages
   up((void**)&e->d_args, nullptr, sizeof(NltArgs) * (size_t)e->stages * nmembers);
   up((void**)&e->d_fm, nullptr, sizeof(ForceMember) * nmembers);
   up((void**)&e->d_step, nullptr, sizeof(uint64_t));
   up((void**)&e->d_done, nullptr, sizeof(unsigned));
   if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_colinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gt::kEnsColSmem);
   if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_colfwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gt::kEnsColSmem);
+  if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_colfwd_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gt::kEnsColSmem);
   if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_row, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gt::kEnsRowSmem);
   if (c == cudaSuccess) c = cudaStreamCreateWithFlags(&e->own, cudaStreamNonBlocking);
   if (c == cudaSuccess) c = cudaEventCreateWithFlags(&e->ev_in, cudaEventDisableTiming);
@@ -340,10 +362,11 @@ int gt_ens_set_fields(gt_ens* e, double* const* z, double* const* znl, double* c
     if (!z[m] || !znl[m] || !u[m] || !v[m] || (e->rko == 4 && !znew[m]))
       return efail(e, GT_ERR_ARG, "gt_ens_set_fields: null field pointer");
     gt_handle* h = e->handles[e->hidx[m]];
-    int* flag = e->d_flags + m;
-    // the stage sequence of gt_step_rk2 / gt_step_rk4 (rkstep.f90:2-131)
+    // the stage sequence of gt_step_rk2 / gt_step_rk4 (rkstep.f90:2-131); even and odd stages
+    // use different flags because pass C of one runs with pass A of the next
     for (int st = 0; st < e->stages; ++st) {
       const double* zin = st == 0 ? z[m] : znl[m];
+      int* flag = e->d_flags + (size_t)(st & 1) * nm + m;
       NltArgs a = gt::handle_nlt_args(h, zin, znl[m], u[m], v[m], flag);
       a.epi.z = reinterpret_cast<const double2*>(z[m]);
       a.epi.znew = znew ? reinterpret_cast<double2*>(znew[m]) : nullptr;

@@ -20,49 +20,54 @@
 
 namespace gt {
 
+#define GT_HD_INL __host__ __device__ __forceinline__
+
 __device__ __forceinline__ int padix(int o) { return o + (o >> 4); }
 __host__ __device__ constexpr int padded(int n) { return n + (n >> 4); }
 
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+GT_HD_INL double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+GT_HD_INL double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 
 // a * (-i) for the forward transform, a * (+i) for the inverse
 template <bool INV>
-__device__ __forceinline__ double2 mul_w4(double2 a) {
+GT_HD_INL double2 mul_w4(double2 a) {
   return INV ? make_double2(-a.y, a.x) : make_double2(a.y, -a.x);
 }
 
 // a * w for the forward transform, a * conj(w) for the inverse (w = exp(-2 pi i k / L))
 template <bool INV>
-__device__ __forceinline__ double2 twmul(double2 a, double2 w) {
+GT_HD_INL double2 twmul(double2 a, double2 w) {
   if (INV) return make_double2(fma(a.x, w.x, a.y * w.y), fma(a.y, w.x, -(a.x * w.y)));
   return make_double2(fma(a.x, w.x, -(a.y * w.y)), fma(a.y, w.x, a.x * w.y));
 }
 
-// a * c * (1 -+ i): the W8^1 twiddle (forward: (1-i)/sqrt2, inverse (1+i)/sqrt2)
+// The W8^1 and W8^3 twiddles are c * P(a) with c = 1/sqrt(2) and P made of additions only.
+// The butterflies below keep P unscaled and fold c into the following additions as FMAs
+// (e +- c P), which removes the two multiplies per twiddle.
+constexpr double kC8 = 0.70710678118654752440;  // cos(pi/4)
+
+// W8^1: forward (1-i)/sqrt2, inverse (1+i)/sqrt2
 template <bool INV>
-__device__ __forceinline__ double2 mul_w8_1(double2 a) {
-  const double c = 0.70710678118654752440;
-  return INV ? make_double2(c * (a.x - a.y), c * (a.x + a.y))
-             : make_double2(c * (a.x + a.y), c * (a.y - a.x));
+GT_HD_INL double2 w8_1_unscaled(double2 a) {
+  return INV ? make_double2(a.x - a.y, a.x + a.y) : make_double2(a.x + a.y, a.y - a.x);
 }
-// W8^3 (forward: -(1+i)/sqrt2, inverse: (-1+i)/sqrt2)
+// W8^3: forward -(1+i)/sqrt2, inverse (-1+i)/sqrt2
 template <bool INV>
-__device__ __forceinline__ double2 mul_w8_3(double2 a) {
-  const double c = 0.70710678118654752440;
-  return INV ? make_double2(-c * (a.x + a.y), c * (a.x - a.y))
-             : make_double2(c * (a.y - a.x), -c * (a.x + a.y));
+GT_HD_INL double2 w8_3_unscaled(double2 a) {
+  return INV ? make_double2(-(a.x + a.y), a.x - a.y) : make_double2(a.y - a.x, -(a.x + a.y));
 }
+// e + s c P and e - s c P (s = +-1 folded into c)
+GT_HD_INL double2 fma_c(double c, double2 p, double2 e) { return make_double2(fma(c, p.x, e.x), fma(c, p.y, e.y)); }
 
 template <bool INV>
-__device__ __forceinline__ void dft2(double2& a0, double2& a1) {
+GT_HD_INL void dft2(double2& a0, double2& a1) {
   double2 t = a0;
   a0 = cadd(t, a1);
   a1 = csub(t, a1);
 }
 
 template <bool INV>
-__device__ __forceinline__ void dft4(double2& a0, double2& a1, double2& a2, double2& a3) {
+GT_HD_INL void dft4(double2& a0, double2& a1, double2& a2, double2& a3) {
   double2 t0 = cadd(a0, a2), t1 = csub(a0, a2);
   double2 t2 = cadd(a1, a3), t3 = mul_w4<INV>(csub(a1, a3));
   a0 = cadd(t0, t2);
@@ -73,54 +78,69 @@ __device__ __forceinline__ void dft4(double2& a0, double2& a1, double2& a2, doub
 
 // Radix-8 as 2 x radix-4: even/odd DFT4s, W8^k twiddles, radix-2 combine. Natural order.
 template <bool INV>
-__device__ __forceinline__ void dft8(double2* a) {
+GT_HD_INL void dft8(double2* a) {
   double2 e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6];
   double2 o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
   dft4<INV>(e0, e1, e2, e3);
   dft4<INV>(o0, o1, o2, o3);
-  o1 = mul_w8_1<INV>(o1);
+  const double2 p1 = w8_1_unscaled<INV>(o1);
+  const double2 p3 = w8_3_unscaled<INV>(o3);
   o2 = mul_w4<INV>(o2);
-  o3 = mul_w8_3<INV>(o3);
   a[0] = cadd(e0, o0); a[4] = csub(e0, o0);
-  a[1] = cadd(e1, o1); a[5] = csub(e1, o1);
+  a[1] = fma_c(kC8, p1, e1); a[5] = fma_c(-kC8, p1, e1);
   a[2] = cadd(e2, o2); a[6] = csub(e2, o2);
-  a[3] = cadd(e3, o3); a[7] = csub(e3, o3);
+  a[3] = fma_c(kC8, p3, e3); a[7] = fma_c(-kC8, p3, e3);
 }
 
-// Radix-16 as 4 x radix-4 with W16^(n1*k2) twiddles. Natural order in and out.
+// Radix-16 as 4 x radix-4 with W16^(n1*k2) twiddles (b[n1][k2] = a[n1 + 4 k2] after the first
+// stage, X[k2 + 4 k1] from the second). Natural order in and out.
 template <bool INV>
-__device__ __forceinline__ void dft16(double2* a) {
-  const double c8 = 0.92387953251128675613;  // cos(pi/8)
-  const double s8 = 0.38268343236508977173;  // sin(pi/8)
+GT_HD_INL void dft16(double2* a) {
+  const double c16 = 0.92387953251128675613;  // cos(pi/8)
+  const double s16 = 0.38268343236508977173;  // sin(pi/8)
 #pragma unroll
   for (int n1 = 0; n1 < 4; ++n1) dft4<INV>(a[n1], a[n1 + 4], a[n1 + 8], a[n1 + 12]);
-  // b[n1][k2] sits in a[n1 + 4*k2]; twiddle by W16^(n1*k2)
-  // n1 = 1: k2 = 1,2,3 -> W16^1, W16^2, W16^3
-  a[5] = twmul<INV>(a[5], make_double2(c8, -s8));
-  a[9] = mul_w8_1<INV>(a[9]);
-  a[13] = twmul<INV>(a[13], make_double2(s8, -c8));
-  // n1 = 2: W16^2, W16^4, W16^6
-  a[6] = mul_w8_1<INV>(a[6]);
-  a[10] = mul_w4<INV>(a[10]);
-  a[14] = mul_w8_3<INV>(a[14]);
-  // n1 = 3: W16^3, W16^6, W16^9
-  a[7] = twmul<INV>(a[7], make_double2(s8, -c8));
-  a[11] = mul_w8_3<INV>(a[11]);
-  a[15] = twmul<INV>(a[15], make_double2(-c8, s8));
+  double2 X[16];
+  // k2 = 0: no twiddles
+  {
+    double2 y0 = a[0], y1 = a[1], y2 = a[2], y3 = a[3];
+    dft4<INV>(y0, y1, y2, y3);
+    X[0] = y0; X[4] = y1; X[8] = y2; X[12] = y3;
+  }
+  // k2 = 1: (b0, W16^1 b1, W16^2 b2, W16^3 b3); W16^2 = W8^1 folded into t0, t1
+  {
+    const double2 b1 = twmul<INV>(a[5], make_double2(c16, -s16));
+    const double2 p2 = w8_1_unscaled<INV>(a[6]);
+    const double2 b3 = twmul<INV>(a[7], make_double2(s16, -c16));
+    const double2 t0 = fma_c(kC8, p2, a[4]), t1 = fma_c(-kC8, p2, a[4]);
+    const double2 t2 = cadd(b1, b3), t3 = mul_w4<INV>(csub(b1, b3));
+    X[1] = cadd(t0, t2); X[9] = csub(t0, t2); X[5] = cadd(t1, t3); X[13] = csub(t1, t3);
+  }
+  // k2 = 2: (b0, W8^1 b1, W4 b2, W8^3 b3); both W8 factors share c: c (P1 +- P3)
+  {
+    const double2 p1 = w8_1_unscaled<INV>(a[9]);
+    const double2 b2 = mul_w4<INV>(a[10]);
+    const double2 p3 = w8_3_unscaled<INV>(a[11]);
+    const double2 t0 = cadd(a[8], b2), t1 = csub(a[8], b2);
+    const double2 sp = cadd(p1, p3), dm = mul_w4<INV>(csub(p1, p3));
+    X[2] = fma_c(kC8, sp, t0); X[10] = fma_c(-kC8, sp, t0);
+    X[6] = fma_c(kC8, dm, t1); X[14] = fma_c(-kC8, dm, t1);
+  }
+  // k2 = 3: (b0, W16^3 b1, W16^6 b2, W16^9 b3); W16^6 = W8^3 folded into t0, t1
+  {
+    const double2 b1 = twmul<INV>(a[13], make_double2(s16, -c16));
+    const double2 p2 = w8_3_unscaled<INV>(a[14]);
+    const double2 b3 = twmul<INV>(a[15], make_double2(-c16, s16));
+    const double2 t0 = fma_c(kC8, p2, a[12]), t1 = fma_c(-kC8, p2, a[12]);
+    const double2 t2 = cadd(b1, b3), t3 = mul_w4<INV>(csub(b1, b3));
+    X[3] = cadd(t0, t2); X[11] = csub(t0, t2); X[7] = cadd(t1, t3); X[15] = csub(t1, t3);
+  }
 #pragma unroll
-  for (int k2 = 0; k2 < 4; ++k2) dft4<INV>(a[4 * k2], a[4 * k2 + 1], a[4 * k2 + 2], a[4 * k2 + 3]);
-  // X[k2 + 4*k1] sits in a[4*k2 + k1]: transpose the 4x4 block
-  double2 t;
-  t = a[1]; a[1] = a[4]; a[4] = t;
-  t = a[2]; a[2] = a[8]; a[8] = t;
-  t = a[3]; a[3] = a[12]; a[12] = t;
-  t = a[6]; a[6] = a[9]; a[9] = t;
-  t = a[7]; a[7] = a[13]; a[13] = t;
-  t = a[11]; a[11] = a[14]; a[14] = t;
+  for (int k = 0; k < 16; ++k) a[k] = X[k];
 }
 
 template <int RP, bool INV>
-__device__ __forceinline__ void dft(double2* a) {
+GT_HD_INL void dft(double2* a) {
   if constexpr (RP == 2) dft2<INV>(a[0], a[1]);
   else if constexpr (RP == 4) dft4<INV>(a[0], a[1], a[2], a[3]);
   else if constexpr (RP == 8) dft8<INV>(a);

@@ -181,9 +181,8 @@ __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
 #pragma unroll
     for (int s = 0; s < 16; ++s) nz |= (v[s].x != 0.0) | (v[s].y != 0.0);
   }
-  if (tile * C > a.kxlim) {
-    if (!__syncthreads_or(nz)) return;
-  }
+  const bool skip = (tile * C > a.kxlim) ? !__syncthreads_or(nz) : false;
+  if (skip) return;
   if (nz) atomicExch(a.flag, 1);
   const double kx = __ldg(&a.fkx[ic]);
   // u = i ky/|k|^a q  (nlt.f90:29-32)
@@ -330,40 +329,52 @@ __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
 #pragma unroll
       for (int s = 0; s < 16; ++s) epilogue(a.epi, i, t + s * T, NH, czero());
     }
-    return;
+  } else {
+    double2* sm = smem + c;
+    double2* af = a.u;
+    const double2* bf = a.v;
+    const double scale = 0.5 / ((double)N * (double)N);
+    const double kxs = __ldg(&a.fkx[ic]) * scale;
+    double2 v[16];
+#pragma unroll
+    for (int s = 0; s < 16; ++s) v[s] = valid ? af[(size_t)(t + s * T) * NH + ic] : czero();
+    fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
+    // keep kx*FA in place of A (the same thread re-reads it below)
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < 16; ++s)
+        af[(size_t)(t + s * T) * NH + i] = make_double2(kxs * v[s].x, kxs * v[s].y);
+    }
+#pragma unroll
+    for (int s = 0; s < 16; ++s) v[s] = valid ? bf[(size_t)(t + s * T) * NH + ic] : czero();
+    __syncthreads();
+    fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
+    if (valid) {
+      const int kc = a.truncate ? __ldg(&a.kcut[i]) : N;
+#pragma unroll
+      for (int s = 0; s < 16; ++s) {
+        const int j = t + s * T;
+        const double kys = __ldg(&a.fky[j]) * scale;
+        const double2 fa = af[(size_t)j * NH + i];
+        // N = -i (kx A + ky B): re = kx Im A + ky Im B, im = -(kx Re A + ky Re B)
+        double2 nh = make_double2(fma(kys, v[s].y, fa.y), -fma(kys, v[s].x, fa.x));
+        const int aj = min(j, N - j);
+        if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
+        epilogue(a.epi, i, j, NH, nh);
+      }
+    }
   }
-  double2* sm = smem + c;
-  double2* af = a.u;
-  const double2* bf = a.v;
-  const double scale = 0.5 / ((double)N * (double)N);
-  const double kxs = __ldg(&a.fkx[ic]) * scale;
-  double2 v[16];
-#pragma unroll
-  for (int s = 0; s < 16; ++s) v[s] = valid ? af[(size_t)(t + s * T) * NH + ic] : czero();
-  fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
-  // keep kx*FA in place of A (the same thread re-reads it below)
-  if (valid) {
-#pragma unroll
-    for (int s = 0; s < 16; ++s)
-      af[(size_t)(t + s * T) * NH + i] = make_double2(kxs * v[s].x, kxs * v[s].y);
-  }
-#pragma unroll
-  for (int s = 0; s < 16; ++s) v[s] = valid ? bf[(size_t)(t + s * T) * NH + ic] : czero();
+}
+
+// Pass C of one Runge-Kutta stage followed by pass A of the next one on the same columns: the
+// stage value written by the epilogue is re-read by the thread that wrote it. The two
+// evaluations use different untruncated-input flags (next.flag != cur.flag): pass C clears
+// cur.flag while pass A may raise next.flag.
+template <int N, int C>
+__device__ __forceinline__ void colfwd_colinv_tile(const NltArgs& cur, const NltArgs& next, int tile) {
+  colfwd_tile<N, C>(cur, tile);
   __syncthreads();
-  fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
-  if (!valid) return;
-  const int kc = a.truncate ? __ldg(&a.kcut[i]) : N;
-#pragma unroll
-  for (int s = 0; s < 16; ++s) {
-    const int j = t + s * T;
-    const double kys = __ldg(&a.fky[j]) * scale;
-    const double2 fa = af[(size_t)j * NH + i];
-    // N = -i (kx A + ky B): re = kx Im A + ky Im B, im = -(kx Re A + ky Re B)
-    double2 nh = make_double2(fma(kys, v[s].y, fa.y), -fma(kys, v[s].x, fa.x));
-    const int aj = min(j, N - j);
-    if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
-    epilogue(a.epi, i, j, NH, nh);
-  }
+  colinv_tile<N, C>(next, tile);
 }
 
 // ---- single-field kernels ---------------------------------------------------------------
@@ -383,6 +394,12 @@ template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
 k_nlt_colfwd(NltArgs a) {
   colfwd_tile<N, Shape<N>::COLS>(a, blockIdx.x);
+}
+
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
+k_nlt_colfwd_inv(NltArgs cur, NltArgs next) {
+  colfwd_colinv_tile<N, Shape<N>::COLS>(cur, next, blockIdx.x);
 }
 
 // ---- ensemble kernels: one launch per pass for every member ------------------------------

@@ -24,12 +24,14 @@ enum OpKind : int {
   OP_ADJ_COLINV = 10, // adjoint passes (N <= 4096)
   OP_ADJ_ROW = 11,
   OP_ADJ_COLFWD = 12,
+  OP_NLT_COLFWD_INV = 13,  // pass C of stage nlt + pass A of stage nlt2
 };
 
 struct GtOp {
   int kind;
   cudaStream_t stream;
   NltArgs nlt;        // passes A, B, C
+  NltArgs nlt2;       // the next stage (OP_NLT_COLFWD_INV)
   TlmArgs tlm;
   AdjArgs adj;
   double2* a;         // field of the standalone transforms

@@ -277,6 +277,7 @@ int op_class(int kind) {
     case gt::OP_NLT_COLINV: return GT_PROF_NLT_COLINV;
     case gt::OP_NLT_ROW: return GT_PROF_NLT_ROW;
     case gt::OP_NLT_COLFWD: return GT_PROF_NLT_COLFWD;
+    case gt::OP_NLT_COLFWD_INV: return GT_PROF_NLT_COLFWD_INV;
     default: return GT_PROF_OTHER;
   }
 }
@@ -453,7 +454,9 @@ int gt_create(const gt_params* p, gt_handle** out) {
   if (!rc) rc = upload(h, &h->d_lcgb, h->lcgb.data(), h->nf);
   if (!rc) rc = upload(h, &h->d_ff, ff.data(), ff.size());
   const int zero = 0;
-  if (!rc) rc = upload(h, &h->d_flag, &zero, 1);
+  const int zeros2[2] = {0, 0};  // untruncated-input flags of even / odd stages
+  (void)zero;
+  if (!rc) rc = upload(h, &h->d_flag, zeros2, 2);
   const int ngroups = (N + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
   if (!rc) rc = upload<double>(h, &h->d_part, nullptr, (size_t)ngroups * h->NBIN * 4);
   if (!rc) rc = upload<double>(h, &h->d_rowsum, nullptr, (size_t)N * 6);
@@ -581,23 +584,52 @@ int gt_nlt(gt_handle* h, double* z, double* u, double* v) {
   return nlt_passes(h, z, z, u, v, make_epi(h, gt::EPI_NLT, z, nullptr, nullptr));
 }
 
+// The stages of one Runge-Kutta step: stage k evaluates N at zin[k] (the first from z, the
+// others from znl, where the previous stage's epilogue left its value) and applies epi[k].
+// Pass C of stage k and pass A of stage k+1 run as one column kernel; the stages alternate
+// between the handle's two untruncated-input flags.
+int stage_chain(gt_handle* h, int nst, const double* const* zin, double* znl, double* u, double* v,
+                const gt::EpiArgs* epi) {
+  GtOp op = base_op(h);
+  auto stage = [&](int k) {
+    gt::NltArgs a = gt::handle_nlt_args(h, zin[k], znl, u, v, h->d_flag + (k & 1));
+    a.epi = epi[k];
+    return a;
+  };
+  op.nlt = stage(0);
+  op.kind = gt::OP_NLT_COLINV;
+  int rc = run(h, op);
+  for (int k = 0; k < nst && !rc; ++k) {
+    op.nlt = stage(k);
+    op.kind = gt::OP_NLT_ROW;
+    rc = run(h, op);
+    if (rc) break;
+    if (k + 1 < nst) {
+      op.nlt2 = stage(k + 1);
+      op.kind = gt::OP_NLT_COLFWD_INV;
+    } else {
+      op.kind = gt::OP_NLT_COLFWD;
+    }
+    rc = run(h, op);
+  }
+  return rc;
+}
+
 int gt_step_rk2(gt_handle* h, double* z, double* znl, double* u, double* v) {
   if (!h || !z || !znl || !u || !v) return fail(h, GT_ERR_ARG, "gt_step_rk2: null argument");
-  gt::EpiArgs E1 = make_epi(h, gt::EPI_RK2A, znl, nullptr, z);
-  gt::EpiArgs E2 = make_epi(h, gt::EPI_RK2B, z, nullptr, z);
-  int rc = nlt_passes(h, z, znl, u, v, E1);
-  if (rc) return rc;
-  return nlt_passes(h, znl, znl, u, v, E2);
+  const gt::EpiArgs epi[2] = {make_epi(h, gt::EPI_RK2A, znl, nullptr, z),
+                              make_epi(h, gt::EPI_RK2B, z, nullptr, z)};
+  const double* zin[2] = {z, znl};
+  return stage_chain(h, 2, zin, znl, u, v, epi);
 }
 
 int gt_step_rk4(gt_handle* h, double* z, double* znl, double* znew, double* u, double* v) {
   if (!h || !z || !znl || !znew || !u || !v) return fail(h, GT_ERR_ARG, "gt_step_rk4: null argument");
   if (h->split) return fail(h, GT_ERR_ARG, "gt_step_rk4: the split integrator exists only for RK2");
-  int rc = nlt_passes(h, z, znl, u, v, make_epi(h, gt::EPI_RK4A, znl, znew, z));
-  if (!rc) rc = nlt_passes(h, znl, znl, u, v, make_epi(h, gt::EPI_RK4B, znl, znew, z));
-  if (!rc) rc = nlt_passes(h, znl, znl, u, v, make_epi(h, gt::EPI_RK4C, znl, znew, z));
-  if (!rc) rc = nlt_passes(h, znl, znl, u, v, make_epi(h, gt::EPI_RK4D, z, znew, nullptr));
-  return rc;
+  const gt::EpiArgs epi[4] = {make_epi(h, gt::EPI_RK4A, znl, znew, z), make_epi(h, gt::EPI_RK4B, znl, znew, z),
+                              make_epi(h, gt::EPI_RK4C, znl, znew, z), make_epi(h, gt::EPI_RK4D, z, znew, nullptr)};
+  const double* zin[4] = {z, znl, znl, znl};
+  return stage_chain(h, 4, zin, znl, u, v, epi);
 }
 
 float gt_rann(int32_t* seed) {

@@ -100,7 +100,8 @@ class Solver:
     def sync(self) -> None:
         self._check(self.lib.gt_sync(self.h))
 
-    PROF_KINDS = ("nlt_colinv", "nlt_row", "nlt_colfwd", "forcing", "diag", "other")
+    PROF_KINDS = ("nlt_colinv", "nlt_row", "nlt_colfwd", "forcing", "diag", "other",
+                  "nlt_colfwd_inv")
 
     def profile(self, enable: bool) -> None:
         """Record CUDA events around every later launch (gt_profile)."""
@@ -108,8 +109,8 @@ class Solver:
 
     def profile_read(self) -> dict:
         """{kind: (total ms, launches)} since the last read (gt_profile_read)."""
-        ms = (ctypes.c_double * 6)()
-        cnt = (ctypes.c_int64 * 6)()
+        ms = (ctypes.c_double * 7)()
+        cnt = (ctypes.c_int64 * 7)()
         self._check(self.lib.gt_profile_read(self.h, ms, cnt))
         return {k: (ms[i], cnt[i]) for i, k in enumerate(self.PROF_KINDS)}
 

@@ -242,7 +242,8 @@ int gt_diag_static(const gt_params* p, const double* z, const double* znl,
 #define GT_PROF_FORCING 3
 #define GT_PROF_DIAG 4
 #define GT_PROF_OTHER 5
-#define GT_PROF_KINDS 6
+#define GT_PROF_NLT_COLFWD_INV 6 /* pass C of a stage fused with pass A of the next */
+#define GT_PROF_KINDS 7
 
 /* No counterpart in the reference (its only timer is a wall clock around the whole run,
  * src/main.f90:191-193). enable=1: record a CUDA event pair on the handle's stream around

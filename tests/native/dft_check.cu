@@ -1,0 +1,43 @@
+// Host check of the register butterflies of gt_fft.cuh against a naive DFT (built and run by
+// tests/test_fft_kernels.py; test infrastructure only).
+#include <cmath>
+#include <cstdio>
+#include <random>
+
+#include "../../gturbo_gb300/csrc/gt_fft.cuh"
+
+template <int R, bool INV>
+static double check(std::mt19937_64& rng) {
+  std::normal_distribution<double> nd;
+  double worst = 0.0;
+  for (int trial = 0; trial < 50; ++trial) {
+    double2 a[R], x[R];
+    for (int k = 0; k < R; ++k) x[k] = a[k] = make_double2(nd(rng), nd(rng));
+    gt::dft<R, INV>(a);
+    const double sgn = INV ? 1.0 : -1.0;
+    for (int k = 0; k < R; ++k) {
+      long double re = 0, im = 0;
+      for (int n = 0; n < R; ++n) {
+        const long double ang = sgn * 2.0L * 3.14159265358979323846264338327950288L * (long double)((k * n) % R) / R;
+        re += x[n].x * cosl(ang) - x[n].y * sinl(ang);
+        im += x[n].x * sinl(ang) + x[n].y * cosl(ang);
+      }
+      const double err = std::hypot((double)(a[k].x - re), (double)(a[k].y - im));
+      worst = std::fmax(worst, err);
+    }
+  }
+  return worst;
+}
+
+int main() {
+  std::mt19937_64 rng(7);
+  const double e[8] = {check<2, false>(rng), check<2, true>(rng), check<4, false>(rng), check<4, true>(rng),
+                       check<8, false>(rng), check<8, true>(rng), check<16, false>(rng), check<16, true>(rng)};
+  const char* names[8] = {"2f", "2i", "4f", "4i", "8f", "8i", "16f", "16i"};
+  int bad = 0;
+  for (int k = 0; k < 8; ++k) {
+    std::printf("radix %s max err %.3e\n", names[k], e[k]);
+    if (!(e[k] < 1e-14)) bad = 1;
+  }
+  return bad;
+}
