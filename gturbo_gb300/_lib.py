@@ -59,6 +59,7 @@ def load(path: str | None = None):
         "gt_fft_dir": ([P, D], ctypes.c_int),
         "gt_fft_inv": ([P, D], ctypes.c_int),
         "gt_trunc": ([P, D], ctypes.c_int),
+        "gt_dump_real4": ([P, D, D], ctypes.c_int),
         "gt_produ": ([P, D, D, D], ctypes.c_int),
         "gt_nlt": ([P, D, D, D], ctypes.c_int),
         "gt_step_rk2": ([P, D, D, D, D], ctypes.c_int),
@@ -89,6 +90,10 @@ def load(path: str | None = None):
         "gt_ens_last_error": ([P], ctypes.c_char_p),
         "gt_profile": ([P, ctypes.c_int], ctypes.c_int),
         "gt_profile_read": ([P, H, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+        "gt_variant_supported": ([ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+        "gt_set_variant": ([P, ctypes.c_int32], ctypes.c_int),
+        "gt_get_variant": ([P, I32P], ctypes.c_int),
+        "gt_autotune": ([P, ctypes.c_int32, H, I32P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

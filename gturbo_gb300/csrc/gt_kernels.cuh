@@ -160,9 +160,9 @@ struct NltArgs {
 
 // Pass A: inverse y-transforms of u, v and q (in that order: zin may alias q, as the
 // reference destroys z, so q is re-read from zin before the q column is overwritten).
-template <int N, int C>
+template <int N, int C, int R = 16>
 __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
-  constexpr int T = N / 16, NH = N / 2 + 1;
+  constexpr int T = N / R, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
   const int c = threadIdx.x % C, t = threadIdx.x / C;
   const int i = tile * C + c;
@@ -170,16 +170,16 @@ __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
   const int ic = valid ? i : NH - 1;
   double2* sm = smem + c;
   const double2* zin = a.zin;
-  double2 v[16];
+  double2 v[R];
 #pragma unroll
-  for (int s = 0; s < 16; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
+  for (int s = 0; s < R; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
   // A column beyond the 2/3 ellipse (i > kxlim) carries data only if the caller passed an
   // untruncated field: then raise the flag so that pass B reads every column. A tile made
   // only of such columns is skipped when all of them are zero.
   int nz = 0;
   if (valid && i > a.kxlim) {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) nz |= (v[s].x != 0.0) | (v[s].y != 0.0);
+    for (int s = 0; s < R; ++s) nz |= (v[s].x != 0.0) | (v[s].y != 0.0);
   }
   const bool skip = (tile * C > a.kxlim) ? !__syncthreads_or(nz) : false;
   if (skip) return;
@@ -187,38 +187,38 @@ __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
   const double kx = __ldg(&a.fkx[ic]);
   // u = i ky/|k|^a q  (nlt.f90:29-32)
 #pragma unroll
-  for (int s = 0; s < 16; ++s) {
+  for (int s = 0; s < R; ++s) {
     const int j = t + s * T;
     const double m = __ldg(&a.fky[j]) * __ldg(&a.kainv[(size_t)j * NH + ic]);
     v[s] = make_double2(-m * v[s].y, m * v[s].x);
   }
-  fft_regs<N, 16, true, C>(v, sm, t, a.tw, 0);
+  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0);
   if (valid) {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) a.u[(size_t)(t + s * T) * NH + i] = v[s];
+    for (int s = 0; s < R; ++s) a.u[(size_t)(t + s * T) * NH + i] = v[s];
   }
   // v = -i kx/|k|^a q  (nlt.f90:33-34)
 #pragma unroll
-  for (int s = 0; s < 16; ++s) {
+  for (int s = 0; s < R; ++s) {
     const int j = t + s * T;
     const double2 q = valid ? zin[(size_t)j * NH + ic] : czero();
     const double m = kx * __ldg(&a.kainv[(size_t)j * NH + ic]);
     v[s] = make_double2(m * q.y, -m * q.x);
   }
   __syncthreads();
-  fft_regs<N, 16, true, C>(v, sm, t, a.tw, 0);
+  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0);
   if (valid) {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) a.v[(size_t)(t + s * T) * NH + i] = v[s];
+    for (int s = 0; s < R; ++s) a.v[(size_t)(t + s * T) * NH + i] = v[s];
   }
   // q (nlt.f90:41)
 #pragma unroll
-  for (int s = 0; s < 16; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
+  for (int s = 0; s < R; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
   __syncthreads();
-  fft_regs<N, 16, true, C>(v, sm, t, a.tw, 0);
+  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0);
   if (valid) {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) a.q[(size_t)(t + s * T) * NH + i] = v[s];
+    for (int s = 0; s < R; ++s) a.q[(size_t)(t + s * T) * NH + i] = v[s];
   }
 }
 
@@ -226,9 +226,9 @@ __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
 // length N), p = (u+iv) q, R2C of p, then A = P[k] + conj P[N-k] = 2 FFT(uq)[k] and
 // B = -i (P[k] - conj P[N-k]) = 2 FFT(vq)[k] written over U and V for k <= kout.
 // Inputs beyond column kin are taken as zero unless the flag says pass A wrote them.
-template <int N, int ROWS>
+template <int N, int ROWS, int R = 16>
 __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
-  constexpr int T = N / 16, NH = N / 2 + 1, M = N / 2;
+  constexpr int T = N / R, NH = N / 2 + 1, M = N / 2;
   extern __shared__ double2 smem[];
   const int r = threadIdx.x / T, t = threadIdx.x % T;
   const int y = tile * ROWS + r;
@@ -240,7 +240,7 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
   const double2* vrow = a.v + (size_t)y * NH;
   // C[k] = U[k] + i V[k], C[N-k] = conj U[k] + i conj V[k]; Im of U, V at k=0, N/2 dropped
 #pragma unroll
-  for (int s = 0; s <= 8; ++s) {
+  for (int s = 0; s <= R / 2; ++s) {
     const int k = t + s * T;
     if (k <= M) {
       const double2 U = (k <= kl) ? urow[k] : czero();
@@ -255,7 +255,7 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
   }
   // Z[k] = (Q[k] + conj Q[M-k]) + i W^-k (Q[k] - conj Q[M-k]), k < M; Im Q[0], Q[M] dropped
 #pragma unroll
-  for (int s = 0; s < 8; ++s) {
+  for (int s = 0; s < R / 2; ++s) {
     const int k = t + s * T;
     double2 p = (k <= kl) ? qrow[k] : czero();
     double2 b = (M - k <= kl) ? qrow[M - k] : czero();
@@ -267,41 +267,41 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
     zs[padix(k)] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
   }
   __syncthreads();
-  // q: inverse length-M transform, 8 values per thread; result back to zs
+  // q: inverse length-M transform, R/2 values per thread; result back to zs
   {
-    double2 h[8];
+    double2 h[R / 2];
 #pragma unroll
-    for (int s = 0; s < 8; ++s) h[s] = zs[padix(t + s * T)];
+    for (int s = 0; s < R / 2; ++s) h[s] = zs[padix(t + s * T)];
     __syncthreads();
-    fft_regs<M, 8, true, 1>(h, zs, t, a.tw, 1);
+    fft_regs<M, R / 2, true, 1>(h, zs, t, a.tw, 1);
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < 8; ++s) zs[padix(t + s * T)] = h[s];
+    for (int s = 0; s < R / 2; ++s) zs[padix(t + s * T)] = h[s];
   }
   // u + i v: inverse length-N transform
-  double2 v[16];
+  double2 v[R];
 #pragma unroll
-  for (int s = 0; s < 16; ++s) v[s] = cs[padix(t + s * T)];
+  for (int s = 0; s < R; ++s) v[s] = cs[padix(t + s * T)];
   __syncthreads();
-  fft_regs<N, 16, true, 1>(v, cs, t, a.tw, 0);
+  fft_regs<N, R, true, 1>(v, cs, t, a.tw, 0);
   __syncthreads();
   // p = (u + i v) q  (produ.f90:18-19); q[2m] = Re z[m], q[2m+1] = Im z[m]
 #pragma unroll
-  for (int s = 0; s < 16; ++s) {
+  for (int s = 0; s < R; ++s) {
     const int x = t + s * T;
     const double2 zq = zs[padix(x >> 1)];
     const double q = (x & 1) ? zq.y : zq.x;
     v[s] = make_double2(v[s].x * q, v[s].y * q);
   }
-  fft_regs<N, 16, false, 1>(v, cs, t, a.tw, 0);
+  fft_regs<N, R, false, 1>(v, cs, t, a.tw, 0);
   __syncthreads();
 #pragma unroll
-  for (int s = 0; s < 16; ++s) cs[padix(t + s * T)] = v[s];
+  for (int s = 0; s < R; ++s) cs[padix(t + s * T)] = v[s];
   __syncthreads();
   double2* urw = a.u + (size_t)y * NH;
   double2* vrw = a.v + (size_t)y * NH;
 #pragma unroll
-  for (int s = 0; s <= 8; ++s) {
+  for (int s = 0; s <= R / 2; ++s) {
     const int k = t + s * T;
     if (k <= a.kout) {
       const double2 P = cs[padix(k)];
@@ -314,9 +314,9 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
 
 // Pass C: forward y-transforms of A and B, N = -i (kx A + ky B) / (2 N^2), the 2/3 mask
 // (row j of column i is kept iff min(j, N-j) <= kcut[i]) and the stage epilogue.
-template <int N, int C>
+template <int N, int C, int R = 16>
 __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
-  constexpr int T = N / 16, NH = N / 2 + 1;
+  constexpr int T = N / R, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
   if (tile == 0 && threadIdx.x == 0) *a.flag = 0;  // pass B of this nlt is complete
   const int c = threadIdx.x % C, t = threadIdx.x / C;
@@ -327,7 +327,7 @@ __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
     // no retained mode in this tile: N = 0
     if (valid) {
 #pragma unroll
-      for (int s = 0; s < 16; ++s) epilogue(a.epi, i, t + s * T, NH, czero());
+      for (int s = 0; s < R; ++s) epilogue(a.epi, i, t + s * T, NH, czero());
     }
   } else {
     double2* sm = smem + c;
@@ -335,24 +335,24 @@ __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
     const double2* bf = a.v;
     const double scale = 0.5 / ((double)N * (double)N);
     const double kxs = __ldg(&a.fkx[ic]) * scale;
-    double2 v[16];
+    double2 v[R];
 #pragma unroll
-    for (int s = 0; s < 16; ++s) v[s] = valid ? af[(size_t)(t + s * T) * NH + ic] : czero();
-    fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
+    for (int s = 0; s < R; ++s) v[s] = valid ? af[(size_t)(t + s * T) * NH + ic] : czero();
+    fft_regs<N, R, false, C>(v, sm, t, a.tw, 0);
     // keep kx*FA in place of A (the same thread re-reads it below)
     if (valid) {
 #pragma unroll
-      for (int s = 0; s < 16; ++s)
+      for (int s = 0; s < R; ++s)
         af[(size_t)(t + s * T) * NH + i] = make_double2(kxs * v[s].x, kxs * v[s].y);
     }
 #pragma unroll
-    for (int s = 0; s < 16; ++s) v[s] = valid ? bf[(size_t)(t + s * T) * NH + ic] : czero();
+    for (int s = 0; s < R; ++s) v[s] = valid ? bf[(size_t)(t + s * T) * NH + ic] : czero();
     __syncthreads();
-    fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
+    fft_regs<N, R, false, C>(v, sm, t, a.tw, 0);
     if (valid) {
       const int kc = a.truncate ? __ldg(&a.kcut[i]) : N;
 #pragma unroll
-      for (int s = 0; s < 16; ++s) {
+      for (int s = 0; s < R; ++s) {
         const int j = t + s * T;
         const double kys = __ldg(&a.fky[j]) * scale;
         const double2 fa = af[(size_t)j * NH + i];
@@ -370,11 +370,11 @@ __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
 // stage value written by the epilogue is re-read by the thread that wrote it. The two
 // evaluations use different untruncated-input flags (next.flag != cur.flag): pass C clears
 // cur.flag while pass A may raise next.flag.
-template <int N, int C>
+template <int N, int C, int R = 16>
 __device__ __forceinline__ void colfwd_colinv_tile(const NltArgs& cur, const NltArgs& next, int tile) {
-  colfwd_tile<N, C>(cur, tile);
+  colfwd_tile<N, C, R>(cur, tile);
   __syncthreads();
-  colinv_tile<N, C>(next, tile);
+  colinv_tile<N, C, R>(next, tile);
 }
 
 // ---- single-field kernels ---------------------------------------------------------------
@@ -400,6 +400,44 @@ template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
 k_nlt_colfwd_inv(NltArgs cur, NltArgs next) {
   colfwd_colinv_tile<N, Shape<N>::COLS>(cur, next, blockIdx.x);
+}
+
+// ---- launch variants of the nonlinear-term passes (picked per handle by gt_autotune) ------
+// V = 0: R = 16 values per thread, Shape<N>'s tiles (best from ~1024^2 up);
+// V = 1: R = 8,  one column / row per CTA;
+// V = 2: R = 4,  one column / row per CTA (small grids: 4x the threads of V = 0, for the
+//        latency-bound regime where a pass leaves most SMs idle).
+template <int N, int V>
+struct Var {
+  static constexpr int R = V == 0 ? 16 : V == 1 ? 8 : 4;
+  static constexpr int T = N / R;
+  static constexpr int NH = N / 2 + 1;
+  static constexpr int COLS = V == 0 ? Shape<N>::COLS : 1;
+  static constexpr int ROWS = V == 0 ? Shape<N>::ROWS : 1;
+  static constexpr int COL_THREADS = COLS * T;
+  static constexpr int ROW_THREADS = ROWS * T;
+  static constexpr int COL_CTAS = (NH + COLS - 1) / COLS;
+  static constexpr int ROW_CTAS = N / ROWS;
+  static constexpr size_t COL_SMEM = (size_t)padded(N) * COLS * sizeof(double2);
+  static constexpr size_t ROW_SMEM = (size_t)(padded(N) + padded(N / 2)) * ROWS * sizeof(double2);
+  static constexpr bool OK = V == 0 || (V == 1 && N <= 4096) || (V == 2 && N <= 1024);
+};
+
+template <int N, int V>
+__global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colinv(NltArgs a) {
+  if constexpr (Var<N, V>::OK) colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
+}
+template <int N, int V>
+__global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_nltv_row(NltArgs a) {
+  if constexpr (Var<N, V>::OK) row_tile<N, Var<N, V>::ROWS, Var<N, V>::R>(a, blockIdx.x);
+}
+template <int N, int V>
+__global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd(NltArgs a) {
+  if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
+}
+template <int N, int V>
+__global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltArgs cur, NltArgs next) {
+  if constexpr (Var<N, V>::OK) colfwd_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(cur, next, blockIdx.x);
 }
 
 // ---- ensemble kernels: one launch per pass for every member ------------------------------
@@ -472,6 +510,35 @@ k_row_c2r(double* z, const double2* __restrict__ tw) {
 #pragma unroll
   for (int s = 0; s < 8; ++s) row[t + s * T] = h[s];
   if (t == 0) row[M] = czero();
+}
+
+// Row C2R of a column-transformed field written as real(4) (N floats per row, no padding): the
+// physical field of a dump (src/write.f90:29-51) without a float64 round trip through HBM.
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::ROW_THREADS)
+k_row_c2r_f32(const double* __restrict__ z, float* __restrict__ out, const double2* __restrict__ tw) {
+  using S = Shape<N>;
+  constexpr int T = S::T, NH = S::NH, M = N / 2;
+  extern __shared__ double2 smem[];
+  const int r = threadIdx.x / T, t = threadIdx.x % T;
+  const int y = blockIdx.x * S::ROWS + r;
+  double2* zs = smem + (size_t)r * padded(M);
+  const double2* row = reinterpret_cast<const double2*>(z) + (size_t)y * NH;
+  double2 h[8];
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {
+    const int k = t + s * T;
+    double2 a = row[k], b = row[M - k];
+    if (k == 0) { a.y = 0.0; b.y = 0.0; }
+    const double2 sm_ = make_double2(a.x + b.x, a.y - b.y);
+    const double2 d = make_double2(a.x - b.x, a.y + b.y);
+    const double2 tt = twmul<true>(d, __ldg(&tw[k]));
+    h[s] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
+  }
+  fft_regs<M, 8, true, 1>(h, zs, t, tw, 1);
+  float2* orow = reinterpret_cast<float2*>(out) + (size_t)y * M;
+#pragma unroll
+  for (int s = 0; s < 8; ++s) orow[t + s * T] = make_float2((float)h[s].x, (float)h[s].y);
 }
 
 // Row R2C in place (N real -> NH complex), half-length packing.

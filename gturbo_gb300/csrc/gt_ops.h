@@ -25,16 +25,19 @@ enum OpKind : int {
   OP_ADJ_ROW = 11,
   OP_ADJ_COLFWD = 12,
   OP_NLT_COLFWD_INV = 13,  // pass C of stage nlt + pass A of stage nlt2
+  OP_ROW_C2R_F32 = 14,     // row C2R of `a` written as floats to `f32` (dumps)
 };
 
 struct GtOp {
   int kind;
+  int variant;        // launch variant of the nonlinear-term passes (Var<N, V>)
   cudaStream_t stream;
   NltArgs nlt;        // passes A, B, C
   NltArgs nlt2;       // the next stage (OP_NLT_COLFWD_INV)
   TlmArgs tlm;
   AdjArgs adj;
   double2* a;         // field of the standalone transforms
+  float* f32;         // real(4) output of OP_ROW_C2R_F32
   const double2* tw;
   double scale;
 };

@@ -46,6 +46,7 @@ struct gt_handle {
   std::vector<uint32_t> lcga, lcgb;  // index k: coefficients of the (k+1)-th draw
   uint32_t lcga_nf = 1, lcgb_nf = 0;
   int device = 0;
+  int variant = 0;  // launch variant of the nonlinear-term passes
   cudaStream_t stream = nullptr;
   std::string err;
   // device tables
@@ -249,6 +250,7 @@ GtOp base_op(const gt_handle* h) {
   GtOp op;
   std::memset(&op, 0, sizeof(op));
   op.stream = h->stream;
+  op.variant = h->variant;
   op.tw = h->d_tw;
   op.nlt = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, h->d_flag);
   return op;
@@ -334,6 +336,9 @@ int gt_create(const gt_params* p, gt_handle** out) {
   const int NH = h->NH = N / 2 + 1;
   h->NBIN = N / 2;
   h->dispatch = dispatch_for(N);
+  // The launch variant that timed fastest on GB300 for this grid size (RK2 and RK4 alike):
+  // 4 values per thread up to 512^2, 8 at 1024^2, 16 from 2048^2 up. gt_autotune re-times.
+  h->variant = N <= 512 ? 2 : N == 1024 ? 1 : 0;
   // inieuler.f90:22-36, 237-244
   int split = 0;
   if (p->alpnu < 1.0005 && p->alpnu > 0.9995 && p->alpmu < 0.0005 && p->alpmu > -0.0005) split = 1;
@@ -564,6 +569,18 @@ int gt_fft_inv(gt_handle* h, double* z) {
   return run(h, op);
 }
 
+int gt_dump_real4(gt_handle* h, double* work, float* out) {
+  if (!h || !work || !out) return fail(h, GT_ERR_ARG, "gt_dump_real4: null argument");
+  GtOp op = base_op(h);
+  op.a = reinterpret_cast<double2*>(work);
+  op.kind = gt::OP_COL_INV;
+  int rc = run(h, op);
+  if (rc) return rc;
+  op.f32 = out;
+  op.kind = gt::OP_ROW_C2R_F32;
+  return run(h, op);
+}
+
 int gt_trunc(gt_handle* h, double* z) {
   if (!h || !z) return fail(h, GT_ERR_ARG, "gt_trunc: null argument");
   gt::k_trunc<<<4 * 152, 256, 0, h->stream>>>(reinterpret_cast<double2*>(z), h->N, h->NH, h->d_kcut);
@@ -740,6 +757,95 @@ int gt_profile_read(gt_handle* h, double* ms, int64_t* launches) {
     launches[h->ev_kind[p]] += 1;
   }
   h->ev_kind.clear();
+  return GT_OK;
+}
+
+int gt_variant_supported(int32_t n, int32_t variant) {
+  if (!pow2_in_range(n)) return 0;
+  switch (variant) {
+    case 0: return 1;
+    case 1: return n <= 4096;
+    case 2: return n <= 1024;
+    default: return 0;
+  }
+}
+
+int gt_set_variant(gt_handle* h, int32_t variant) {
+  if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_variant: null handle");
+  if (!gt_variant_supported(h->N, variant))
+    return fail(h, GT_ERR_ARG, "gt_set_variant: variant " + std::to_string(variant) +
+                                   " does not exist for n=" + std::to_string(h->N));
+  h->variant = variant;
+  return GT_OK;
+}
+
+int gt_get_variant(const gt_handle* h, int32_t* variant) {
+  if (!h || !variant) return fail(nullptr, GT_ERR_ARG, "gt_get_variant: null argument");
+  *variant = h->variant;
+  return GT_OK;
+}
+
+int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best) {
+  if (!h) return fail(nullptr, GT_ERR_ARG, "gt_autotune: null handle");
+  if (steps < 1) return fail(h, GT_ERR_ARG, "gt_autotune: steps must be >= 1");
+  double ms[GT_NVARIANTS];
+  int navail = 0;
+  for (int v = 0; v < GT_NVARIANTS; ++v) {
+    ms[v] = -1.0;
+    navail += gt_variant_supported(h->N, v);
+  }
+  int choice = h->variant;
+  if (navail > 1) {
+    const size_t nd = (size_t)h->N * (size_t)(h->N + 2);
+    double* buf = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    const int saved = h->variant;
+    const bool prof = h->prof;
+    h->prof = false;
+    int rc = GT_OK;
+    cudaError_t e = cudaMalloc((void**)&buf, 5 * nd * sizeof(double));
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "gt_autotune: cudaMalloc");
+    if (!rc) e = cudaMemsetAsync(buf, 0, 5 * nd * sizeof(double), h->stream);
+    if (!rc && e == cudaSuccess) e = cudaEventCreate(&ev[0]);
+    if (!rc && e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+    if (!rc && e != cudaSuccess) rc = cuda_fail(h, e, "gt_autotune: set-up");
+    double* f[5];
+    for (int k = 0; k < 5; ++k) f[k] = buf ? buf + k * nd : nullptr;
+    auto one_step = [&]() {
+      return h->rko == 4 ? gt_step_rk4(h, f[0], f[1], f[2], f[3], f[4]) : gt_step_rk2(h, f[0], f[1], f[3], f[4]);
+    };
+    double best_ms = 0.0;
+    for (int v = 0; v < GT_NVARIANTS && !rc; ++v) {
+      if (!gt_variant_supported(h->N, v)) continue;
+      h->variant = v;
+      for (int w = 0; w < 3 && !rc; ++w) rc = one_step();
+      if (!rc) e = cudaEventRecord(ev[0], h->stream);
+      for (int s = 0; s < steps && !rc; ++s) rc = one_step();
+      if (!rc && e == cudaSuccess) e = cudaEventRecord(ev[1], h->stream);
+      if (!rc && e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+      float t = 0.0f;
+      if (!rc && e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+      if (!rc && e != cudaSuccess) rc = cuda_fail(h, e, "gt_autotune: timing");
+      if (rc) break;
+      ms[v] = (double)t / steps;
+      if (v == 0 || ms[v] < best_ms) {
+        best_ms = ms[v];
+        choice = v;
+      }
+    }
+    if (buf) {
+      cudaStreamSynchronize(h->stream);
+      cudaFree(buf);
+    }
+    for (cudaEvent_t x : ev)
+      if (x) cudaEventDestroy(x);
+    h->prof = prof;
+    h->variant = rc ? saved : choice;
+    if (rc) return rc;
+  }
+  if (ms_per_step)
+    for (int v = 0; v < GT_NVARIANTS; ++v) ms_per_step[v] = ms[v];
+  if (best) *best = h->variant;
   return GT_OK;
 }
 

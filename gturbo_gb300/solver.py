@@ -23,12 +23,39 @@ solver's stream (the current torch stream at construction unless one is given).
 from __future__ import annotations
 
 import ctypes
+import json
+import os
 
 import numpy as np
 import torch
 
 from . import _lib
 from .params import GtInfo, Params
+
+
+def _tune_cache_default() -> str:
+    """Autotuner cache: $GTURBO_TUNE_CACHE, else autotune.json beside the built library."""
+    return os.environ.get("GTURBO_TUNE_CACHE") or os.path.join(os.path.dirname(_lib.LIB_PATH),
+                                                               "autotune.json")
+
+
+def _read_cache(path: str | None) -> dict:
+    if path is None or not os.path.exists(path):
+        return {}
+    try:
+        with open(path) as f:
+            table = json.load(f)
+        return table if isinstance(table, dict) else {}
+    except (OSError, ValueError):
+        return {}
+
+
+def _write_cache(path: str, table: dict) -> None:
+    os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    tmp = f"{path}.{os.getpid()}.tmp"
+    with open(tmp, "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
 
 
 def spec(z: torch.Tensor) -> torch.Tensor:
@@ -114,12 +141,63 @@ class Solver:
         self._check(self.lib.gt_profile_read(self.h, ms, cnt))
         return {k: (ms[i], cnt[i]) for i, k in enumerate(self.PROF_KINDS)}
 
+    # -- launch variants (gt_set_variant / gt_autotune) -----------------------------------
+    NVARIANTS = 3
+
+    @property
+    def variant(self) -> int:
+        v = ctypes.c_int32()
+        self._check(self.lib.gt_get_variant(self.h, ctypes.byref(v)))
+        return v.value
+
+    @variant.setter
+    def variant(self, v: int) -> None:
+        self._check(self.lib.gt_set_variant(self.h, int(v)))
+
+    def supported_variants(self) -> list[int]:
+        return [v for v in range(self.NVARIANTS) if self.lib.gt_variant_supported(self.n, v)]
+
+    def autotune(self, steps: int = 20, cache: str | None = "default") -> dict:
+        """Pick the fastest launch variant of the nonlinear-term passes (gt_autotune).
+
+        With a cache file (JSON, keyed by device name, N and integrator order), a stored
+        choice is reused without timing; None disables the cache. Returns
+        {"variant": v, "ms_per_step": [...] or None, "cached": bool}.
+        """
+        if cache == "default":
+            cache = _tune_cache_default()
+        key = f"{torch.cuda.get_device_name(self.device)}|n={self.n}|rko={self.info.rko}"
+        table = _read_cache(cache)
+        if key in table and table[key]["variant"] in self.supported_variants():
+            self.variant = table[key]["variant"]
+            return {"variant": self.variant, "ms_per_step": table[key].get("ms_per_step"),
+                    "cached": True}
+        ms = (ctypes.c_double * self.NVARIANTS)()
+        best = ctypes.c_int32()
+        self._check(self.lib.gt_autotune(self.h, int(steps), ms, ctypes.byref(best)))
+        res = {"variant": best.value, "ms_per_step": list(ms), "cached": False}
+        if cache is not None:
+            table[key] = {"variant": best.value, "ms_per_step": list(ms)}
+            _write_cache(cache, table)
+        return res
+
     # -- the reference's routines -----------------------------------------------------------
     def fft_dir(self, z: torch.Tensor) -> None:
         self._check(self.lib.gt_fft_dir(self.h, self._ptr(z)))
 
     def fft_inv(self, z: torch.Tensor) -> None:
         self._check(self.lib.gt_fft_inv(self.h, self._ptr(z)))
+
+    def dump_real4(self, z: torch.Tensor) -> np.ndarray:
+        """The physical field of z as the reference's real(4) dump (src/write.f90:29-51): an
+        N x N float32 array (x fastest), inverse-transformed and converted on the device."""
+        with torch.cuda.stream(self.stream):
+            work = z.clone()
+            out = torch.empty((self.n, self.n), dtype=torch.float32, device=self.device)
+        self._check(self.lib.gt_dump_real4(self.h, self._ptr(work), out.data_ptr()))
+        with torch.cuda.stream(self.stream):
+            host = out.cpu()
+        return host.numpy()
 
     def trunc(self, z: torch.Tensor) -> None:
         self._check(self.lib.gt_trunc(self.h, self._ptr(z)))

@@ -100,6 +100,11 @@ int gt_fft_dir(gt_handle* h, double* z);
  * imaginary parts of the kx=0 and kx=N/2 values after the y-transform are
  * taken as zero (Hermitian input); the 2 padding doubles per row are zeroed. */
 int gt_fft_inv(gt_handle* h, double* z);
+/* Field dump (src/main.f90:119-125 + src/write.f90:29-51 without the host-side
+ * conversion): the physical field of the spectral field in `work` (destroyed,
+ * normally a copy of z as the reference's znl = z) written to the DEVICE array
+ * `out` as N*N real(4) values, x fastest: the record of fields/w.NNN.MMM. */
+int gt_dump_real4(gt_handle* h, double* work, float* out);
 /* 2/3-rule ellipse mask and zero mean, in place (src/trunc.f90:10-25). */
 int gt_trunc(gt_handle* h, double* z);
 /* Physical-space products u <- z*u, v <- z*v, padding zeroed (src/produ.f90:11-23). */
@@ -252,6 +257,27 @@ int gt_profile(gt_handle* h, int enable);
 /* Synchronises the stream, returns per class the summed kernel time (ms) and the number of
  * launches since the last read, and resets both. ms, launches: GT_PROF_KINDS entries. */
 int gt_profile_read(gt_handle* h, double* ms, int64_t* launches);
+
+/* ---- launch variants and the autotuner ---------------------------------- */
+
+/* No counterpart in the reference, whose transforms are cuFFT plans (src/fft_dir.f90,
+ * src/fft_inv.f90) that the library tunes internally. The three passes of the nonlinear
+ * term come in GT_NVARIANTS launch shapes: 0 = 16 values per thread, several columns/rows per
+ * block (large grids); 1 = 8 values per thread, one column/row per block (n <= 4096);
+ * 2 = 4 values per thread, one column/row per block (n <= 1024, for small latency-bound
+ * grids). The variants differ only in the radix decomposition of the transforms, so their
+ * results agree to rounding (relative differences of order 1e-15 per step). */
+#define GT_NVARIANTS 3
+/* 1 if launch variant `variant` exists for grid size n, else 0 (host only, no GPU needed). */
+int gt_variant_supported(int32_t n, int32_t variant);
+/* Select the variant used by every later nlt / step call of h (GT_ERR_ARG if unsupported). */
+int gt_set_variant(gt_handle* h, int32_t variant);
+int gt_get_variant(const gt_handle* h, int32_t* variant);
+/* Time `steps` steps of the handle's integrator (RK2 or RK4) for every supported variant on
+ * zero fields of its own (allocated and freed here, 5 fields; nothing when only one variant
+ * exists), keep the fastest, and return ms per step in ms_per_step[GT_NVARIANTS] (-1 for
+ * unsupported variants) and the choice in *best (either pointer may be null). Synchronous. */
+int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best);
 
 #ifdef __cplusplus
 }

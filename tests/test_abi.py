@@ -85,6 +85,15 @@ def test_null_arguments_are_errors_not_crashes(lib):
     assert lib.gt_diag(None, None, None, None, None, None, None, None) == 1
 
 
+def test_variant_table(lib):
+    """Launch variants by grid size: 0 always, 1 up to 4096, 2 up to 1024 (host only)."""
+    for n in (16, 64, 1024, 2048, 4096, 8192):
+        got = [lib.gt_variant_supported(n, v) for v in range(3)]
+        assert got == [1, int(n <= 4096), int(n <= 1024)], n
+    assert lib.gt_variant_supported(100, 0) == 0 and lib.gt_variant_supported(64, 3) == 0
+    assert lib.gt_set_variant(None, 0) == 1 and lib.gt_autotune(None, 1, None, None) == 1
+
+
 def test_read_params_dat_format():
     from gturbo_gb300.params import read_params_dat
     text = """6.2831853071795864769d0\t6.2831853071795864769d0

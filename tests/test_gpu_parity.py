@@ -65,6 +65,25 @@ def test_fft_dir(n):
     assert rel_l2(_host(z), ref) < TOL
 
 
+@pytest.mark.parametrize("n", [64, 512, 2048])
+def test_dump_real4(n, tmp_path):
+    """The real(4) field dump equals the oracle's fft_inv rounded to float32 (src/write.f90)
+    and round-trips through the reference's fields/w.NNN record format."""
+    from gturbo_gb300.ic import read_field, write_field
+    p = _params(n)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 21)
+    ref = a.copy()
+    orc.fft_inv(ref)
+    w = sol.dump_real4(_dev(a))
+    assert w.dtype == np.float32 and w.shape == (n, n)
+    ref32 = ref[:, :n].astype(np.float32)
+    assert np.all(np.abs(w - ref32) <= np.spacing(np.abs(ref32)))
+    f = tmp_path / "w.001.001"
+    write_field(str(f), w)
+    assert np.array_equal(read_field(str(f), n)[:, :n], w.astype(np.float64))
+
+
 @pytest.mark.parametrize("n", [16, 64, 256, 1024])
 def test_trunc_exact(n):
     p = _params(n)
@@ -314,3 +333,71 @@ def test_single_mode_decay_on_gpu():
     sol.rk_step(z, sol.work())
     e = orc.emk()[5, 3]
     assert spec(_host(z))[5, 3] == pytest.approx(e * e * (0.7 - 0.2j), rel=1e-14)
+
+
+# -- launch variants of the nonlinear-term passes and the autotuner ------------------------
+@pytest.mark.parametrize("n", [16, 64, 256, 1024, 4096])
+def test_nlt_variants(n):
+    """Every launch variant gives the oracle's nonlinear term."""
+    p = _params(n, alpv=1.0)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 21)
+    ref = a.copy()
+    orc.nlt(ref)
+    assert sol.supported_variants()[0] == 0
+    for v in sol.supported_variants():
+        sol.variant = v
+        z, u, vv = _dev(a), sol.field(), sol.field()
+        sol.nlt(z, u, vv)
+        assert rel_l2(_host(z), ref) < TOL, f"variant {v}"
+
+
+@pytest.mark.parametrize("n,rko", [(32, 4), (256, 2), (1024, 4)])
+def test_step_variants_untruncated(n, rko):
+    """Steps from an untruncated field (every column live in pass B) in every variant."""
+    p = _params(n, rko=rko, dt=2e-3)
+    orc = Oracle(p)
+    a = rand_field(orc, 22, truncate=False) * 20.0
+    ref = a.copy()
+    orc.rk_step(ref)
+    orc.rk_step(ref)
+    sol = _solver(p)
+    for v in sol.supported_variants():
+        sol.variant = v
+        z, work = _dev(a), sol.work()
+        sol.rk_step(z, work)
+        sol.rk_step(z, work)
+        assert rel_l2(_host(z), ref) < TOL, f"variant {v}"
+
+
+def test_variant_rejected_when_unsupported():
+    from gturbo_gb300._lib import GturboError
+    sol = _solver(_params(2048))
+    assert sol.supported_variants() == [0, 1]
+    with pytest.raises(GturboError):
+        sol.variant = 2
+    assert sol.variant == 0
+
+
+def test_autotune_and_cache(tmp_path):
+    p = _params(256, rko=2, dt=2e-3)
+    sol = _solver(p)
+    cache = str(tmp_path / "tune.json")
+    res = sol.autotune(steps=5, cache=cache)
+    assert not res["cached"]
+    assert res["variant"] in sol.supported_variants() and sol.variant == res["variant"]
+    ms = res["ms_per_step"]
+    assert all(ms[v] > 0 for v in sol.supported_variants())
+    assert ms[res["variant"]] == min(ms[v] for v in sol.supported_variants())
+    # a second solver reuses the stored choice without timing
+    sol2 = _solver(p)
+    res2 = sol2.autotune(steps=5, cache=cache)
+    assert res2["cached"] and sol2.variant == res["variant"]
+    # and the tuned handle still steps exactly like the oracle
+    orc = Oracle(p)
+    a = rand_field(orc, 23) * 50.0
+    ref = a.copy()
+    orc.rk_step(ref)
+    z = _dev(a)
+    sol2.rk_step(z, sol2.work())
+    assert rel_l2(_host(z), ref) < TOL
