@@ -131,6 +131,7 @@ gt::GtOp op_of(const gt_handle* h, int kind) {
   gt::GtOp op;
   std::memset(&op, 0, sizeof(op));
   op.kind = kind;
+  op.variant = gt::handle_variant(h);
   op.stream = gt::handle_stream(h);
   return op;
 }

@@ -52,9 +52,9 @@ __device__ __forceinline__ double stage_e(const double* emk, const double* emkx,
   return split ? __ldg(&emkx[i]) * __ldg(&emky[j]) : __ldg(&emk[(size_t)j * NH + i]);
 }
 
-template <int N, int C>
+template <int N, int C, int R = 16>
 __device__ __forceinline__ void tlm_colinv_tile(const TlmArgs& a, int tile) {
-  constexpr int T = N / 16, NH = N / 2 + 1;
+  constexpr int T = N / R, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
   const int c = threadIdx.x % C, t = threadIdx.x / C;
   const int i = tile * C + c;
@@ -62,13 +62,13 @@ __device__ __forceinline__ void tlm_colinv_tile(const TlmArgs& a, int tile) {
   const int ic = valid ? i : NH - 1;
   double2* sm = smem + c;
   const double kx = __ldg(&a.fkx[ic]);
-  double2 v[16];
+  double2 v[R];
   for (int f = 0; f < 6; ++f) {
     const double2* src = f < 3 ? a.x : a.dx;
     double2* dst = f == 0 ? a.q : f == 1 ? a.u : f == 2 ? a.v : f == 3 ? a.dq : f == 4 ? a.du : a.dv;
     const int kind = f % 3;  // 0: q, 1: Mu q, 2: Mv q
 #pragma unroll
-    for (int s = 0; s < 16; ++s) {
+    for (int s = 0; s < R; ++s) {
       const int j = t + s * T;
       const size_t o = (size_t)j * NH + ic;
       const double2 q = valid ? src[o] : czero();
@@ -83,20 +83,20 @@ __device__ __forceinline__ void tlm_colinv_tile(const TlmArgs& a, int tile) {
       }
     }
     __syncthreads();
-    fft_regs<N, 16, true, C>(v, sm, t, a.tw, 0);
+    fft_regs<N, R, true, C>(v, sm, t, a.tw, 0);
     if (valid) {
 #pragma unroll
-      for (int s = 0; s < 16; ++s) dst[(size_t)(t + s * T) * NH + i] = v[s];
+      for (int s = 0; s < R; ++s) dst[(size_t)(t + s * T) * NH + i] = v[s];
     }
   }
 }
 
 // X + iY as one complex spectrum of length N from two half spectra (Im at k=0, N/2 dropped)
-template <int N>
+template <int N, int R = 16>
 __device__ __forceinline__ void pair_spectrum(double2* cs, const double2* xrow, const double2* yrow, int t) {
-  constexpr int T = N / 16, M = N / 2;
+  constexpr int T = N / R, M = N / 2;
 #pragma unroll
-  for (int s = 0; s <= 8; ++s) {
+  for (int s = 0; s <= R / 2; ++s) {
     const int k = t + s * T;
     if (k <= M) {
       const double2 X = xrow[k], Y = yrow[k];
@@ -111,11 +111,11 @@ __device__ __forceinline__ void pair_spectrum(double2* cs, const double2* xrow, 
 }
 
 // split P (length N, in smem) into 2 FFT(Re p)[k] -> xrow, 2 FFT(Im p)[k] -> yrow, k <= N/2
-template <int N>
+template <int N, int R = 16>
 __device__ __forceinline__ void split_spectrum(const double2* cs, double2* xrow, double2* yrow, int t) {
-  constexpr int T = N / 16, M = N / 2;
+  constexpr int T = N / R, M = N / 2;
 #pragma unroll
-  for (int s = 0; s <= 8; ++s) {
+  for (int s = 0; s <= R / 2; ++s) {
     const int k = t + s * T;
     if (k <= M) {
       const double2 P = cs[padix(k)];
@@ -126,9 +126,9 @@ __device__ __forceinline__ void split_spectrum(const double2* cs, double2* xrow,
   }
 }
 
-template <int N, int ROWS>
+template <int N, int ROWS, int R = 16>
 __device__ __forceinline__ void tlm_row_tile(const TlmArgs& a, int tile) {
-  constexpr int T = N / 16, NH = N / 2 + 1;
+  constexpr int T = N / R, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
   const int r = threadIdx.x / T, t = threadIdx.x % T;
   const int y = tile * ROWS + r;
@@ -136,25 +136,25 @@ __device__ __forceinline__ void tlm_row_tile(const TlmArgs& a, int tile) {
   double2* c2 = c1 + padded(N);
   double2* c3 = c2 + padded(N);
   const size_t ro = (size_t)y * NH;
-  pair_spectrum<N>(c1, a.u + ro, a.v + ro, t);    // u + i v
-  pair_spectrum<N>(c2, a.du + ro, a.dv + ro, t);  // du + i dv
-  pair_spectrum<N>(c3, a.q + ro, a.dq + ro, t);   // q + i dq
+  pair_spectrum<N, R>(c1, a.u + ro, a.v + ro, t);    // u + i v
+  pair_spectrum<N, R>(c2, a.du + ro, a.dv + ro, t);  // du + i dv
+  pair_spectrum<N, R>(c3, a.q + ro, a.dq + ro, t);   // q + i dq
   __syncthreads();
-  double2 v[16];
+  double2 v[R];
   double2* bufs[3] = {c1, c2, c3};
   for (int b = 0; b < 3; ++b) {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) v[s] = bufs[b][padix(t + s * T)];
+    for (int s = 0; s < R; ++s) v[s] = bufs[b][padix(t + s * T)];
     __syncthreads();
-    fft_regs<N, 16, true, 1>(v, bufs[b], t, a.tw, 0);
+    fft_regs<N, R, true, 1>(v, bufs[b], t, a.tw, 0);
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < 16; ++s) bufs[b][padix(t + s * T)] = v[s];
+    for (int s = 0; s < R; ++s) bufs[b][padix(t + s * T)] = v[s];
   }
   __syncthreads();
   // products: p = (u + i v) q, dp = (du + i dv) q + (u + i v) dq
 #pragma unroll
-  for (int s = 0; s < 16; ++s) {
+  for (int s = 0; s < R; ++s) {
     const int x = padix(t + s * T);
     const double2 uv = c1[x], duv = c2[x], qq = c3[x];
     c1[x] = make_double2(uv.x * qq.x, uv.y * qq.x);
@@ -163,21 +163,21 @@ __device__ __forceinline__ void tlm_row_tile(const TlmArgs& a, int tile) {
   __syncthreads();
   for (int b = 0; b < 2; ++b) {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) v[s] = bufs[b][padix(t + s * T)];
+    for (int s = 0; s < R; ++s) v[s] = bufs[b][padix(t + s * T)];
     __syncthreads();
-    fft_regs<N, 16, false, 1>(v, bufs[b], t, a.tw, 0);
+    fft_regs<N, R, false, 1>(v, bufs[b], t, a.tw, 0);
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < 16; ++s) bufs[b][padix(t + s * T)] = v[s];
+    for (int s = 0; s < R; ++s) bufs[b][padix(t + s * T)] = v[s];
   }
   __syncthreads();
-  split_spectrum<N>(c1, a.u + ro, a.v + ro, t);
-  split_spectrum<N>(c2, a.du + ro, a.dv + ro, t);
+  split_spectrum<N, R>(c1, a.u + ro, a.v + ro, t);
+  split_spectrum<N, R>(c2, a.du + ro, a.dv + ro, t);
 }
 
-template <int N, int C>
+template <int N, int C, int R = 16>
 __device__ __forceinline__ void tlm_colfwd_tile(const TlmArgs& a, int tile) {
-  constexpr int T = N / 16, NH = N / 2 + 1;
+  constexpr int T = N / R, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
   const int c = threadIdx.x % C, t = threadIdx.x / C;
   const int i = tile * C + c;
@@ -187,26 +187,26 @@ __device__ __forceinline__ void tlm_colfwd_tile(const TlmArgs& a, int tile) {
   const double scale = 0.5 / ((double)N * (double)N);
   const double kxs = __ldg(&a.fkx[ic]) * scale;
   const int kc = a.truncate ? (valid ? __ldg(&a.kcut[i]) : -1) : N;
-  double2 v[16];
+  double2 v[R];
   for (int pr = 0; pr < 2; ++pr) {
     double2* af = pr == 0 ? a.u : a.du;
     const double2* bf = pr == 0 ? a.v : a.dv;
 #pragma unroll
-    for (int s = 0; s < 16; ++s) v[s] = valid ? af[(size_t)(t + s * T) * NH + ic] : czero();
+    for (int s = 0; s < R; ++s) v[s] = valid ? af[(size_t)(t + s * T) * NH + ic] : czero();
     __syncthreads();
-    fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
+    fft_regs<N, R, false, C>(v, sm, t, a.tw, 0);
     if (valid) {
 #pragma unroll
-      for (int s = 0; s < 16; ++s)
+      for (int s = 0; s < R; ++s)
         af[(size_t)(t + s * T) * NH + i] = make_double2(kxs * v[s].x, kxs * v[s].y);
     }
 #pragma unroll
-    for (int s = 0; s < 16; ++s) v[s] = valid ? bf[(size_t)(t + s * T) * NH + ic] : czero();
+    for (int s = 0; s < R; ++s) v[s] = valid ? bf[(size_t)(t + s * T) * NH + ic] : czero();
     __syncthreads();
-    fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
+    fft_regs<N, R, false, C>(v, sm, t, a.tw, 0);
     if (valid) {
 #pragma unroll
-      for (int s = 0; s < 16; ++s) {
+      for (int s = 0; s < R; ++s) {
         const int j = t + s * T;
         const size_t o = (size_t)j * NH + i;
         const double kys = __ldg(&a.fky[j]) * scale;
@@ -219,7 +219,7 @@ __device__ __forceinline__ void tlm_colfwd_tile(const TlmArgs& a, int tile) {
   }
   if (!valid) return;
 #pragma unroll
-  for (int s = 0; s < 16; ++s) {
+  for (int s = 0; s < R; ++s) {
     const int j = t + s * T;
     const size_t o = (size_t)j * NH + i;
     const double e = stage_e(a.emk, a.emkx, a.emky, a.split, i, j, NH);
@@ -270,9 +270,9 @@ struct AdjArgs {
   double dt, dt2;
 };
 
-template <int N, int C>
+template <int N, int C, int R = 16>
 __device__ __forceinline__ void adj_colinv_tile(const AdjArgs& a, int tile) {
-  constexpr int T = N / 16, NH = N / 2 + 1;
+  constexpr int T = N / R, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
   const int c = threadIdx.x % C, t = threadIdx.x / C;
   const int i = tile * C + c;
@@ -282,11 +282,11 @@ __device__ __forceinline__ void adj_colinv_tile(const AdjArgs& a, int tile) {
   const double kx = __ldg(&a.fkx[ic]);
   const int kc = a.truncate ? __ldg(&a.kcut[ic]) : N;
   const double wcol = (ic == 0 || ic == NH - 1) ? 1.0 : 0.5;
-  double2 v[16];
+  double2 v[R];
   for (int f = 0; f < 5; ++f) {
     double2* dst = f == 0 ? a.q : f == 1 ? a.u : f == 2 ? a.v : f == 3 ? a.a : a.b;
 #pragma unroll
-    for (int s = 0; s < 16; ++s) {
+    for (int s = 0; s < R; ++s) {
       const int j = t + s * T;
       const size_t o = (size_t)j * NH + ic;
       if (f < 3) {
@@ -313,17 +313,17 @@ __device__ __forceinline__ void adj_colinv_tile(const AdjArgs& a, int tile) {
       }
     }
     __syncthreads();
-    fft_regs<N, 16, true, C>(v, sm, t, a.tw, 0);
+    fft_regs<N, R, true, C>(v, sm, t, a.tw, 0);
     if (valid) {
 #pragma unroll
-      for (int s = 0; s < 16; ++s) dst[(size_t)(t + s * T) * NH + i] = v[s];
+      for (int s = 0; s < R; ++s) dst[(size_t)(t + s * T) * NH + i] = v[s];
     }
   }
 }
 
-template <int N, int ROWS>
+template <int N, int ROWS, int R = 16>
 __device__ __forceinline__ void adj_row_tile(const AdjArgs& a, int tile) {
-  constexpr int T = N / 16, NH = N / 2 + 1, M = N / 2;
+  constexpr int T = N / R, NH = N / 2 + 1, M = N / 2;
   extern __shared__ double2 smem[];
   const int r = threadIdx.x / T, t = threadIdx.x % T;
   const int y = tile * ROWS + r;
@@ -331,11 +331,11 @@ __device__ __forceinline__ void adj_row_tile(const AdjArgs& a, int tile) {
   double2* c2 = c1 + padded(N);
   double2* zs = c2 + padded(N);
   const size_t ro = (size_t)y * NH;
-  pair_spectrum<N>(c1, a.u + ro, a.v + ro, t);  // u + i v
-  pair_spectrum<N>(c2, a.a + ro, a.b + ro, t);  // a + i b
+  pair_spectrum<N, R>(c1, a.u + ro, a.v + ro, t);  // u + i v
+  pair_spectrum<N, R>(c2, a.a + ro, a.b + ro, t);  // a + i b
   const double2* qrow = a.q + ro;
 #pragma unroll
-  for (int s = 0; s < 8; ++s) {  // half-length C2R packing of q
+  for (int s = 0; s < R / 2; ++s) {  // half-length C2R packing of q
     const int k = t + s * T;
     double2 p = qrow[k], b = qrow[M - k];
     if (k == 0) { p.y = 0.0; b.y = 0.0; }
@@ -346,32 +346,32 @@ __device__ __forceinline__ void adj_row_tile(const AdjArgs& a, int tile) {
   }
   __syncthreads();
   {
-    double2 h[8];
+    double2 h[R / 2];
 #pragma unroll
-    for (int s = 0; s < 8; ++s) h[s] = zs[padix(t + s * T)];
+    for (int s = 0; s < R / 2; ++s) h[s] = zs[padix(t + s * T)];
     __syncthreads();
-    fft_regs<M, 8, true, 1>(h, zs, t, a.tw, 1);
+    fft_regs<M, R / 2, true, 1>(h, zs, t, a.tw, 1);
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < 8; ++s) zs[padix(t + s * T)] = h[s];
+    for (int s = 0; s < R / 2; ++s) zs[padix(t + s * T)] = h[s];
   }
-  double2 v[16];
+  double2 v[R];
   double2* bufs[2] = {c1, c2};
   for (int b = 0; b < 2; ++b) {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) v[s] = bufs[b][padix(t + s * T)];
+    for (int s = 0; s < R; ++s) v[s] = bufs[b][padix(t + s * T)];
     __syncthreads();
-    fft_regs<N, 16, true, 1>(v, bufs[b], t, a.tw, 0);
+    fft_regs<N, R, true, 1>(v, bufs[b], t, a.tw, 0);
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < 16; ++s) bufs[b][padix(t + s * T)] = v[s];
+    for (int s = 0; s < R; ++s) bufs[b][padix(t + s * T)] = v[s];
   }
   __syncthreads();
   // s1 = u a + v b (into zs, as packed pairs), s2 + i s3 = q (a + i b) (into c2); a, b / N^2
   const double inv = 1.0 / ((double)N * (double)N);
-  double s1v[16];
+  double s1v[R];
 #pragma unroll
-  for (int s = 0; s < 16; ++s) {
+  for (int s = 0; s < R; ++s) {
     const int x = t + s * T;
     const double2 uv = c1[padix(x)];
     const double2 ab = c2[padix(x)];
@@ -384,7 +384,7 @@ __device__ __forceinline__ void adj_row_tile(const AdjArgs& a, int tile) {
   __syncthreads();
   // repack s1 as z[m] = s1[2m] + i s1[2m+1] in zs (x even -> .x, odd -> .y)
 #pragma unroll
-  for (int s = 0; s < 16; ++s) {
+  for (int s = 0; s < R; ++s) {
     const int x = t + s * T;
     double* zd = reinterpret_cast<double*>(zs + padix(x >> 1));
     zd[x & 1] = s1v[s];
@@ -392,28 +392,28 @@ __device__ __forceinline__ void adj_row_tile(const AdjArgs& a, int tile) {
   __syncthreads();
   // forward transforms: s2 + i s3 (length N), s1 (half length)
 #pragma unroll
-  for (int s = 0; s < 16; ++s) v[s] = c2[padix(t + s * T)];
+  for (int s = 0; s < R; ++s) v[s] = c2[padix(t + s * T)];
   __syncthreads();
-  fft_regs<N, 16, false, 1>(v, c2, t, a.tw, 0);
+  fft_regs<N, R, false, 1>(v, c2, t, a.tw, 0);
   __syncthreads();
 #pragma unroll
-  for (int s = 0; s < 16; ++s) c2[padix(t + s * T)] = v[s];
+  for (int s = 0; s < R; ++s) c2[padix(t + s * T)] = v[s];
   {
-    double2 h[8];
+    double2 h[R / 2];
 #pragma unroll
-    for (int s = 0; s < 8; ++s) h[s] = zs[padix(t + s * T)];
+    for (int s = 0; s < R / 2; ++s) h[s] = zs[padix(t + s * T)];
     __syncthreads();
-    fft_regs<M, 8, false, 1>(h, zs, t, a.tw, 1);
+    fft_regs<M, R / 2, false, 1>(h, zs, t, a.tw, 1);
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < 8; ++s) zs[padix(t + s * T)] = h[s];
+    for (int s = 0; s < R / 2; ++s) zs[padix(t + s * T)] = h[s];
   }
   __syncthreads();
-  split_spectrum<N>(c2, a.u + ro, a.v + ro, t);  // 2 FFT(s2), 2 FFT(s3)
+  split_spectrum<N, R>(c2, a.u + ro, a.v + ro, t);  // 2 FFT(s2), 2 FFT(s3)
   // 2 FFT(s1)[k] = (Z[k] + conj Z[M-k]) - i W^k (Z[k] - conj Z[M-k]), k in [0, M]
   double2* s1row = a.q + ro;
 #pragma unroll
-  for (int s = 0; s <= 8; ++s) {
+  for (int s = 0; s <= R / 2; ++s) {
     const int k = t + s * T;
     if (k <= M) {
       const double2 p = zs[padix(k & (M - 1))];
@@ -426,9 +426,9 @@ __device__ __forceinline__ void adj_row_tile(const AdjArgs& a, int tile) {
   }
 }
 
-template <int N, int C>
+template <int N, int C, int R = 16>
 __device__ __forceinline__ void adj_colfwd_tile(const AdjArgs& a, int tile) {
-  constexpr int T = N / 16, NH = N / 2 + 1;
+  constexpr int T = N / R, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
   const int c = threadIdx.x % C, t = threadIdx.x / C;
   const int i = tile * C + c;
@@ -438,16 +438,16 @@ __device__ __forceinline__ void adj_colfwd_tile(const AdjArgs& a, int tile) {
   const double kx = __ldg(&a.fkx[ic]);
   // c o (.)/2: the row pass delivered 2 FFT(s); c = 1 on kx=0 and Nyquist, 2 inside
   const double cw = (ic == 0 || ic == NH - 1) ? 0.5 : 1.0;
-  double2 v[16];
+  double2 v[R];
   for (int f = 0; f < 3; ++f) {
     const double2* src = f == 0 ? a.q : f == 1 ? a.u : a.v;
 #pragma unroll
-    for (int s = 0; s < 16; ++s) v[s] = valid ? src[(size_t)(t + s * T) * NH + ic] : czero();
+    for (int s = 0; s < R; ++s) v[s] = valid ? src[(size_t)(t + s * T) * NH + ic] : czero();
     __syncthreads();
-    fft_regs<N, 16, false, C>(v, sm, t, a.tw, 0);
+    fft_regs<N, R, false, C>(v, sm, t, a.tw, 0);
     if (valid) {
 #pragma unroll
-      for (int s = 0; s < 16; ++s) {
+      for (int s = 0; s < R; ++s) {
         const int j = t + s * T;
         const size_t o = (size_t)j * NH + i;
         double2 acc;
@@ -465,7 +465,7 @@ __device__ __forceinline__ void adj_colfwd_tile(const AdjArgs& a, int tile) {
   }
   if (!valid) return;
 #pragma unroll
-  for (int s = 0; s < 16; ++s) {
+  for (int s = 0; s < R; ++s) {
     const int j = t + s * T;
     const size_t o = (size_t)j * NH + i;
     const double2 g = a.q[o];
@@ -514,6 +514,41 @@ __global__ void __launch_bounds__(Shape<N>::ROW_THREADS) k_adj_row(AdjArgs a) {
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS) k_adj_colfwd(AdjArgs a) {
   if constexpr (AdjShape<N>::OK) adj_colfwd_tile<N, Shape<N>::COLS>(a, blockIdx.x);
+}
+
+// The tangent-linear and adjoint passes in launch variant V of the nonlinear-term passes
+// (Var<N, V>: 8 or 4 values per thread, one column / row per block).
+template <int N, int V>
+struct AdjVar {
+  using W = Var<N, V>;
+  static constexpr size_t TLM_ROW_SMEM = (size_t)3 * padded(N) * W::ROWS * sizeof(double2);
+  static constexpr size_t ADJ_ROW_SMEM = (size_t)(2 * padded(N) + padded(N / 2)) * W::ROWS * sizeof(double2);
+  static constexpr bool OK = W::OK && AdjShape<N>::OK;
+};
+
+template <int N, int V>
+__global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_tlmv_colinv(TlmArgs a) {
+  if constexpr (AdjVar<N, V>::OK) tlm_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
+}
+template <int N, int V>
+__global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_tlmv_row(TlmArgs a) {
+  if constexpr (AdjVar<N, V>::OK) tlm_row_tile<N, Var<N, V>::ROWS, Var<N, V>::R>(a, blockIdx.x);
+}
+template <int N, int V>
+__global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_tlmv_colfwd(TlmArgs a) {
+  if constexpr (AdjVar<N, V>::OK) tlm_colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
+}
+template <int N, int V>
+__global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_adjv_colinv(AdjArgs a) {
+  if constexpr (AdjVar<N, V>::OK) adj_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
+}
+template <int N, int V>
+__global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_adjv_row(AdjArgs a) {
+  if constexpr (AdjVar<N, V>::OK) adj_row_tile<N, Var<N, V>::ROWS, Var<N, V>::R>(a, blockIdx.x);
+}
+template <int N, int V>
+__global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_adjv_colfwd(AdjArgs a) {
+  if constexpr (AdjVar<N, V>::OK) adj_colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
 }
 
 }  // namespace gt

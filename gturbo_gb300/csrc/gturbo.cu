@@ -136,6 +136,7 @@ int* handle_flag(const gt_handle* h) { return h->d_flag; }
 
 const gt_params* handle_params(const gt_handle* h) { return &h->p; }
 int handle_rko(const gt_handle* h) { return h->rko; }
+int handle_variant(const gt_handle* h) { return h->variant; }
 cudaStream_t handle_stream(const gt_handle* h) { return h->stream; }
 
 }  // namespace gt

@@ -118,3 +118,26 @@ def test_adjoint_limits():
     sol = Solver(Params(n=64, rko=4))
     with pytest.raises(_lib.GturboError):
         gradient(sol, sol.field(), 2, SEED, KMIN, KMAX)
+
+
+@pytest.mark.parametrize("n", [128, 1024])
+def test_adjoint_in_every_launch_variant(n):
+    """The gradient and the tangent-linear dJ in each launch variant: dot-product test per
+    variant, and the same gradient (to rounding) from every variant."""
+    from gturbo_gb300.adjoint import gradient, tlm_run
+    p, sol, z0, ns = _setup(n=n, nsteps=6)
+    dz = _direction(z0, 3)
+    grads = []
+    for v in sol.supported_variants():
+        sol.variant = v
+        J, gz, gf, _, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=3)
+        J2, dJ = tlm_run(sol, z0, dz, 0.4, ns, SEED, KMIN, KMAX)
+        adj = float((gz * dz).sum().item()) + gf * 0.4
+        assert J2 == pytest.approx(J, rel=1e-14), v
+        assert adj == pytest.approx(dJ, rel=1e-11, abs=1e-14 * abs(J)), v
+        grads.append((J, gz, gf))
+    J0, g0, f0 = grads[0]
+    for J, gz, gf in grads[1:]:
+        assert J == pytest.approx(J0, rel=1e-12)
+        assert float((gz - g0).norm() / g0.norm()) < 1e-12
+        assert gf == pytest.approx(f0, rel=1e-11)
