@@ -55,6 +55,34 @@ def test_struct_layout_matches_header(ctype, cname):
     assert offs == [getattr(ctype, f).offset for f in fields]
 
 
+def test_fortran_module_matches_header():
+    """include/gturbo_c.f90 (the bind(C) module for the Fortran driver; no Fortran compiler
+    here): every bound name is declared in gturbo.h with the same number of arguments, and its
+    gt_params type lists the C struct's fields in order with matching kinds."""
+    import re
+    text = open(os.path.join(ROOT, "include", "gturbo_c.f90")).read()
+    header = open(_lib.HEADER).read()
+    header = re.sub(r"/\*.*?\*/", "", header, flags=re.S)
+    binds = re.findall(r"function\s+(\w+)\s*\(([^)]*)\)\s*&?\s*bind\(C, name=\"(\w+)\"\)", text)
+    assert len(binds) >= 19
+    for fname, args, cname in binds:
+        assert fname == cname
+        m = re.search(r"\b%s\s*\(([^)]*)\)" % cname, header)
+        assert m, cname
+        n_c = len([a for a in m.group(1).split(",") if a.strip()])
+        n_f = len([a for a in args.split(",") if a.strip()])
+        assert n_c == n_f, (cname, n_c, n_f)
+    ftype = re.search(r"type, bind\(C\) :: gt_params(.*?)end type", text, re.S).group(1)
+    fields = []
+    for line in ftype.strip().splitlines():
+        kind, names = line.split("::")
+        fields += [(kind.strip(), n.strip()) for n in names.split(",")]
+    assert [n for _, n in fields] == [f for f, _ in GtParams._fields_]
+    for (kind, name), (_, ct) in zip(fields, GtParams._fields_):
+        assert ("c_int32_t" in kind) == (ct is ctypes.c_int32), name
+        assert ("c_double" in kind) == (ct is ctypes.c_double), name
+
+
 def test_gt_rann_is_the_reference_lcg(lib):
     s = ctypes.c_int32(481929)
     got = np.array([lib.gt_rann(ctypes.byref(s)) for _ in range(500)], np.float32)
