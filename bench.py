@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--config", default="c2")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU-baseline sample budget")
     ap.add_argument("--no-extras", action="store_true", help="skip e2e / cpu / ref-equivalent legs")
+    ap.add_argument("--only", choices=["ensemble", "adjoint"], default=None,
+                    help="run one secondary leg alone and print its JSON object (profiling)")
     return ap.parse_args()
 
 
@@ -532,6 +534,14 @@ def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.only is not None:
+        import torch
+        if args.only == "ensemble":
+            res = ensemble_run(args.steps, max(3, args.warmup), torch)
+        else:
+            res = adjoint_run(torch)
+        print(json.dumps(res), flush=True)
+        return 0
     return ours_arm(args)
 
 
