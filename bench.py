@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--config", default="c2")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU-baseline sample budget")
     ap.add_argument("--no-extras", action="store_true", help="skip e2e / cpu / ref-equivalent legs")
+    ap.add_argument("--variant", type=int, default=None,
+                    help="launch variant of the nonlinear-term passes (default: autotuned)")
     ap.add_argument("--only", choices=["ensemble", "adjoint"], default=None,
                     help="run one secondary leg alone and print its JSON object (profiling)")
     return ap.parse_args()
@@ -244,7 +246,11 @@ def ours_arm(args):
     sol = Solver(p, device=local)
     # launch variant of the nonlinear-term passes: timed per variant before the run (like a
     # cuFFT plan, outside the timed region)
-    tune = sol.autotune(steps=50 if p.n <= 1024 else 10, cache=None)
+    if args.variant is None:
+        tune = sol.autotune(steps=50 if p.n <= 1024 else 10, cache=None)
+    else:
+        sol.variant = args.variant
+        tune = {"variant": args.variant, "ms_per_step": None}
     stream = sol.stream
     work = sol.work()
     z0 = torch.from_numpy(random_phase_ic(p, k0, 0.5, seed=replica_ic_seed(rank))).to(dev)

@@ -178,10 +178,18 @@ int forcing_dot_dev(gt_handle* h, const double* lam, uint32_t seed0, double* d_o
   return GT_OK;
 }
 
+// Physical fields of one forward evaluation, as its pass B stores them (both null: not kept).
+struct Phys {
+  double2* uv = nullptr;
+  double2* q = nullptr;
+};
+
 // w = P0 e (z + dt/2 N(z)): the forward stage A with the fused passes (work: 3 fields)
-int stage_a(gt_handle* h, const double* z, double* w, double* const* work) {
+int stage_a(gt_handle* h, const double* z, double* w, double* const* work, Phys keep = Phys()) {
   gt::GtOp op = op_of(h, gt::OP_NLT_COLINV);
   op.nlt = gt::handle_nlt_args(h, z, work[0], work[1], work[2], gt::handle_flag(h));
+  op.nlt.phys_uv = keep.uv;
+  op.nlt.phys_q = keep.q;
   op.nlt.epi.mode = gt::EPI_RK2A;
   op.nlt.epi.out = reinterpret_cast<double2*>(w);
   op.nlt.epi.z = reinterpret_cast<const double2*>(z);
@@ -189,9 +197,11 @@ int stage_a(gt_handle* h, const double* z, double* w, double* const* work) {
 }
 
 // z_next = P0 e (e z + dt N(w)) written to `out` (may alias z) (work: 3 fields)
-int stage_b(gt_handle* h, const double* w, double* out, double* const* work) {
+int stage_b(gt_handle* h, const double* w, double* out, double* const* work, Phys keep = Phys()) {
   gt::GtOp op = op_of(h, gt::OP_NLT_COLINV);
   op.nlt = gt::handle_nlt_args(h, w, work[0], work[1], work[2], gt::handle_flag(h));
+  op.nlt.phys_uv = keep.uv;
+  op.nlt.phys_q = keep.q;
   op.nlt.epi.mode = gt::EPI_RK2B;
   op.nlt.epi.out = reinterpret_cast<double2*>(out);
   op.nlt.epi.z = reinterpret_cast<const double2*>(out);
@@ -235,11 +245,14 @@ gt::AdjArgs adj_args(const gt_handle* h) {
   a.split = t.split;
   a.dt = t.dt;
   a.dt2 = t.dt2;
+  a.kxlim = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, nullptr).kxlim;
   return a;
 }
 
-// one adjoint step (without the forcing dot), work: q, u, v, a, b, rho
-int adj_step(gt_handle* h, const double* z, const double* w, double* lam, double* const* work) {
+// one adjoint step (without the forcing dot), work: q, u, v, a, b, rho; pz, pw: the physical
+// fields of the forward evaluations at z and w when the caller kept them
+int adj_step(gt_handle* h, const double* z, const double* w, double* lam, double* const* work,
+             Phys pz = Phys(), Phys pw = Phys()) {
   gt::GtOp op = op_of(h, gt::OP_ADJ_COLINV);
   gt::AdjArgs a = adj_args(h);
   a.q = reinterpret_cast<double2*>(work[0]);
@@ -253,6 +266,8 @@ int adj_step(gt_handle* h, const double* z, const double* w, double* lam, double
   a.mode = gt::ADJ_STAGE_B;
   a.x = reinterpret_cast<const double2*>(w);
   a.lin = reinterpret_cast<const double2*>(lam);
+  a.phys_uv = pw.uv;
+  a.phys_q = pw.q;
   op.adj = a;
   int rc = run3(h, op, gt::OP_ADJ_COLINV);
   if (rc) return rc;
@@ -260,6 +275,8 @@ int adj_step(gt_handle* h, const double* z, const double* w, double* lam, double
   a.mode = gt::ADJ_STAGE_A;
   a.x = reinterpret_cast<const double2*>(z);
   a.lin = a.rho;
+  a.phys_uv = pz.uv;
+  a.phys_q = pz.q;
   op.adj = a;
   return run3(h, op, gt::OP_ADJ_COLINV);
 }
@@ -382,6 +399,26 @@ int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed
     return afail(h, GT_ERR_NOMEM, "gt_adj_gradient: cudaMalloc of the checkpoint storage failed");
   double* dots = scal;           // [nsteps]
   double* rows = scal + nsteps;  // [n + 1], objective scratch + result
+  // The physical u+iv and q of every recomputed stage of a segment (2K evaluations, 24 N^2 bytes
+  // each), so that the adjoint passes do not transform the linearisation points again. Without
+  // the memory for them the adjoint recomputes those transforms itself.
+  DevPool phys_pool;
+  std::vector<Phys> pz(K), pw(K);
+  {
+    const size_t uvb = sizeof(double2) * (size_t)n * n, qb = sizeof(double2) * (size_t)n * (n / 2);
+    bool ok = true;
+    for (int r = 0; r < K && ok; ++r) {
+      pz[r].uv = reinterpret_cast<double2*>(phys_pool.field(uvb));
+      pz[r].q = reinterpret_cast<double2*>(phys_pool.field(qb));
+      pw[r].uv = reinterpret_cast<double2*>(phys_pool.field(uvb));
+      pw[r].q = reinterpret_cast<double2*>(phys_pool.field(qb));
+      ok = pz[r].uv && pz[r].q && pw[r].uv && pw[r].q;
+    }
+    if (!ok) {
+      cudaGetLastError();  // clear the failed allocation
+      for (int r = 0; r < K; ++r) pz[r] = pw[r] = Phys();
+    }
+  }
   cudaEvent_t e0, e1, e2;
   GA_CUDA(h, cudaEventCreate(&e0));
   GA_CUDA(h, cudaEventCreate(&e1));
@@ -390,12 +427,22 @@ int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed
   GA_CUDA(h, cudaEventRecord(e0, s));
   // forward sweep, checkpoint every K steps
   GA_CUDA(h, cudaMemcpyAsync(z, z0, fb, cudaMemcpyDeviceToDevice, s));
+  // The last segment keeps its states (z_s, w_s) and physical fields as it goes: the backward
+  // sweep starts on it without recomputing it.
+  const int last0 = (ncp - 1) * K;
   int32_t sd = seed;
   for (int st = 0; st < nsteps; ++st) {
     if (st % K == 0) GA_CUDA(h, cudaMemcpyAsync(cp[st / K], z, fb, cudaMemcpyDeviceToDevice, s));
     seeds[st] = sd;
-    rc = stage_a(h, z, ws[0], work.data());
-    if (!rc) rc = stage_b(h, ws[0], z, work.data());
+    if (st >= last0) {
+      const int r = st - last0;
+      GA_CUDA(h, cudaMemcpyAsync(zs[r], z, fb, cudaMemcpyDeviceToDevice, s));
+      rc = stage_a(h, z, ws[r], work.data(), pz[r]);
+      if (!rc) rc = stage_b(h, ws[r], z, work.data(), pw[r]);
+    } else {
+      rc = stage_a(h, z, ws[0], work.data());
+      if (!rc) rc = stage_b(h, ws[0], z, work.data());
+    }
     if (!rc) rc = gt_forcing(h, z, &sd);
     if (rc) return rc;
   }
@@ -406,14 +453,15 @@ int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed
   // backward sweep: per segment, recompute and store (z_s, w_s), then run the adjoint back
   for (int c = ncp - 1; c >= 0; --c) {
     const int s0 = c * K, s1 = (s0 + K < nsteps) ? s0 + K : nsteps;
-    GA_CUDA(h, cudaMemcpyAsync(zs[0], cp[c], fb, cudaMemcpyDeviceToDevice, s));
-    for (int st = s0; st < s1; ++st) {
+    const bool kept = (c == ncp - 1);  // stored by the forward sweep
+    if (!kept) GA_CUDA(h, cudaMemcpyAsync(zs[0], cp[c], fb, cudaMemcpyDeviceToDevice, s));
+    for (int st = s0; st < s1 && !kept; ++st) {
       const int r = st - s0;
-      rc = stage_a(h, zs[r], ws[r], work.data());
+      rc = stage_a(h, zs[r], ws[r], work.data(), pz[r]);
       if (rc) return rc;
       if (st + 1 < s1) {
         GA_CUDA(h, cudaMemcpyAsync(zs[r + 1], zs[r], fb, cudaMemcpyDeviceToDevice, s));
-        rc = stage_b(h, ws[r], zs[r + 1], work.data());
+        rc = stage_b(h, ws[r], zs[r + 1], work.data(), pw[r]);
         int32_t sk = seeds[st];
         if (!rc) rc = gt_forcing(h, zs[r + 1], &sk);
         if (rc) return rc;
@@ -422,7 +470,8 @@ int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed
     for (int st = s1 - 1; st >= s0; --st) {
       const int r = st - s0;
       rc = forcing_dot_dev(h, lam, (uint32_t)seeds[st], dots + st);
-      if (!rc) rc = adj_step(h, zs[r], ws[r], lam, work.data());
+      // a recomputed segment's last stage B was not evaluated: its adjoint transforms w itself
+      if (!rc) rc = adj_step(h, zs[r], ws[r], lam, work.data(), pz[r], (kept || st + 1 < s1) ? pw[r] : Phys());
       if (rc) return rc;
     }
   }

@@ -93,13 +93,15 @@ __device__ __forceinline__ void tlm_colinv_tile(const TlmArgs& a, int tile) {
 
 // X + iY as one complex spectrum of length N from two half spectra (Im at k=0, N/2 dropped)
 template <int N, int R = 16>
-__device__ __forceinline__ void pair_spectrum(double2* cs, const double2* xrow, const double2* yrow, int t) {
+__device__ __forceinline__ void pair_spectrum(double2* cs, const double2* xrow, const double2* yrow, int t,
+                                              int kl = N / 2) {
   constexpr int T = N / R, M = N / 2;
 #pragma unroll
   for (int s = 0; s <= R / 2; ++s) {
     const int k = t + s * T;
     if (k <= M) {
-      const double2 X = xrow[k], Y = yrow[k];
+      const double2 X = (k <= kl) ? xrow[k] : czero();
+      const double2 Y = (k <= kl) ? yrow[k] : czero();
       if (k == 0 || k == M) {
         cs[padix(k)] = make_double2(X.x, Y.x);
       } else {
@@ -251,8 +253,15 @@ enum AdjMode : int {
 
 struct AdjArgs {
   int n;
+  int kxlim;           // last column with a retained mode (N/2 without dealiasing)
   const double2* x;    // linearisation point
   const double2* lin;  // adjoint input (l' or rho)
+  // Optional: the physical u + i v and packed q at x, as pass B of the forward evaluation at x
+  // stored them (NltArgs::phys_uv / phys_q). Given them, pass A transforms only the adjoint
+  // inputs a, b (whose columns beyond kxlim are zero after the 2/3 mask) and pass B skips the
+  // three inverse transforms of x.
+  const double2* phys_uv;
+  const double2* phys_q;
   double2 *q, *u, *v, *a, *b;  // scratch; S1, S2, S3 leave in q, u, v
   const double* kainv;
   const double* fkx;
@@ -283,7 +292,9 @@ __device__ __forceinline__ void adj_colinv_tile(const AdjArgs& a, int tile) {
   const int kc = a.truncate ? __ldg(&a.kcut[ic]) : N;
   const double wcol = (ic == 0 || ic == NH - 1) ? 1.0 : 0.5;
   double2 v[R];
-  for (int f = 0; f < 5; ++f) {
+  const bool phys = a.phys_uv != nullptr;
+  if (phys && tile * C > a.kxlim) return;  // a, b are zero there; pass B reads them as zero
+  for (int f = phys ? 3 : 0; f < 5; ++f) {
     double2* dst = f == 0 ? a.q : f == 1 ? a.u : f == 2 ? a.v : f == 3 ? a.a : a.b;
 #pragma unroll
     for (int s = 0; s < R; ++s) {
@@ -331,40 +342,60 @@ __device__ __forceinline__ void adj_row_tile(const AdjArgs& a, int tile) {
   double2* c2 = c1 + padded(N);
   double2* zs = c2 + padded(N);
   const size_t ro = (size_t)y * NH;
-  pair_spectrum<N, R>(c1, a.u + ro, a.v + ro, t);  // u + i v
-  pair_spectrum<N, R>(c2, a.a + ro, a.b + ro, t);  // a + i b
-  const double2* qrow = a.q + ro;
-#pragma unroll
-  for (int s = 0; s < R / 2; ++s) {  // half-length C2R packing of q
-    const int k = t + s * T;
-    double2 p = qrow[k], b = qrow[M - k];
-    if (k == 0) { p.y = 0.0; b.y = 0.0; }
-    const double2 sm_ = make_double2(p.x + b.x, p.y - b.y);
-    const double2 d = make_double2(p.x - b.x, p.y + b.y);
-    const double2 tt = twmul<true>(d, __ldg(&a.tw[k]));
-    zs[padix(k)] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
-  }
-  __syncthreads();
-  {
-    double2 h[R / 2];
-#pragma unroll
-    for (int s = 0; s < R / 2; ++s) h[s] = zs[padix(t + s * T)];
-    __syncthreads();
-    fft_regs<M, R / 2, true, 1>(h, zs, t, a.tw, 1);
-    __syncthreads();
-#pragma unroll
-    for (int s = 0; s < R / 2; ++s) zs[padix(t + s * T)] = h[s];
-  }
   double2 v[R];
   double2* bufs[2] = {c1, c2};
-  for (int b = 0; b < 2; ++b) {
+  if (a.phys_uv) {
+    // u + i v and the packed q at x, stored by the forward evaluation's pass B; a + i b
+    // (zero beyond column kxlim) is the only row to transform
+    const double2* uvrow = a.phys_uv + (size_t)y * N;
+    const double2* pqrow = a.phys_q + (size_t)y * M;
 #pragma unroll
-    for (int s = 0; s < R; ++s) v[s] = bufs[b][padix(t + s * T)];
-    __syncthreads();
-    fft_regs<N, R, true, 1>(v, bufs[b], t, a.tw, 0);
+    for (int s = 0; s < R; ++s) c1[padix(t + s * T)] = uvrow[t + s * T];
+#pragma unroll
+    for (int s = 0; s < R / 2; ++s) zs[padix(t + s * T)] = pqrow[t + s * T];
+    pair_spectrum<N, R>(c2, a.a + ro, a.b + ro, t, a.kxlim);  // a + i b
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < R; ++s) bufs[b][padix(t + s * T)] = v[s];
+    for (int s = 0; s < R; ++s) v[s] = c2[padix(t + s * T)];
+    __syncthreads();
+    fft_regs<N, R, true, 1>(v, c2, t, a.tw, 0);
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < R; ++s) c2[padix(t + s * T)] = v[s];
+  } else {
+    pair_spectrum<N, R>(c1, a.u + ro, a.v + ro, t);  // u + i v
+    pair_spectrum<N, R>(c2, a.a + ro, a.b + ro, t);  // a + i b
+    const double2* qrow = a.q + ro;
+#pragma unroll
+    for (int s = 0; s < R / 2; ++s) {  // half-length C2R packing of q
+      const int k = t + s * T;
+      double2 p = qrow[k], b = qrow[M - k];
+      if (k == 0) { p.y = 0.0; b.y = 0.0; }
+      const double2 sm_ = make_double2(p.x + b.x, p.y - b.y);
+      const double2 d = make_double2(p.x - b.x, p.y + b.y);
+      const double2 tt = twmul<true>(d, __ldg(&a.tw[k]));
+      zs[padix(k)] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
+    }
+    __syncthreads();
+    {
+      double2 h[R / 2];
+#pragma unroll
+      for (int s = 0; s < R / 2; ++s) h[s] = zs[padix(t + s * T)];
+      __syncthreads();
+      fft_regs<M, R / 2, true, 1>(h, zs, t, a.tw, 1);
+      __syncthreads();
+#pragma unroll
+      for (int s = 0; s < R / 2; ++s) zs[padix(t + s * T)] = h[s];
+    }
+    for (int b = 0; b < 2; ++b) {
+#pragma unroll
+      for (int s = 0; s < R; ++s) v[s] = bufs[b][padix(t + s * T)];
+      __syncthreads();
+      fft_regs<N, R, true, 1>(v, bufs[b], t, a.tw, 0);
+      __syncthreads();
+#pragma unroll
+      for (int s = 0; s < R; ++s) bufs[b][padix(t + s * T)] = v[s];
+    }
   }
   __syncthreads();
   // s1 = u a + v b (into zs, as packed pairs), s2 + i s3 = q (a + i b) (into c2); a, b / N^2

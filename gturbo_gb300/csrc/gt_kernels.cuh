@@ -156,6 +156,11 @@ struct NltArgs {
   int kxlim, kin, kout, truncate;
   int* flag;             // untruncated-input flag of this field
   EpiArgs epi;
+  // Optional (null: not written): pass B stores the physical fields of this evaluation, row y
+  // at phys_uv[y*N + x] = u + i v and phys_q[y*N/2 + m] = q[2m] + i q[2m+1]. The adjoint's
+  // backward sweep keeps them from the recomputed forward stages instead of transforming again.
+  double2* phys_uv;
+  double2* phys_q;
 };
 
 // Pass A: inverse y-transforms of u, v and q (in that order: zin may alias q, as the
@@ -277,6 +282,10 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
     __syncthreads();
 #pragma unroll
     for (int s = 0; s < R / 2; ++s) zs[padix(t + s * T)] = h[s];
+    if (a.phys_q) {
+#pragma unroll
+      for (int s = 0; s < R / 2; ++s) a.phys_q[(size_t)y * M + t + s * T] = h[s];
+    }
   }
   // u + i v: inverse length-N transform
   double2 v[R];
@@ -285,6 +294,10 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
   __syncthreads();
   fft_regs<N, R, true, 1>(v, cs, t, a.tw, 0);
   __syncthreads();
+  if (a.phys_uv) {
+#pragma unroll
+    for (int s = 0; s < R; ++s) a.phys_uv[(size_t)y * N + t + s * T] = v[s];
+  }
   // p = (u + i v) q  (produ.f90:18-19); q[2m] = Re z[m], q[2m+1] = Im z[m]
 #pragma unroll
   for (int s = 0; s < R; ++s) {

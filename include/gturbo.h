@@ -195,7 +195,9 @@ int gt_adj_step_rk2(gt_handle* h, const double* z, const double* w, double* lam,
  * gt_adj_step_rk2 back over it. Outputs: J and *grad_famp (host), grad_z0 and
  * zT (device; zT may be NULL), times_ms[2] = forward / backward sweep times
  * (may be NULL). Allocates ceil(nsteps/K) + 2K + 8 fields with cudaMalloc for
- * the duration of the call. Synchronous. */
+ * the duration of the call, and, when the memory is there, the physical u+iv and
+ * q of the 2K recomputed stages of a segment (24 N^2 bytes each), which spare the
+ * adjoint passes three of their transforms. Synchronous. */
 int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed, int32_t K,
                     double kmin, double kmax, double* J, double* grad_z0, double* grad_famp,
                     double* zT, double* times_ms);

@@ -141,3 +141,38 @@ def test_adjoint_in_every_launch_variant(n):
         assert J == pytest.approx(J0, rel=1e-12)
         assert float((gz - g0).norm() / g0.norm()) < 1e-12
         assert gf == pytest.approx(f0, rel=1e-11)
+
+
+@pytest.mark.parametrize("n,variant", [(128, 0), (128, 2), (256, 1)])
+def test_gradient_driver_matches_step_by_step_adjoint(n, variant):
+    """gt_adj_gradient (whose adjoint passes read the physical fields that the recomputed
+    forward stages kept) against a step-by-step backward sweep through gt_adj_step_rk2 (whose
+    passes transform the linearisation points themselves)."""
+    import ctypes
+    from gturbo_gb300.adjoint import gradient, objective
+    p, sol, z0, ns = _setup(n=n, nsteps=7)
+    sol.variant = variant
+    J, gz, gf, zT, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=3)
+    # forward: states z_s, stage states w_s, LCG states
+    work = sol.work(6)
+    P = ctypes.c_void_p
+    wk = (P * 6)(*[w.data_ptr() for w in work])
+    zs, ws, seeds = [], [], []
+    z, sd = z0.clone(), SEED
+    for _ in range(ns):
+        w = sol.field()
+        sol._check(sol.lib.gt_adj_stage(sol.h, sol._ptr(z), sol._ptr(w), wk))
+        zs.append(z.clone())
+        ws.append(w)
+        seeds.append(sd)
+        sol.step(z, *work[:3])
+        sd = sol.forcing(z, sd)
+    J2, lam = objective(sol, z, KMIN, KMAX, grad=True)
+    assert J2 == pytest.approx(J, rel=1e-14)
+    gfamp = ctypes.c_double(0.0)
+    for st in reversed(range(ns)):
+        sol._check(sol.lib.gt_adj_step_rk2(sol.h, sol._ptr(zs[st]), sol._ptr(ws[st]), sol._ptr(lam),
+                                           int(seeds[st]), ctypes.byref(gfamp), wk))
+    torch.cuda.synchronize()
+    assert float((gz - lam).norm() / lam.norm()) < 1e-13
+    assert gf == pytest.approx(gfamp.value, rel=1e-12)
