@@ -401,3 +401,25 @@ def test_autotune_and_cache(tmp_path):
     z = _dev(a)
     sol2.rk_step(z, sol2.work())
     assert rel_l2(_host(z), ref) < TOL
+
+
+def test_host_pipeline_matches_serial_loop():
+    """HostPipeline (copies on their own streams, two device buffers) gives the results of the
+    plain upload -> step -> download loop, bit for bit."""
+    from gturbo_gb300.pipeline import HostPipeline
+    p = _params(256, rko=4, dt=2e-3)
+    sol = _solver(p)
+    orc = Oracle(p)
+    inputs = [torch.from_numpy(rand_field(orc, 30 + k) * 30.0).pin_memory() for k in range(3)]
+    outs = [torch.empty_like(inputs[0]).pin_memory() for _ in range(5)]
+    work = sol.work()
+    pipe = HostPipeline(sol)
+    seed_p = pipe.run(inputs, outs, 5, 481929, work, diag_every=2)
+    pipe.sync()
+    seed = 481929
+    for k in range(5):
+        z = inputs[k % 3].cuda()
+        seed, _ = sol.main_step(z, seed, work, diag=(k + 1) % 2 == 0)
+        torch.cuda.synchronize()
+        assert torch.equal(z.cpu(), outs[k]), k
+    assert seed == seed_p
