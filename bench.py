@@ -148,6 +148,32 @@ def cpu_oracle_run(p, k0, steps, budget_s, threads=None):
                       f"C oracle with OpenMP"}
 
 
+def numpy_run(p, k0, budget_s):
+    """Main-loop steps/s of the single-threaded numpy restatement (pocketfft) within ~budget_s."""
+    import numpy as np
+
+    from gturbo_gb300.ic import random_phase_ic
+    from oracle.np_oracle import NpOracle, from_phys_layout
+
+    orc = NpOracle(p)
+    zk = from_phys_layout(random_phase_ic(p, k0, 0.5, seed=1))
+    seed = SEED
+    t0 = time.perf_counter()
+    zk = orc.rk_step(zk)
+    zk, seed = orc.forcing(zk, seed)
+    t1 = time.perf_counter() - t0
+    k = max(1, int(budget_s / max(t1, 1e-6)))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        zk = orc.rk_step(zk)
+        zk, seed = orc.forcing(zk, seed)
+    dt = time.perf_counter() - t0
+    assert np.isfinite(zk).all()
+    return {"value": k / dt, "unit": "steps/s", "cores": 1, "steps": k,
+            "sample": f"{k} steps (RK{p.rko} + forcing, no diagnostics) of the {p.n}^2 workload, "
+                      "numpy restatement, pocketfft"}
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -385,6 +411,15 @@ def ours_arm(args):
                 extras["cpu_baseline"] = cpu_oracle_run(p, k0, 10 ** 6, args.cpu_seconds)
             except Exception as e:
                 extras["cpu_baseline"] = {"unavailable": str(e)[:200]}
+            # ---- numpy, one thread, at 256^2 (c1) and at the bench's own size --------
+            try:
+                from gturbo_gb300.params import IC_K0, config
+                np1 = {"c1": numpy_run(config("c1"), IC_K0["c1"], 3.0)}
+                if args.config != "c1":
+                    np1[args.config] = numpy_run(p, k0, 5.0)
+                extras["cpu_baseline"]["numpy_1thread"] = np1
+            except Exception as e:
+                extras["cpu_baseline"]["numpy_1thread"] = {"unavailable": str(e)[:200]}
         if "e2e" not in extras:
             extras["e2e"] = {"value": None, "unit": "steps/s", "h2d_bytes_per_step": 0,
                              "d2h_bytes_per_step": 0, "note": "skipped (--no-extras)"}

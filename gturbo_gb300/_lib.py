@@ -60,6 +60,7 @@ def load(path: str | None = None):
         "gt_fft_inv": ([P, D], ctypes.c_int),
         "gt_trunc": ([P, D], ctypes.c_int),
         "gt_dump_real4": ([P, D, D], ctypes.c_int),
+        "gt_load_real4": ([P, D, D], ctypes.c_int),
         "gt_produ": ([P, D, D, D], ctypes.c_int),
         "gt_nlt": ([P, D, D, D], ctypes.c_int),
         "gt_step_rk2": ([P, D, D, D, D], ctypes.c_int),

@@ -554,6 +554,44 @@ k_row_c2r_f32(const double* __restrict__ z, float* __restrict__ out, const doubl
   for (int s = 0; s < 8; ++s) orow[t + s * T] = make_float2((float)h[s].x, (float)h[s].y);
 }
 
+// Row R2C of a real(4) record (src/read.f90:3-27 widens it to real(8) with zero padding; the
+// row transform of fft_dir follows): in[y*N + x] float -> z row y, NH complex values.
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::ROW_THREADS)
+k_row_r2c_f32(const float* __restrict__ in, double* __restrict__ z, const double2* __restrict__ tw) {
+  using S = Shape<N>;
+  constexpr int T = S::T, NH = S::NH, M = N / 2;
+  extern __shared__ double2 smem[];
+  const int r = threadIdx.x / T, t = threadIdx.x % T;
+  const int y = blockIdx.x * S::ROWS + r;
+  double2* zs = smem + (size_t)r * padded(M);
+  const float2* irow = reinterpret_cast<const float2*>(in) + (size_t)y * M;
+  double2* row = reinterpret_cast<double2*>(z) + (size_t)y * NH;
+  double2 h[8];
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {  // z[m] = x[2m] + i x[2m+1], widened exactly
+    const float2 w = irow[t + s * T];
+    h[s] = make_double2((double)w.x, (double)w.y);
+  }
+  fft_regs<M, 8, false, 1>(h, zs, t, tw, 1);
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < 8; ++s) zs[padix(t + s * T)] = h[s];
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s <= 8; ++s) {
+    const int k = t + s * T;
+    if (k <= M) {
+      const double2 a = zs[padix(k & (M - 1))];
+      const double2 b = zs[padix((M - k) & (M - 1))];
+      const double2 sm_ = make_double2(a.x + b.x, a.y - b.y);
+      const double2 d = make_double2(a.x - b.x, a.y + b.y);
+      const double2 tt = twmul<false>(d, __ldg(&tw[k]));
+      row[k] = make_double2(0.5 * (sm_.x + tt.y), 0.5 * (sm_.y - tt.x));
+    }
+  }
+}
+
 // Row R2C in place (N real -> NH complex), half-length packing.
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::ROW_THREADS)

@@ -26,6 +26,7 @@ enum OpKind : int {
   OP_ADJ_COLFWD = 12,
   OP_NLT_COLFWD_INV = 13,  // pass C of stage nlt + pass A of stage nlt2
   OP_ROW_C2R_F32 = 14,     // row C2R of `a` written as floats to `f32` (dumps)
+  OP_ROW_R2C_F32 = 15,     // row R2C of the floats `f32` into `a` (restarts)
 };
 
 struct GtOp {

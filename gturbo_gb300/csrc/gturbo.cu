@@ -582,6 +582,21 @@ int gt_dump_real4(gt_handle* h, double* work, float* out) {
   return run(h, op);
 }
 
+int gt_load_real4(gt_handle* h, const float* in, double* z) {
+  if (!h || !in || !z) return fail(h, GT_ERR_ARG, "gt_load_real4: null argument");
+  GtOp op = base_op(h);
+  op.a = reinterpret_cast<double2*>(z);
+  op.f32 = const_cast<float*>(in);
+  op.kind = gt::OP_ROW_R2C_F32;
+  int rc = run(h, op);
+  if (rc) return rc;
+  op.kind = gt::OP_COL_FWD;
+  op.scale = 1.0 / ((double)h->N * (double)h->N);
+  rc = run(h, op);
+  if (rc || !h->truncate) return rc;
+  return gt_trunc(h, z);
+}
+
 int gt_trunc(gt_handle* h, double* z) {
   if (!h || !z) return fail(h, GT_ERR_ARG, "gt_trunc: null argument");
   gt::k_trunc<<<4 * 152, 256, 0, h->stream>>>(reinterpret_cast<double2*>(z), h->N, h->NH, h->d_kcut);

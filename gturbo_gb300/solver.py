@@ -199,6 +199,22 @@ class Solver:
             host = out.cpu()
         return host.numpy()
 
+    def load_real4(self, w, z: torch.Tensor | None = None) -> torch.Tensor:
+        """Restart from a real(4) dump (src/read.f90:3-27 + src/main.f90:89-92): the N x N
+        float32 physical field w (numpy or tensor, x fastest) -> spectral field z, fft_dir'ed
+        and truncated on the device (gt_load_real4). Returns z."""
+        with torch.cuda.stream(self.stream):
+            wd = torch.as_tensor(np.ascontiguousarray(w, np.float32) if isinstance(w, np.ndarray) else w)
+            wd = wd.to(self.device, torch.float32).contiguous()
+            if wd.shape != (self.n, self.n):
+                raise ValueError(f"dump must be {self.n} x {self.n} float32")
+            if z is None:
+                z = self.field()
+        # wd was allocated on the solver's stream: its memory is not reused before the
+        # kernels enqueued here have read it
+        self._check(self.lib.gt_load_real4(self.h, wd.data_ptr(), self._ptr(z)))
+        return z
+
     def trunc(self, z: torch.Tensor) -> None:
         self._check(self.lib.gt_trunc(self.h, self._ptr(z)))
 

@@ -105,6 +105,12 @@ int gt_fft_inv(gt_handle* h, double* z);
  * normally a copy of z as the reference's znl = z) written to the DEVICE array
  * `out` as N*N real(4) values, x fastest: the record of fields/w.NNN.MMM. */
 int gt_dump_real4(gt_handle* h, double* work, float* out);
+/* Restart from a field dump (src/read.f90:3-27 readf, then src/main.f90:89-92):
+ * the N*N real(4) physical values `in` (DEVICE array, x fastest: the record of
+ * fields/w.NNN) are widened to real(8) with zero padding, transformed as
+ * gt_fft_dir into the spectral field z, and truncated as gt_trunc when the
+ * handle's truncate = 1. */
+int gt_load_real4(gt_handle* h, const float* in, double* z);
 /* 2/3-rule ellipse mask and zero mean, in place (src/trunc.f90:10-25). */
 int gt_trunc(gt_handle* h, double* z);
 /* Physical-space products u <- z*u, v <- z*v, padding zeroed (src/produ.f90:11-23). */

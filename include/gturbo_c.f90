@@ -64,6 +64,13 @@ module gturbo_c
       real(c_double) :: work(*)
       real(c_float) :: out(*)
     end function
+    ! restart: readf (src/read.f90:3-27) + fft_dir + trunc (src/main.f90:89-92); in: N*N real(4), DEVICE
+    integer(c_int) function gt_load_real4(h, w, z) bind(C, name="gt_load_real4")
+      import :: c_int, c_ptr, c_double, c_float
+      type(c_ptr), value :: h
+      real(c_float) :: w(*)
+      real(c_double) :: z(*)
+    end function
     ! trunc, produ, nlt (src/trunc.f90, src/produ.f90, src/nlt.f90)
     integer(c_int) function gt_trunc(h, z) bind(C, name="gt_trunc")
       import :: c_int, c_ptr, c_double

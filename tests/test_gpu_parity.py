@@ -84,6 +84,35 @@ def test_dump_real4(n, tmp_path):
     assert np.array_equal(read_field(str(f), n)[:, :n], w.astype(np.float64))
 
 
+@pytest.mark.parametrize("n,truncate", [(64, 1), (512, 1), (256, 0), (2048, 1)])
+def test_load_real4_restart(n, truncate):
+    """Restart from a real(4) record: readf's widening + fft_dir + trunc (src/read.f90:3-27,
+    src/main.f90:89-92) against the oracle, and the dump -> restart round trip."""
+    p = _params(n, truncate=truncate)
+    orc, sol = Oracle(p), _solver(p)
+    rng = np.random.default_rng(40 + n)
+    w = rng.standard_normal((n, n)).astype(np.float32)
+    ref = np.zeros((n, n + 2))
+    ref[:, :n] = w.astype(np.float64)
+    orc.fft_dir(ref)
+    if truncate:
+        orc.trunc(ref)
+    z = sol.load_real4(w)
+    assert rel_l2(_host(z), ref) < TOL
+    # round trip: a truncated field, dumped as real(4) and restarted, within float rounding
+    a = rand_field(orc, 41)
+    w2 = sol.dump_real4(_dev(a))
+    z2 = sol.load_real4(w2)
+    back = _host(z2)
+    assert rel_l2(back, a) < 1e-6
+    ref2 = np.zeros((n, n + 2))
+    ref2[:, :n] = w2.astype(np.float64)
+    orc.fft_dir(ref2)
+    if truncate:
+        orc.trunc(ref2)
+    assert rel_l2(back, ref2) < TOL
+
+
 @pytest.mark.parametrize("n", [16, 64, 256, 1024])
 def test_trunc_exact(n):
     p = _params(n)
