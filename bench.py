@@ -246,6 +246,23 @@ def pass_model(p, kind):
     return None, None
 
 
+# DRAM bytes (read + write) per launch of a pass, from single-kernel ncu captures
+# (dram__bytes_read.sum + dram__bytes_write.sum) of the same launch variant:
+#   2048^2, variant 0: ncu --set full -k "regex:k_nlt_(row|colfwd_inv|colinv)" -s 52 -c 3
+#                      python bench.py --steps 2 --warmup 3 --no-extras
+#   256^2, variant 2:  ncu --set full --kernel-name-base demangled
+#                      -k "regex:k_nltv_(row|colfwd_inv|colinv)<\(int\)256, \(int\)2>" -s 8 -c 3
+#                      python bench.py --config c1 --steps 2 --warmup 3 --no-extras --variant 2
+NCU_TRAFFIC = {
+    (2048, 0, "nlt_colinv"): 47.07e6 + 18.51e6,
+    (2048, 0, "nlt_row"): 67.99e6 + 1.53e6,
+    (2048, 0, "nlt_colfwd_inv"): 110.95e6 + 41.28e6,
+    (256, 2, "nlt_colinv"): 0.774e6,
+    (256, 2, "nlt_row"): 1.177e6,
+    (256, 2, "nlt_colfwd_inv"): 1.854e6,
+}
+
+
 def ours_arm(args):
     import numpy as np
     import torch
@@ -337,7 +354,9 @@ def ours_arm(args):
                 "achieved": fl / (ms / 1e3) / 1e12 if fl else None, "unit": "TFLOP/s",
                 "peak": fp64, "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
                 "(FP64 pipe; MEASURED_PEAKS.json has no FP64 figure)",
-                "traffic": None,
+                "traffic": NCU_TRAFFIC.get((p.n, sol.variant, top)),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch "
+                                  "(capture of the same kernel and launch variant)",
                 "hbm_achieved_gbs": by / (ms / 1e3) / 1e9 if by else None,
                 "hbm_peak_gbs": peaks.get("hbm_gbs"), "hbm_peak_source": src}
         roof["frac"] = roof["achieved"] / fp64 if roof["achieved"] else None
