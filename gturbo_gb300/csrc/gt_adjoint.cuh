@@ -554,7 +554,7 @@ struct AdjVar {
   using W = Var<N, V>;
   static constexpr size_t TLM_ROW_SMEM = (size_t)3 * padded(N) * W::ROWS * sizeof(double2);
   static constexpr size_t ADJ_ROW_SMEM = (size_t)(2 * padded(N) + padded(N / 2)) * W::ROWS * sizeof(double2);
-  static constexpr bool OK = W::OK && AdjShape<N>::OK;
+  static constexpr bool OK = W::OK && !W::GROUPED && AdjShape<N>::OK;
 };
 
 template <int N, int V>

@@ -390,6 +390,116 @@ __device__ __forceinline__ void colfwd_colinv_tile(const NltArgs& cur, const Nlt
   colinv_tile<N, C, R>(next, tile);
 }
 
+// ---- grouped column tiles ------------------------------------------------------------------
+// One column per CTA, worked on by kColGroups thread groups of T = N/R threads. The independent
+// transforms of the column (u, v, q in pass A; A and B in pass C) run at the same time, one per
+// group, instead of one after another: for grids whose column passes leave most SMs idle, this
+// shortens the dependent chain of a CTA. Every group executes the same transform code, so every
+// thread meets the same sequence of block barriers; a group with nothing to transform (pass C)
+// transforms zeros.
+constexpr int kColGroups = 3;
+
+// Pass A, group g transforming field g (0: u, 1: v, 2: q). zin may alias q: every group loads
+// its column before the barrier that precedes the stores.
+template <int N, int R>
+__device__ __forceinline__ void colinv_grp_tile(const NltArgs& a, int tile) {
+  constexpr int T = N / R, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  const int g = threadIdx.x / T, t = threadIdx.x % T;
+  const int i = tile;  // one column per CTA, i < NH
+  double2* sm = smem + (size_t)g * padded(N);
+  const double2* zin = a.zin;
+  double2 v[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = zin[(size_t)(t + s * T) * NH + i];
+  // a column beyond the 2/3 ellipse carries data only for an untruncated input (see colinv_tile)
+  int nz = 0;
+  if (i > a.kxlim) {
+#pragma unroll
+    for (int s = 0; s < R; ++s) nz |= (v[s].x != 0.0) | (v[s].y != 0.0);
+  }
+  const bool skip = (i > a.kxlim) ? !__syncthreads_or(nz) : false;
+  if (skip) return;
+  if (nz) atomicExch(a.flag, 1);
+  if (g == 0) {  // u = i ky/|k|^a q  (nlt.f90:29-32)
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int j = t + s * T;
+      const double m = __ldg(&a.fky[j]) * __ldg(&a.kainv[(size_t)j * NH + i]);
+      v[s] = make_double2(-m * v[s].y, m * v[s].x);
+    }
+  } else if (g == 1) {  // v = -i kx/|k|^a q  (nlt.f90:33-34)
+    const double kx = __ldg(&a.fkx[i]);
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int j = t + s * T;
+      const double m = kx * __ldg(&a.kainv[(size_t)j * NH + i]);
+      v[s] = make_double2(m * v[s].y, -m * v[s].x);
+    }
+  }
+  fft_regs<N, R, true, 1>(v, sm, t, a.tw, 0);
+  __syncthreads();  // every load of zin is done before q (which may alias it) is written
+  double2* dst = g == 0 ? a.u : g == 1 ? a.v : a.q;
+#pragma unroll
+  for (int s = 0; s < R; ++s) dst[(size_t)(t + s * T) * NH + i] = v[s];
+}
+
+// Pass C: group 0 transforms A, group 1 transforms B, group 2 zeros; group 0 hands kx*FA to
+// group 1 through its exchange buffer (free once fft_regs has returned), and group 1 forms N
+// and runs the epilogue.
+template <int N, int R>
+__device__ __forceinline__ void colfwd_grp_tile(const NltArgs& a, int tile) {
+  constexpr int T = N / R, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  if (tile == 0 && threadIdx.x == 0) *a.flag = 0;  // pass B of this nlt is complete
+  const int g = threadIdx.x / T, t = threadIdx.x % T;
+  const int i = tile;
+  if (i > a.kxlim) {
+    // no retained mode in this column: N = 0
+    if (g == 0) {
+#pragma unroll
+      for (int s = 0; s < R; ++s) epilogue(a.epi, i, t + s * T, NH, czero());
+    }
+  } else {
+    double2* sm = smem + (size_t)g * padded(N);
+    const double scale = 0.5 / ((double)N * (double)N);
+    const double2* src = g == 0 ? a.u : a.v;
+    double2 v[R];
+#pragma unroll
+    for (int s = 0; s < R; ++s) v[s] = g < 2 ? src[(size_t)(t + s * T) * NH + i] : czero();
+    fft_regs<N, R, false, 1>(v, sm, t, a.tw, 0);
+    if (g == 0) {
+      const double kxs = __ldg(&a.fkx[i]) * scale;
+#pragma unroll
+      for (int s = 0; s < R; ++s) sm[padix(t + s * T)] = make_double2(kxs * v[s].x, kxs * v[s].y);
+    }
+    __syncthreads();
+    if (g == 1) {
+      const double2* fa = smem;  // group 0's buffer
+      const int kc = a.truncate ? __ldg(&a.kcut[i]) : N;
+#pragma unroll
+      for (int s = 0; s < R; ++s) {
+        const int j = t + s * T;
+        const double kys = __ldg(&a.fky[j]) * scale;
+        const double2 f = fa[padix(j)];
+        // N = -i (kx A + ky B): re = kx Im A + ky Im B, im = -(kx Re A + ky Re B)
+        double2 nh = make_double2(fma(kys, v[s].y, f.y), -fma(kys, v[s].x, f.x));
+        const int aj = min(j, N - j);
+        if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
+        epilogue(a.epi, i, j, NH, nh);
+      }
+    }
+  }
+}
+
+// Pass C of one stage and pass A of the next on the same column (see colfwd_colinv_tile).
+template <int N, int R>
+__device__ __forceinline__ void colfwd_colinv_grp_tile(const NltArgs& cur, const NltArgs& next, int tile) {
+  colfwd_grp_tile<N, R>(cur, tile);
+  __syncthreads();
+  colinv_grp_tile<N, R>(next, tile);
+}
+
 // ---- single-field kernels ---------------------------------------------------------------
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
@@ -419,26 +529,30 @@ k_nlt_colfwd_inv(NltArgs cur, NltArgs next) {
 // V = 0: R = 16 values per thread, Shape<N>'s tiles (best from ~1024^2 up);
 // V = 1: R = 8,  one column / row per CTA;
 // V = 2: R = 4,  one column / row per CTA (small grids: 4x the threads of V = 0, for the
-//        latency-bound regime where a pass leaves most SMs idle).
+//        latency-bound regime where a pass leaves most SMs idle);
+// V = 3: R = 4,  grouped column tiles (the column's transforms side by side), rows as V = 2;
+// V = 4: R = 8,  grouped column tiles, rows as V = 1.
 template <int N, int V>
 struct Var {
-  static constexpr int R = V == 0 ? 16 : V == 1 ? 8 : 4;
+  static constexpr bool GROUPED = V >= 3;
+  static constexpr int R = V == 0 ? 16 : (V == 1 || V == 4) ? 8 : 4;
   static constexpr int T = N / R;
   static constexpr int NH = N / 2 + 1;
   static constexpr int COLS = V == 0 ? Shape<N>::COLS : 1;
   static constexpr int ROWS = V == 0 ? Shape<N>::ROWS : 1;
-  static constexpr int COL_THREADS = COLS * T;
+  static constexpr int COL_THREADS = (GROUPED ? kColGroups : COLS) * T;
   static constexpr int ROW_THREADS = ROWS * T;
   static constexpr int COL_CTAS = (NH + COLS - 1) / COLS;
   static constexpr int ROW_CTAS = N / ROWS;
-  static constexpr size_t COL_SMEM = (size_t)padded(N) * COLS * sizeof(double2);
+  static constexpr size_t COL_SMEM = (size_t)padded(N) * (GROUPED ? kColGroups : COLS) * sizeof(double2);
   static constexpr size_t ROW_SMEM = (size_t)(padded(N) + padded(N / 2)) * ROWS * sizeof(double2);
-  static constexpr bool OK = V == 0 || (V == 1 && N <= 4096) || (V == 2 && N <= 1024);
+  static constexpr bool OK = V == 0 || (V == 1 && N <= 4096) || (V >= 2 && V <= 4 && N <= 1024);
 };
 
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colinv(NltArgs a) {
-  if constexpr (Var<N, V>::OK) colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
+  if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colinv_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
+  else if constexpr (Var<N, V>::OK) colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_nltv_row(NltArgs a) {
@@ -446,11 +560,15 @@ __global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_nltv_row(NltArgs a) 
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd(NltArgs a) {
-  if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
+  if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colfwd_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
+  else if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltArgs cur, NltArgs next) {
-  if constexpr (Var<N, V>::OK) colfwd_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(cur, next, blockIdx.x);
+  if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED)
+    colfwd_colinv_grp_tile<N, Var<N, V>::R>(cur, next, blockIdx.x);
+  else if constexpr (Var<N, V>::OK)
+    colfwd_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(cur, next, blockIdx.x);
 }
 
 // ---- ensemble kernels: one launch per pass for every member ------------------------------

@@ -338,8 +338,9 @@ int gt_create(const gt_params* p, gt_handle** out) {
   h->NBIN = N / 2;
   h->dispatch = dispatch_for(N);
   // The launch variant that timed fastest on GB300 for this grid size (RK2 and RK4 alike):
-  // 4 values per thread up to 512^2, 8 at 1024^2, 16 from 2048^2 up. gt_autotune re-times.
-  h->variant = N <= 512 ? 2 : N == 1024 ? 1 : 0;
+  // grouped columns with 4 values per thread up to 256^2, 4 values per thread at 512^2, 8 at
+  // 1024^2 and 4096^2, 16 at 2048^2 and 8192^2. gt_autotune re-times.
+  h->variant = N <= 256 ? 3 : N == 512 ? 2 : (N == 1024 || N == 4096) ? 1 : 0;
   // inieuler.f90:22-36, 237-244
   int split = 0;
   if (p->alpnu < 1.0005 && p->alpnu > 0.9995 && p->alpmu < 0.0005 && p->alpmu > -0.0005) split = 1;
@@ -781,7 +782,9 @@ int gt_variant_supported(int32_t n, int32_t variant) {
   switch (variant) {
     case 0: return 1;
     case 1: return n <= 4096;
-    case 2: return n <= 1024;
+    case 2:
+    case 3:
+    case 4: return n <= 1024;
     default: return 0;
   }
 }

@@ -273,9 +273,11 @@ int gt_profile_read(gt_handle* h, double* ms, int64_t* launches);
  * term come in GT_NVARIANTS launch shapes: 0 = 16 values per thread, several columns/rows per
  * block (large grids); 1 = 8 values per thread, one column/row per block (n <= 4096);
  * 2 = 4 values per thread, one column/row per block (n <= 1024, for small latency-bound
- * grids). The variants differ only in the radix decomposition of the transforms, so their
- * results agree to rounding (relative differences of order 1e-15 per step). */
-#define GT_NVARIANTS 3
+ * grids); 3 and 4 = 4 and 8 values per thread with the independent transforms of a column
+ * (u, v, q; A, B) run side by side by three thread groups of the block (n <= 1024). The
+ * variants differ only in the radix decomposition of the transforms, so their results agree
+ * to rounding (relative differences of order 1e-15 per step). */
+#define GT_NVARIANTS 5
 /* 1 if launch variant `variant` exists for grid size n, else 0 (host only, no GPU needed). */
 int gt_variant_supported(int32_t n, int32_t variant);
 /* Select the variant used by every later nlt / step call of h (GT_ERR_ARG if unsupported). */

@@ -114,11 +114,11 @@ def test_null_arguments_are_errors_not_crashes(lib):
 
 
 def test_variant_table(lib):
-    """Launch variants by grid size: 0 always, 1 up to 4096, 2 up to 1024 (host only)."""
+    """Launch variants by grid size: 0 always, 1 up to 4096, 2-4 up to 1024 (host only)."""
     for n in (16, 64, 1024, 2048, 4096, 8192):
-        got = [lib.gt_variant_supported(n, v) for v in range(3)]
-        assert got == [1, int(n <= 4096), int(n <= 1024)], n
-    assert lib.gt_variant_supported(100, 0) == 0 and lib.gt_variant_supported(64, 3) == 0
+        got = [lib.gt_variant_supported(n, v) for v in range(5)]
+        assert got == [1, int(n <= 4096)] + [int(n <= 1024)] * 3, n
+    assert lib.gt_variant_supported(100, 0) == 0 and lib.gt_variant_supported(64, 5) == 0
     assert lib.gt_set_variant(None, 0) == 1 and lib.gt_autotune(None, 1, None, None) == 1
 
 
