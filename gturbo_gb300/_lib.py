@@ -95,6 +95,9 @@ def load(path: str | None = None):
         "gt_set_variant": ([P, ctypes.c_int32], ctypes.c_int),
         "gt_get_variant": ([P, I32P], ctypes.c_int),
         "gt_autotune": ([P, ctypes.c_int32, H, I32P], ctypes.c_int),
+        "gt_row_variant_supported": ([ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+        "gt_set_variants": ([P, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+        "gt_get_variants": ([P, I32P, I32P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

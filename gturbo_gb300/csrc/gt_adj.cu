@@ -132,6 +132,7 @@ gt::GtOp op_of(const gt_handle* h, int kind) {
   std::memset(&op, 0, sizeof(op));
   op.kind = kind;
   op.variant = gt::handle_variant(h);
+  op.row_variant = gt::handle_row_variant(h);
   op.stream = gt::handle_stream(h);
   return op;
 }

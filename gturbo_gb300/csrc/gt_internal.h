@@ -42,8 +42,9 @@ int* handle_flag(const gt_handle* h);
 // Grid size, RK order and the parameters a handle was created with.
 const gt_params* handle_params(const gt_handle* h);
 int handle_rko(const gt_handle* h);
-// Launch variant of the nonlinear-term (and tangent-linear / adjoint) passes.
+// Launch variants of the column and row passes (nonlinear term, tangent-linear, adjoint).
 int handle_variant(const gt_handle* h);
+int handle_row_variant(const gt_handle* h);
 // Records msg as h's last error (h == NULL: the thread's create/no-handle error); returns code.
 int set_error(gt_handle* h, int code, const char* msg);
 

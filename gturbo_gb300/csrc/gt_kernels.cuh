@@ -13,8 +13,9 @@
 //      fft_dir.f90:17-21), the 2/3 mask (trunc.f90:10-25) and the Runge-Kutta stage update
 //      of rkstep.f90 fused into the store.
 // With truncate=1 the columns kx > kxlim hold no retained mode: pass C writes N=0 there
-// without transforming, and pass A skips any such column block whose input is entirely zero;
-// a device flag tells pass B whether the skipped columns are known to be zero.
+// without transforming, and pass A stores zeros without transforming for any such column
+// block whose input is entirely zero. A device flag tells pass B whether any column beyond
+// kxlim carried data (an untruncated input); only then does pass B read those columns.
 #pragma once
 
 #include "gt_fft.cuh"
@@ -180,14 +181,26 @@ __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
   for (int s = 0; s < R; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
   // A column beyond the 2/3 ellipse (i > kxlim) carries data only if the caller passed an
   // untruncated field: then raise the flag so that pass B reads every column. A tile made
-  // only of such columns is skipped when all of them are zero.
+  // only of such columns needs no transform when all of them are zero: it stores zeros, which
+  // pass B reads if another tile raised the flag.
   int nz = 0;
   if (valid && i > a.kxlim) {
 #pragma unroll
     for (int s = 0; s < R; ++s) nz |= (v[s].x != 0.0) | (v[s].y != 0.0);
   }
   const bool skip = (tile * C > a.kxlim) ? !__syncthreads_or(nz) : false;
-  if (skip) return;
+  if (skip) {
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < R; ++s) {
+        const size_t o = (size_t)(t + s * T) * NH + i;
+        a.u[o] = czero();
+        a.v[o] = czero();
+        a.q[o] = czero();
+      }
+    }
+    return;
+  }
   if (nz) atomicExch(a.flag, 1);
   const double kx = __ldg(&a.fkx[ic]);
   // u = i ky/|k|^a q  (nlt.f90:29-32)
@@ -412,14 +425,20 @@ __device__ __forceinline__ void colinv_grp_tile(const NltArgs& a, int tile) {
   double2 v[R];
 #pragma unroll
   for (int s = 0; s < R; ++s) v[s] = zin[(size_t)(t + s * T) * NH + i];
-  // a column beyond the 2/3 ellipse carries data only for an untruncated input (see colinv_tile)
+  // a column beyond the 2/3 ellipse carries data only for an untruncated input; an all-zero
+  // one stores zeros without a transform (see colinv_tile)
   int nz = 0;
   if (i > a.kxlim) {
 #pragma unroll
     for (int s = 0; s < R; ++s) nz |= (v[s].x != 0.0) | (v[s].y != 0.0);
   }
   const bool skip = (i > a.kxlim) ? !__syncthreads_or(nz) : false;
-  if (skip) return;
+  if (skip) {
+    double2* dst = g == 0 ? a.u : g == 1 ? a.v : a.q;
+#pragma unroll
+    for (int s = 0; s < R; ++s) dst[(size_t)(t + s * T) * NH + i] = czero();
+    return;
+  }
   if (nz) atomicExch(a.flag, 1);
   if (g == 0) {  // u = i ky/|k|^a q  (nlt.f90:29-32)
 #pragma unroll

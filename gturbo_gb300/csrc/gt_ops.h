@@ -31,7 +31,8 @@ enum OpKind : int {
 
 struct GtOp {
   int kind;
-  int variant;        // launch variant of the nonlinear-term passes (Var<N, V>)
+  int variant;        // launch variant of the column passes (Var<N, V>, V in 0..4)
+  int row_variant;    // launch variant of the row passes (0, 1, 2: 16, 8, 4 values per thread)
   cudaStream_t stream;
   NltArgs nlt;        // passes A, B, C
   NltArgs nlt2;       // the next stage (OP_NLT_COLFWD_INV)

@@ -46,7 +46,8 @@ struct gt_handle {
   std::vector<uint32_t> lcga, lcgb;  // index k: coefficients of the (k+1)-th draw
   uint32_t lcga_nf = 1, lcgb_nf = 0;
   int device = 0;
-  int variant = 0;  // launch variant of the nonlinear-term passes
+  int variant = 0;      // launch variant of the column passes
+  int row_variant = 0;  // launch variant of the row passes
   cudaStream_t stream = nullptr;
   std::string err;
   // device tables
@@ -137,6 +138,7 @@ int* handle_flag(const gt_handle* h) { return h->d_flag; }
 const gt_params* handle_params(const gt_handle* h) { return &h->p; }
 int handle_rko(const gt_handle* h) { return h->rko; }
 int handle_variant(const gt_handle* h) { return h->variant; }
+int handle_row_variant(const gt_handle* h) { return h->row_variant; }
 cudaStream_t handle_stream(const gt_handle* h) { return h->stream; }
 
 }  // namespace gt
@@ -166,6 +168,9 @@ int cuda_fail(gt_handle* h, cudaError_t e, const char* what) {
   } while (0)
 
 bool pow2_in_range(int n) { return n >= 16 && n <= 8192 && (n & (n - 1)) == 0; }
+
+// The row variant with the register radix of column variant v (16, 8, 4 values per thread).
+int natural_row_variant(int v) { return v == 0 ? 0 : (v == 1 || v == 4) ? 1 : 2; }
 
 // exp(-2 pi i k / n) for k in [0, n), each value from an argument reduced to [0, pi/4].
 void make_twiddles(int n, std::vector<double2>& tw) {
@@ -252,6 +257,7 @@ GtOp base_op(const gt_handle* h) {
   std::memset(&op, 0, sizeof(op));
   op.stream = h->stream;
   op.variant = h->variant;
+  op.row_variant = h->row_variant;
   op.tw = h->d_tw;
   op.nlt = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, h->d_flag);
   return op;
@@ -337,10 +343,12 @@ int gt_create(const gt_params* p, gt_handle** out) {
   const int NH = h->NH = N / 2 + 1;
   h->NBIN = N / 2;
   h->dispatch = dispatch_for(N);
-  // The launch variant that timed fastest on GB300 for this grid size (RK2 and RK4 alike):
-  // grouped columns with 4 values per thread up to 256^2, 4 values per thread at 512^2, 8 at
-  // 1024^2 and 4096^2, 16 at 2048^2 and 8192^2. gt_autotune re-times.
+  // The launch variants that timed fastest on GB300 for this grid size (RK2 and RK4 alike).
+  // Columns: grouped with 4 values per thread up to 256^2, 4 values per thread at 512^2, 8 at
+  // 1024^2 and 4096^2, 16 at 2048^2 and 8192^2. Rows: 4 values per thread up to 256^2, 8 at
+  // 512^2 and 1024^2, 16 from 2048^2 up. gt_autotune re-times.
   h->variant = N <= 256 ? 3 : N == 512 ? 2 : (N == 1024 || N == 4096) ? 1 : 0;
+  h->row_variant = N <= 256 ? 2 : N <= 1024 ? 1 : 0;
   // inieuler.f90:22-36, 237-244
   int split = 0;
   if (p->alpnu < 1.0005 && p->alpnu > 0.9995 && p->alpmu < 0.0005 && p->alpmu > -0.0005) split = 1;
@@ -789,18 +797,38 @@ int gt_variant_supported(int32_t n, int32_t variant) {
   }
 }
 
+int gt_row_variant_supported(int32_t n, int32_t row_variant) {
+  return row_variant >= 0 && row_variant < GT_NROW_VARIANTS && gt_variant_supported(n, row_variant);
+}
+
+int gt_set_variants(gt_handle* h, int32_t col_variant, int32_t row_variant) {
+  if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_variants: null handle");
+  if (!gt_variant_supported(h->N, col_variant) || !gt_row_variant_supported(h->N, row_variant))
+    return fail(h, GT_ERR_ARG, "gt_set_variants: variants (" + std::to_string(col_variant) + ", " +
+                                   std::to_string(row_variant) + ") do not exist for n=" + std::to_string(h->N));
+  h->variant = col_variant;
+  h->row_variant = row_variant;
+  return GT_OK;
+}
+
 int gt_set_variant(gt_handle* h, int32_t variant) {
   if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_variant: null handle");
   if (!gt_variant_supported(h->N, variant))
     return fail(h, GT_ERR_ARG, "gt_set_variant: variant " + std::to_string(variant) +
                                    " does not exist for n=" + std::to_string(h->N));
-  h->variant = variant;
-  return GT_OK;
+  return gt_set_variants(h, variant, natural_row_variant(variant));
 }
 
 int gt_get_variant(const gt_handle* h, int32_t* variant) {
   if (!h || !variant) return fail(nullptr, GT_ERR_ARG, "gt_get_variant: null argument");
   *variant = h->variant;
+  return GT_OK;
+}
+
+int gt_get_variants(const gt_handle* h, int32_t* col_variant, int32_t* row_variant) {
+  if (!h || !col_variant || !row_variant) return fail(nullptr, GT_ERR_ARG, "gt_get_variants: null argument");
+  *col_variant = h->variant;
+  *row_variant = h->row_variant;
   return GT_OK;
 }
 
@@ -813,12 +841,11 @@ int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best)
     ms[v] = -1.0;
     navail += gt_variant_supported(h->N, v);
   }
-  int choice = h->variant;
   if (navail > 1) {
     const size_t nd = (size_t)h->N * (size_t)(h->N + 2);
     double* buf = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
-    const int saved = h->variant;
+    const int saved_col = h->variant, saved_row = h->row_variant;
     const bool prof = h->prof;
     h->prof = false;
     int rc = GT_OK;
@@ -833,10 +860,10 @@ int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best)
     auto one_step = [&]() {
       return h->rko == 4 ? gt_step_rk4(h, f[0], f[1], f[2], f[3], f[4]) : gt_step_rk2(h, f[0], f[1], f[3], f[4]);
     };
-    double best_ms = 0.0;
-    for (int v = 0; v < GT_NVARIANTS && !rc; ++v) {
-      if (!gt_variant_supported(h->N, v)) continue;
-      h->variant = v;
+    // ms per step of (column variant c, row variant r), or -1 on failure
+    auto time_pair = [&](int c, int r) -> double {
+      h->variant = c;
+      h->row_variant = r;
       for (int w = 0; w < 3 && !rc; ++w) rc = one_step();
       if (!rc) e = cudaEventRecord(ev[0], h->stream);
       for (int s = 0; s < steps && !rc; ++s) rc = one_step();
@@ -845,11 +872,24 @@ int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best)
       float t = 0.0f;
       if (!rc && e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
       if (!rc && e != cudaSuccess) rc = cuda_fail(h, e, "gt_autotune: timing");
-      if (rc) break;
-      ms[v] = (double)t / steps;
-      if (v == 0 || ms[v] < best_ms) {
-        best_ms = ms[v];
-        choice = v;
+      return rc ? -1.0 : (double)t / steps;
+    };
+    // stage 1: every column variant with the row tiles of its own register radix
+    int best_c = 0;
+    for (int v = 0; v < GT_NVARIANTS && !rc; ++v) {
+      if (!gt_variant_supported(h->N, v)) continue;
+      ms[v] = time_pair(v, natural_row_variant(v));
+      if (!rc && (ms[best_c] < 0.0 || ms[v] < ms[best_c])) best_c = v;
+    }
+    // stage 2: the row variants under the best column variant
+    int best_r = natural_row_variant(best_c);
+    double best_ms = ms[best_c];
+    for (int r = 0; r < GT_NROW_VARIANTS && !rc; ++r) {
+      if (r == natural_row_variant(best_c) || !gt_row_variant_supported(h->N, r)) continue;
+      const double t = time_pair(best_c, r);
+      if (!rc && t < best_ms) {
+        best_ms = t;
+        best_r = r;
       }
     }
     if (buf) {
@@ -859,7 +899,8 @@ int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best)
     for (cudaEvent_t x : ev)
       if (x) cudaEventDestroy(x);
     h->prof = prof;
-    h->variant = rc ? saved : choice;
+    h->variant = rc ? saved_col : best_c;
+    h->row_variant = rc ? saved_row : best_r;
     if (rc) return rc;
   }
   if (ms_per_step)

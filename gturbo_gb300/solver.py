@@ -154,30 +154,48 @@ class Solver:
     def variant(self, v: int) -> None:
         self._check(self.lib.gt_set_variant(self.h, int(v)))
 
+    @property
+    def variants(self) -> tuple[int, int]:
+        """(column variant, row variant) of the handle."""
+        c, r = ctypes.c_int32(), ctypes.c_int32()
+        self._check(self.lib.gt_get_variants(self.h, ctypes.byref(c), ctypes.byref(r)))
+        return c.value, r.value
+
+    @variants.setter
+    def variants(self, cr) -> None:
+        self._check(self.lib.gt_set_variants(self.h, int(cr[0]), int(cr[1])))
+
     def supported_variants(self) -> list[int]:
         return [v for v in range(self.NVARIANTS) if self.lib.gt_variant_supported(self.n, v)]
+
+    def supported_row_variants(self) -> list[int]:
+        return [r for r in range(3) if self.lib.gt_row_variant_supported(self.n, r)]
 
     def autotune(self, steps: int = 20, cache: str | None = "default") -> dict:
         """Pick the fastest launch variant of the nonlinear-term passes (gt_autotune).
 
         With a cache file (JSON, keyed by device name, N and integrator order), a stored
         choice is reused without timing; None disables the cache. Returns
-        {"variant": v, "ms_per_step": [...] or None, "cached": bool}.
+        {"variant": column variant, "row_variant": row variant, "ms_per_step": per column
+        variant or None, "cached": bool}.
         """
         if cache == "default":
             cache = _tune_cache_default()
         key = f"{torch.cuda.get_device_name(self.device)}|n={self.n}|rko={self.info.rko}"
         table = _read_cache(cache)
-        if key in table and table[key]["variant"] in self.supported_variants():
-            self.variant = table[key]["variant"]
-            return {"variant": self.variant, "ms_per_step": table[key].get("ms_per_step"),
-                    "cached": True}
+        hit = table.get(key)
+        if (hit and hit.get("variant") in self.supported_variants()
+                and hit.get("row_variant") in self.supported_row_variants()):
+            self.variants = (hit["variant"], hit["row_variant"])
+            return {"variant": hit["variant"], "row_variant": hit["row_variant"],
+                    "ms_per_step": hit.get("ms_per_step"), "cached": True}
         ms = (ctypes.c_double * self.NVARIANTS)()
         best = ctypes.c_int32()
         self._check(self.lib.gt_autotune(self.h, int(steps), ms, ctypes.byref(best)))
-        res = {"variant": best.value, "ms_per_step": list(ms), "cached": False}
+        col, row = self.variants
+        res = {"variant": col, "row_variant": row, "ms_per_step": list(ms), "cached": False}
         if cache is not None:
-            table[key] = {"variant": best.value, "ms_per_step": list(ms)}
+            table[key] = {"variant": col, "row_variant": row, "ms_per_step": list(ms)}
             _write_cache(cache, table)
         return res
 

@@ -278,15 +278,25 @@ int gt_profile_read(gt_handle* h, double* ms, int64_t* launches);
  * variants differ only in the radix decomposition of the transforms, so their results agree
  * to rounding (relative differences of order 1e-15 per step). */
 #define GT_NVARIANTS 5
+/* The row pass has its own choice of register radix: row variant 0, 1, 2 = 16, 8, 4 values
+ * per thread (the row tiles of column variants 0, 1 / 4, 2 / 3). */
+#define GT_NROW_VARIANTS 3
 /* 1 if launch variant `variant` exists for grid size n, else 0 (host only, no GPU needed). */
 int gt_variant_supported(int32_t n, int32_t variant);
-/* Select the variant used by every later nlt / step call of h (GT_ERR_ARG if unsupported). */
+int gt_row_variant_supported(int32_t n, int32_t row_variant);
+/* Select the variant used by every later call of h: the column passes take `variant`, the row
+ * passes the row variant of the same register radix (GT_ERR_ARG if unsupported). */
 int gt_set_variant(gt_handle* h, int32_t variant);
 int gt_get_variant(const gt_handle* h, int32_t* variant);
-/* Time `steps` steps of the handle's integrator (RK2 or RK4) for every supported variant on
- * zero fields of its own (allocated and freed here, 5 fields; nothing when only one variant
- * exists), keep the fastest, and return ms per step in ms_per_step[GT_NVARIANTS] (-1 for
- * unsupported variants) and the choice in *best (either pointer may be null). Synchronous. */
+/* Select the column and row variants separately. */
+int gt_set_variants(gt_handle* h, int32_t col_variant, int32_t row_variant);
+int gt_get_variants(const gt_handle* h, int32_t* col_variant, int32_t* row_variant);
+/* Time `steps` steps of the handle's integrator (RK2 or RK4) on zero fields of its own
+ * (allocated and freed here, 5 fields; nothing when only one variant exists): first every
+ * supported column variant with its own row tiles, then the other row variants under the
+ * fastest column variant. Keeps the fastest pair; returns ms per step of each column variant
+ * in ms_per_step[GT_NVARIANTS] (-1 for unsupported variants) and the column choice in *best
+ * (either pointer may be null; gt_get_variants gives the pair). Synchronous. */
 int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best);
 
 #ifdef __cplusplus

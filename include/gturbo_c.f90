@@ -132,6 +132,11 @@ module gturbo_c
       type(c_ptr), value :: h
       integer(c_int32_t), value :: variant
     end function
+    integer(c_int) function gt_set_variants(h, col_variant, row_variant) bind(C, name="gt_set_variants")
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: h
+      integer(c_int32_t), value :: col_variant, row_variant
+    end function
     integer(c_int) function gt_autotune(h, steps, ms_per_step, best) bind(C, name="gt_autotune")
       import :: c_int, c_ptr, c_int32_t, c_double
       type(c_ptr), value :: h

@@ -399,6 +399,24 @@ def test_step_variants_untruncated(n, rko):
         assert rel_l2(_host(z), ref) < TOL, f"variant {v}"
 
 
+@pytest.mark.parametrize("n,rko", [(64, 4), (512, 2), (2048, 2)])
+def test_mixed_row_and_column_variants(n, rko):
+    """Every (column variant, row variant) pair steps like the oracle."""
+    p = _params(n, rko=rko, dt=2e-3 if n <= 512 else 2e-4)
+    orc = Oracle(p)
+    a = rand_field(orc, 24, truncate=False) * 20.0
+    ref = a.copy()
+    orc.rk_step(ref)
+    sol = _solver(p)
+    for c in sol.supported_variants():
+        for r in sol.supported_row_variants():
+            sol.variants = (c, r)
+            assert sol.variants == (c, r)
+            z = _dev(a)
+            sol.rk_step(z, sol.work())
+            assert rel_l2(_host(z), ref) < TOL, (c, r)
+
+
 def test_variant_rejected_when_unsupported():
     from gturbo_gb300._lib import GturboError
     sol = _solver(_params(2048))
@@ -415,13 +433,14 @@ def test_autotune_and_cache(tmp_path):
     res = sol.autotune(steps=5, cache=cache)
     assert not res["cached"]
     assert res["variant"] in sol.supported_variants() and sol.variant == res["variant"]
+    assert sol.variants == (res["variant"], res["row_variant"])
     ms = res["ms_per_step"]
     assert all(ms[v] > 0 for v in sol.supported_variants())
     assert ms[res["variant"]] == min(ms[v] for v in sol.supported_variants())
     # a second solver reuses the stored choice without timing
     sol2 = _solver(p)
     res2 = sol2.autotune(steps=5, cache=cache)
-    assert res2["cached"] and sol2.variant == res["variant"]
+    assert res2["cached"] and sol2.variants == (res["variant"], res["row_variant"])
     # and the tuned handle still steps exactly like the oracle
     orc = Oracle(p)
     a = rand_field(orc, 23) * 50.0
@@ -452,3 +471,29 @@ def test_host_pipeline_matches_serial_loop():
         torch.cuda.synchronize()
         assert torch.equal(z.cpu(), outs[k]), k
     assert seed == seed_p
+
+
+@pytest.mark.parametrize("n", [64, 512, 1024])
+def test_nlt_partly_untruncated_input(n):
+    """Modes beyond the 2/3 ellipse in a few columns only, exact zeros in the columns past them:
+    pass A transforms the nonzero columns and raises the flag, stores zeros for the all-zero
+    column blocks, and pass B reads every column (in every launch variant)."""
+    p = _params(n)
+    orc = Oracle(p)
+    a = rand_field(orc, 25)
+    full = rand_field(orc, 26, truncate=False)
+    kx0 = n // 3 + 1
+    zs, fs = spec(a), spec(full)
+    zs[:, kx0:kx0 + 2] = fs[:, kx0:kx0 + 2]  # two columns just past the ellipse
+    ref = a.copy()
+    orc.nlt(ref)
+    sol = _solver(p)
+    for v in sol.supported_variants():
+        sol.variant = v
+        u, vv = sol.field(), sol.field()
+        # stale data in the scratch fields, as a previous evaluation would leave
+        u.fill_(7.0)
+        vv.fill_(-3.0)
+        z = _dev(a)
+        sol.nlt(z, u, vv)
+        assert rel_l2(_host(z), ref) < TOL, v
