@@ -505,12 +505,23 @@ def adjoint_run(torch):
             "fd_step": h}
 
 
-def ensemble_run(steps, warm, torch):
+def ensemble_run(steps, warm, torch, shard=False):
     """Member-steps/s of the 64-member mixed-size ensemble: batched (one launch per pass, CUDA
-    graph) against the plain loop over members through the single-field C-ABI."""
+    graph) against the plain loop over members through the single-field C-ABI. With
+    ``shard`` (every rank of the process group calls it) the members are split over the ranks
+    by cost and the rates are whole-job: all ranks' member-steps over the slowest rank's time."""
     from gturbo_gb300.ensemble import Ensemble, PlainLoop, ensemble_c4
 
+    import torch.distributed as dist
+
+    from gturbo_gb300.replicas import member_cost, shard_members, whole_job_rate
+
     members = ensemble_c4()
+    # sharded: each rank advances its own members (no data-path collective)
+    world = dist.get_world_size() if shard and dist.is_available() and dist.is_initialized() else 1
+    rank = dist.get_rank() if world > 1 else 0
+    mine = shard_members([member_cost(m.params.n, m.params.rko) for m in members], world)[rank]
+    members = [members[i] for i in mine]
     ens = Ensemble(members)
     ens.load_ic()
     z0 = [z.clone() for z in ens.z]
@@ -541,11 +552,17 @@ def ensemble_run(steps, warm, torch):
     torch.cuda.synchronize()
     tp = e0.elapsed_time(e1) / 1e3
     nm = len(members)
-    return {"members": nm, "sizes": "32x256^2 + 24x512^2 + 8x1024^2", "rk": 4,
+    if world > 1:
+        _, _, rate_b = whole_job_rate(nm * steps, tb)
+        _, _, rate_p = whole_job_rate(nm * kp, tp)
+    else:
+        rate_b, rate_p = nm * steps / tb, nm * kp / tp
+    return {"members": 64, "members_per_rank": nm, "ranks": world,
+            "sizes": "32x256^2 + 24x512^2 + 8x1024^2", "rk": 4,
             "alphas": "drawn from {0.5,1,2,3}", "dt": "0.25/N", "forcing": "Philox per member",
-            "batched_member_steps_s": nm * steps / tb, "batched_steps": steps,
-            "plain_member_steps_s": nm * kp / tp, "plain_steps": kp,
-            "speedup": (nm * steps / tb) / (nm * kp / tp), "graph": True, "finite": finite}
+            "batched_member_steps_s": rate_b, "batched_steps": steps,
+            "plain_member_steps_s": rate_p, "plain_steps": kp,
+            "speedup": rate_b / rate_p, "graph": True, "finite": finite}
 
 
 def refeq_run(p, k0, steps, warm, dev, torch):
@@ -599,11 +616,22 @@ def main():
         return reference_arm(args)
     if args.only is not None:
         import torch
+        import torch.distributed as dist
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         if args.only == "ensemble":
-            res = ensemble_run(args.steps, max(3, args.warmup), torch)
-        else:
+            if world > 1:  # members sharded over the ranks
+                dist.init_process_group("nccl", device_id=torch.device("cuda", torch.cuda.current_device()))
+            res = ensemble_run(args.steps, max(3, args.warmup), torch, shard=world > 1)
+            if world > 1:
+                dist.destroy_process_group()
+        elif rank == 0:
             res = adjoint_run(torch)
-        print(json.dumps(res), flush=True)
+        else:
+            return 0
+        if rank == 0:
+            print(json.dumps(res), flush=True)
         return 0
     return ours_arm(args)
 

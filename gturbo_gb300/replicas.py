@@ -33,3 +33,28 @@ def whole_job_rate(local_units: float, local_seconds: float) -> tuple[float, flo
     dist.all_reduce(secs, op=dist.ReduceOp.MAX)
     u, s = float(units.item()), float(secs.item())
     return u, s, u / s
+
+
+def member_cost(n: int, rko: int) -> float:
+    """Relative cost of one step of a member of size n: the FFT work n^2 log2 n per stage."""
+    import math
+
+    return (4 if rko == 4 else 2) * float(n) * float(n) * math.log2(n)
+
+
+def shard_members(costs: list[float], world: int) -> list[list[int]]:
+    """Partition member indices over ``world`` ranks, balancing the summed cost: members are
+    independent (own field, own Philox key), so an ensemble shards by member with no collective
+    on the data path. Longest-processing-time greedy: largest cost first, each member to the
+    rank with the least load so far (ties to the lowest rank), so the result is deterministic
+    and every rank computes the same partition. Each rank's list keeps ascending order."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    load = [0.0] * world
+    shards: list[list[int]] = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        shards[r].append(i)
+        load[r] += costs[i]
+    return [sorted(s) for s in shards]
