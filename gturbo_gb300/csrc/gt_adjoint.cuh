@@ -373,8 +373,7 @@ __device__ __forceinline__ void adj_row_tile(const AdjArgs& a, int tile) {
       if (k == 0) { p.y = 0.0; b.y = 0.0; }
       const double2 sm_ = make_double2(p.x + b.x, p.y - b.y);
       const double2 d = make_double2(p.x - b.x, p.y + b.y);
-      const double2 tt = twmul<true>(d, __ldg(&a.tw[k]));
-      zs[padix(k)] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
+      zs[padix(k)] = pack_c2r(sm_, d, __ldg(&a.tw[k]));
     }
     __syncthreads();
     {

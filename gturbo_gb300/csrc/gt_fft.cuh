@@ -41,6 +41,12 @@ GT_HD_INL double2 twmul(double2 a, double2 w) {
   return make_double2(fma(a.x, w.x, -(a.y * w.y)), fma(a.y, w.x, a.x * w.y));
 }
 
+// s + i conj(w) d: the term of the half-length C2R packing, Z[k] = S[k] + i W^-k D[k], as four
+// FMAs (the twiddle product is accumulated into s instead of being formed and then added).
+GT_HD_INL double2 pack_c2r(double2 s, double2 d, double2 w) {
+  return make_double2(fma(d.x, w.y, fma(-d.y, w.x, s.x)), fma(d.x, w.x, fma(d.y, w.y, s.y)));
+}
+
 // The W8^1 and W8^3 twiddles are c * P(a) with c = 1/sqrt(2) and P made of additions only.
 // The butterflies below keep P unscaled and fold c into the following additions as FMAs
 // (e +- c P), which removes the two multiplies per twiddle.

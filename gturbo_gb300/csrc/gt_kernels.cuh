@@ -280,9 +280,7 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
     if (k == 0) { p.y = 0.0; b.y = 0.0; }
     const double2 sm_ = make_double2(p.x + b.x, p.y - b.y);
     const double2 d = make_double2(p.x - b.x, p.y + b.y);
-    const double2 w = __ldg(&a.tw[k]);
-    const double2 tt = twmul<true>(d, w);  // W^-k d
-    zs[padix(k)] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
+    zs[padix(k)] = pack_c2r(sm_, d, __ldg(&a.tw[k]));
   }
   __syncthreads();
   // q: inverse length-M transform, R/2 values per thread; result back to zs
@@ -652,8 +650,7 @@ k_row_c2r(double* z, const double2* __restrict__ tw) {
     if (k == 0) { a.y = 0.0; b.y = 0.0; }
     const double2 sm_ = make_double2(a.x + b.x, a.y - b.y);
     const double2 d = make_double2(a.x - b.x, a.y + b.y);
-    const double2 tt = twmul<true>(d, __ldg(&tw[k]));
-    h[s] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
+    h[s] = pack_c2r(sm_, d, __ldg(&tw[k]));
   }
   fft_regs<M, 8, true, 1>(h, zs, t, tw, 1);
   __syncthreads();  // every thread has read its row values before the row is overwritten
@@ -682,8 +679,7 @@ k_row_c2r_f32(const double* __restrict__ z, float* __restrict__ out, const doubl
     if (k == 0) { a.y = 0.0; b.y = 0.0; }
     const double2 sm_ = make_double2(a.x + b.x, a.y - b.y);
     const double2 d = make_double2(a.x - b.x, a.y + b.y);
-    const double2 tt = twmul<true>(d, __ldg(&tw[k]));
-    h[s] = make_double2(sm_.x - tt.y, sm_.y + tt.x);
+    h[s] = pack_c2r(sm_, d, __ldg(&tw[k]));
   }
   fft_regs<M, 8, true, 1>(h, zs, t, tw, 1);
   float2* orow = reinterpret_cast<float2*>(out) + (size_t)y * M;

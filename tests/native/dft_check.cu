@@ -29,6 +29,25 @@ static double check(std::mt19937_64& rng) {
   return worst;
 }
 
+// twmul (a w forward, a conj(w) inverse) and pack_c2r (s + i conj(w) d) against long double
+static double check_products(std::mt19937_64& rng) {
+  std::normal_distribution<double> nd;
+  double worst = 0.0;
+  for (int trial = 0; trial < 1000; ++trial) {
+    const double2 a = make_double2(nd(rng), nd(rng)), sv = make_double2(nd(rng), nd(rng));
+    const double th = 6.283185307179586 * (trial + 0.5) / 1000.0;
+    const double2 w = make_double2(std::cos(th), -std::sin(th));
+    const long double ax = a.x, ay = a.y, wx = w.x, wy = w.y;
+    const double2 f = gt::twmul<false>(a, w), b = gt::twmul<true>(a, w), p = gt::pack_c2r(sv, a, w);
+    // conj(w) a = (wx ax + wy ay, wx ay - wy ax); i conj(w) a = (-(wx ay - wy ax), wx ax + wy ay)
+    const long double e[6] = {f.x - (ax * wx - ay * wy), f.y - (ax * wy + ay * wx),
+                              b.x - (wx * ax + wy * ay), b.y - (wx * ay - wy * ax),
+                              p.x - (sv.x - (wx * ay - wy * ax)), p.y - (sv.y + (wx * ax + wy * ay))};
+    for (long double d : e) worst = std::fmax(worst, (double)fabsl(d));
+  }
+  return worst;
+}
+
 int main() {
   std::mt19937_64 rng(7);
   const double e[8] = {check<2, false>(rng), check<2, true>(rng), check<4, false>(rng), check<4, true>(rng),
@@ -39,5 +58,8 @@ int main() {
     std::printf("radix %s max err %.3e\n", names[k], e[k]);
     if (!(e[k] < 1e-14)) bad = 1;
   }
+  const double ep = check_products(rng);
+  std::printf("twmul / pack_c2r max err %.3e\n", ep);
+  if (!(ep < 1e-14)) bad = 1;
   return bad;
 }
