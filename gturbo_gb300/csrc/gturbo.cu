@@ -468,9 +468,7 @@ int gt_create(const gt_params* p, gt_handle** out) {
   if (!rc) rc = upload(h, &h->d_lcga, h->lcga.data(), h->nf);
   if (!rc) rc = upload(h, &h->d_lcgb, h->lcgb.data(), h->nf);
   if (!rc) rc = upload(h, &h->d_ff, ff.data(), ff.size());
-  const int zero = 0;
   const int zeros2[2] = {0, 0};  // untruncated-input flags of even / odd stages
-  (void)zero;
   if (!rc) rc = upload(h, &h->d_flag, zeros2, 2);
   const int ngroups = (N + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
   if (!rc) rc = upload<double>(h, &h->d_part, nullptr, (size_t)ngroups * h->NBIN * 4);
