@@ -250,16 +250,19 @@ def pass_model(p, kind):
 # (dram__bytes_read.sum + dram__bytes_write.sum) of the same launch variant:
 #   2048^2, variant 0: ncu --set full -k "regex:k_nlt_(row|colfwd_inv|colinv)" -s 52 -c 3
 #                      python bench.py --steps 2 --warmup 3 --no-extras
-#   256^2, variant 2:  ncu --set full --kernel-name-base demangled
-#                      -k "regex:k_nltv_(row|colfwd_inv|colinv)<\(int\)256, \(int\)2>" -s 8 -c 3
-#                      python bench.py --config c1 --steps 2 --warmup 3 --no-extras --variant 2
+#   256^2, column variant 3, row variant 2:
+#                      ncu --set full --kernel-name-base demangled -k "regex:k_nltv_(row<\(int\)256,
+#                      \(int\)2>|colfwd_inv<\(int\)256, \(int\)3>|colinv<\(int\)256, \(int\)3>)" -s 8 -c 3
+#                      python bench.py --config c1 --steps 2 --warmup 3 --no-extras --variant 3
+# Keyed by (N, the launch variant of that kernel: the row variant for the row pass, the column
+# variant otherwise, pass).
 NCU_TRAFFIC = {
     (2048, 0, "nlt_colinv"): 47.07e6 + 18.51e6,
     (2048, 0, "nlt_row"): 67.99e6 + 1.53e6,
     (2048, 0, "nlt_colfwd_inv"): 110.95e6 + 41.28e6,
-    (256, 2, "nlt_colinv"): 0.774e6,
+    (256, 3, "nlt_colinv"): 0.757e6,
     (256, 2, "nlt_row"): 1.177e6,
-    (256, 2, "nlt_colfwd_inv"): 1.854e6,
+    (256, 3, "nlt_colfwd_inv"): 1.828e6,
 }
 
 
@@ -354,7 +357,7 @@ def ours_arm(args):
                 "achieved": fl / (ms / 1e3) / 1e12 if fl else None, "unit": "TFLOP/s",
                 "peak": fp64, "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
                 "(FP64 pipe; MEASURED_PEAKS.json has no FP64 figure)",
-                "traffic": NCU_TRAFFIC.get((p.n, sol.variant, top)),
+                "traffic": NCU_TRAFFIC.get((p.n, sol.variants[1] if top == "nlt_row" else sol.variants[0], top)),
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch "
                                   "(capture of the same kernel and launch variant)",
                 "hbm_achieved_gbs": by / (ms / 1e3) / 1e9 if by else None,
