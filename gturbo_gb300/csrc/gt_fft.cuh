@@ -202,7 +202,7 @@ struct StockhamPass {
 };
 
 // Full transform of length L held as R values per thread (see StockhamPass). Every thread of
-// the block must call it (it contains __syncthreads when L > R).
+// the block must call it, from the same call site (it contains __syncthreads when L > R).
 template <int L, int R, bool INV, int SS>
 __device__ __forceinline__ void fft_regs(double2 (&v)[R], double2* sm, int t,
                                          const double2* __restrict__ tw, int twshift) {

@@ -509,6 +509,91 @@ __device__ __forceinline__ void colfwd_grp_tile(const NltArgs& a, int tile) {
   }
 }
 
+// Pass B with two thread groups of T = N/R threads on one row, each with an exchange buffer
+// of its own: group 0 transforms u + i v while group 1 transforms q, extended to a Hermitian
+// spectrum of length N (its inverse transform is real q), so that both groups run the same
+// transform from the same call site and every thread meets the same barrier instructions.
+// Group 0 then forms the product and runs the forward transform; group 1 runs the same call on
+// its own buffer and discards the result.
+template <int N, int R>
+__device__ __forceinline__ void row_grp_tile(const NltArgs& a, int tile) {
+  constexpr int T = N / R, NH = N / 2 + 1, M = N / 2;
+  extern __shared__ double2 smem[];
+  const int g = threadIdx.x / T, t = threadIdx.x % T;
+  const int y = tile;  // one row per CTA
+  double2* cs = smem;               // group 0: u + i v, then the product
+  double2* qs = smem + padded(N);   // group 1: q
+  double2* buf = g == 0 ? cs : qs;
+  const int kl = (*a.flag) ? M : a.kin;
+  const double2* urow = a.u + (size_t)y * NH;
+  const double2* qrow = a.q + (size_t)y * NH;
+  const double2* vrow = a.v + (size_t)y * NH;
+  // group 0: C[k] = U[k] + i V[k], C[N-k] = conj U[k] + i conj V[k];
+  // group 1: C[k] = Q[k], C[N-k] = conj Q[k]; Im of the k=0 and N/2 values dropped
+#pragma unroll
+  for (int s = 0; s <= R / 2; ++s) {
+    const int k = t + s * T;
+    if (k <= M) {
+      const double2 U = (k <= kl) ? (g == 0 ? urow[k] : qrow[k]) : czero();
+      const double2 V = (g == 0 && k <= kl) ? vrow[k] : czero();
+      if (k == 0 || k == M) {
+        buf[padix(k)] = make_double2(U.x, V.x);
+      } else {
+        buf[padix(k)] = make_double2(U.x - V.y, U.y + V.x);
+        buf[padix(N - k)] = make_double2(U.x + V.y, V.x - U.y);
+      }
+    }
+  }
+  __syncthreads();
+  double2 v[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = buf[padix(t + s * T)];
+  __syncthreads();
+  fft_regs<N, R, true, 1>(v, buf, t, a.tw, 0);  // both groups
+  // group 0 holds u + i v, group 1 holds q (real part) at x = t + s*T
+  __syncthreads();
+  if (g == 1) {
+#pragma unroll
+    for (int s = 0; s < R; ++s) qs[padix(t + s * T)] = v[s];
+  }
+  if (g == 0 && a.phys_uv) {
+#pragma unroll
+    for (int s = 0; s < R; ++s) a.phys_uv[(size_t)y * N + t + s * T] = v[s];
+  }
+  __syncthreads();
+  if (g == 1 && a.phys_q) {  // packed as q[2m] + i q[2m+1]
+#pragma unroll
+    for (int s = 0; s < R / 2; ++s) {
+      const int m = t + s * T;
+      a.phys_q[(size_t)y * M + m] = make_double2(qs[padix(2 * m)].x, qs[padix(2 * m + 1)].x);
+    }
+  }
+  if (g == 0) {  // p = (u + i v) q  (produ.f90:18-19)
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const double q = qs[padix(t + s * T)].x;
+      v[s] = make_double2(v[s].x * q, v[s].y * q);
+    }
+  }
+  __syncthreads();  // every read of qs is done before group 1 reuses it as exchange buffer
+  fft_regs<N, R, false, 1>(v, buf, t, a.tw, 0);  // both groups; group 1's result is unused
+  __syncthreads();
+  if (g == 0) {
+#pragma unroll
+    for (int s = 0; s < R; ++s) cs[padix(t + s * T)] = v[s];
+  }
+  __syncthreads();
+  // A = P[k] + conj P[N-k], B = -i (P[k] - conj P[N-k]) for k <= kout, by both groups
+  double2* urw = a.u + (size_t)y * NH;
+  double2* vrw = a.v + (size_t)y * NH;
+  for (int k = threadIdx.x; k <= a.kout; k += 2 * T) {
+    const double2 P = cs[padix(k)];
+    const double2 Q = cs[padix((N - k) & (N - 1))];
+    urw[k] = make_double2(P.x + Q.x, P.y - Q.y);
+    vrw[k] = make_double2(P.y + Q.y, Q.x - P.x);
+  }
+}
+
 // Pass C of one stage and pass A of the next on the same column (see colfwd_colinv_tile).
 template <int N, int R>
 __device__ __forceinline__ void colfwd_colinv_grp_tile(const NltArgs& cur, const NltArgs& next, int tile) {
@@ -547,8 +632,10 @@ k_nlt_colfwd_inv(NltArgs cur, NltArgs next) {
 // V = 1: R = 8,  one column / row per CTA;
 // V = 2: R = 4,  one column / row per CTA (small grids: 4x the threads of V = 0, for the
 //        latency-bound regime where a pass leaves most SMs idle);
-// V = 3: R = 4,  grouped column tiles (the column's transforms side by side), rows as V = 2;
-// V = 4: R = 8,  grouped column tiles, rows as V = 1.
+// V = 3: R = 4,  grouped tiles: a column's transforms side by side in 3 thread groups, a row's
+//        u + i v and q transforms side by side in 2;
+// V = 4: R = 8,  grouped tiles.
+// The row pass and the column passes take their variants separately (GtOp::row_variant).
 template <int N, int V>
 struct Var {
   static constexpr bool GROUPED = V >= 3;
@@ -558,11 +645,13 @@ struct Var {
   static constexpr int COLS = V == 0 ? Shape<N>::COLS : 1;
   static constexpr int ROWS = V == 0 ? Shape<N>::ROWS : 1;
   static constexpr int COL_THREADS = (GROUPED ? kColGroups : COLS) * T;
-  static constexpr int ROW_THREADS = ROWS * T;
+  static constexpr int ROW_THREADS = (GROUPED ? 2 : ROWS) * T;
   static constexpr int COL_CTAS = (NH + COLS - 1) / COLS;
   static constexpr int ROW_CTAS = N / ROWS;
   static constexpr size_t COL_SMEM = (size_t)padded(N) * (GROUPED ? kColGroups : COLS) * sizeof(double2);
-  static constexpr size_t ROW_SMEM = (size_t)(padded(N) + padded(N / 2)) * ROWS * sizeof(double2);
+  // grouped rows: two length-N exchange buffers (u + i v and q)
+  static constexpr size_t ROW_SMEM = GROUPED ? (size_t)2 * padded(N) * sizeof(double2)
+                                             : (size_t)(padded(N) + padded(N / 2)) * ROWS * sizeof(double2);
   static constexpr bool OK = V == 0 || (V == 1 && N <= 4096) || (V >= 2 && V <= 4 && N <= 1024);
 };
 
@@ -573,7 +662,8 @@ __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colinv(NltArgs 
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_nltv_row(NltArgs a) {
-  if constexpr (Var<N, V>::OK) row_tile<N, Var<N, V>::ROWS, Var<N, V>::R>(a, blockIdx.x);
+  if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) row_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
+  else if constexpr (Var<N, V>::OK) row_tile<N, Var<N, V>::ROWS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd(NltArgs a) {

@@ -169,8 +169,8 @@ int cuda_fail(gt_handle* h, cudaError_t e, const char* what) {
 
 bool pow2_in_range(int n) { return n >= 16 && n <= 8192 && (n & (n - 1)) == 0; }
 
-// The row variant with the register radix of column variant v (16, 8, 4 values per thread).
-int natural_row_variant(int v) { return v == 0 ? 0 : (v == 1 || v == 4) ? 1 : 2; }
+// The row variant that goes with column variant v in gt_set_variant: the same launch variant.
+int natural_row_variant(int v) { return v; }
 
 // exp(-2 pi i k / n) for k in [0, n), each value from an argument reduced to [0, pi/4].
 void make_twiddles(int n, std::vector<double2>& tw) {
@@ -798,6 +798,7 @@ int gt_variant_supported(int32_t n, int32_t variant) {
 int gt_row_variant_supported(int32_t n, int32_t row_variant) {
   return row_variant >= 0 && row_variant < GT_NROW_VARIANTS && gt_variant_supported(n, row_variant);
 }
+static_assert(GT_NROW_VARIANTS == GT_NVARIANTS, "row and column variants share their numbering");
 
 int gt_set_variants(gt_handle* h, int32_t col_variant, int32_t row_variant) {
   if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_variants: null handle");

@@ -169,7 +169,7 @@ class Solver:
         return [v for v in range(self.NVARIANTS) if self.lib.gt_variant_supported(self.n, v)]
 
     def supported_row_variants(self) -> list[int]:
-        return [r for r in range(3) if self.lib.gt_row_variant_supported(self.n, r)]
+        return [r for r in range(self.NVARIANTS) if self.lib.gt_row_variant_supported(self.n, r)]
 
     def autotune(self, steps: int = 20, cache: str | None = "default") -> dict:
         """Pick the fastest launch variant of the nonlinear-term passes (gt_autotune).

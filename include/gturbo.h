@@ -278,14 +278,15 @@ int gt_profile_read(gt_handle* h, double* ms, int64_t* launches);
  * variants differ only in the radix decomposition of the transforms, so their results agree
  * to rounding (relative differences of order 1e-15 per step). */
 #define GT_NVARIANTS 5
-/* The row pass has its own choice of register radix: row variant 0, 1, 2 = 16, 8, 4 values
- * per thread (the row tiles of column variants 0, 1 / 4, 2 / 3). */
-#define GT_NROW_VARIANTS 3
+/* The row pass takes its own launch variant, numbered like the column variants: 0, 1, 2 =
+ * 16, 8, 4 values per thread; 3, 4 = 4 and 8 values per thread with the u + i v and q
+ * transforms of a row run side by side by two thread groups (n <= 1024). */
+#define GT_NROW_VARIANTS 5
 /* 1 if launch variant `variant` exists for grid size n, else 0 (host only, no GPU needed). */
 int gt_variant_supported(int32_t n, int32_t variant);
 int gt_row_variant_supported(int32_t n, int32_t row_variant);
-/* Select the variant used by every later call of h: the column passes take `variant`, the row
- * passes the row variant of the same register radix (GT_ERR_ARG if unsupported). */
+/* Select the variant used by every later call of h, for the column and the row passes alike
+ * (GT_ERR_ARG if unsupported). */
 int gt_set_variant(gt_handle* h, int32_t variant);
 int gt_get_variant(const gt_handle* h, int32_t* variant);
 /* Select the column and row variants separately. */

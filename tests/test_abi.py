@@ -120,8 +120,8 @@ def test_variant_table(lib):
         assert got == [1, int(n <= 4096)] + [int(n <= 1024)] * 3, n
     assert lib.gt_variant_supported(100, 0) == 0 and lib.gt_variant_supported(64, 5) == 0
     for n in (64, 2048, 8192):
-        assert [lib.gt_row_variant_supported(n, r) for r in range(4)] == \
-            [1, int(n <= 4096), int(n <= 1024), 0], n
+        assert [lib.gt_row_variant_supported(n, r) for r in range(6)] == \
+            [1, int(n <= 4096)] + [int(n <= 1024)] * 3 + [0], n
     assert lib.gt_set_variant(None, 0) == 1 and lib.gt_autotune(None, 1, None, None) == 1
 
 
