@@ -1,6 +1,6 @@
-"""Gradients of a final-time spectral objective (tangent-linear model and discrete adjoint of
-the Lawson RK2 step with the LCG forcing kick; ``gt_objective``, ``gt_tlm_*``, ``gt_adj_*`` of
-include/gturbo.h).
+"""Gradients of a final-time spectral objective: tangent-linear model and discrete adjoint of
+the Lawson RK2 step, discrete adjoint of the Lawson RK4 step, each with the LCG forcing kick
+(``gt_objective``, ``gt_tlm_*``, ``gt_adj_*`` of include/gturbo.h).
 
 The objective is the energy in the shells kmin <= |k| <= kmax of the final field, with the
 reference's weights: J = sum fac |q|^2 / |k|^alpha (fac = 1/2 on the kx=0 and Nyquist columns).
@@ -27,12 +27,13 @@ def objective(sol: Solver, z: torch.Tensor, kmin: float, kmax: float, grad: bool
 
 def forward_objective(sol: Solver, z0: torch.Tensor, nsteps: int, seed: int, kmin: float,
                       kmax: float) -> float:
-    """J after nsteps of RK2 + kick (the plain forward path, gt_step_rk2 + gt_forcing)."""
+    """J after nsteps of the handle's integrator + kick (the plain forward path,
+    gt_step_rk2 or gt_step_rk4, then gt_forcing)."""
     z = z0.clone()
-    work = sol.work(3)
+    work = sol.work(4)
     s = seed
     for _ in range(nsteps):
-        sol.step(z, *work)
+        sol.rk_step(z, work)
         s = sol.forcing(z, s)
     return objective(sol, z, kmin, kmax)
 

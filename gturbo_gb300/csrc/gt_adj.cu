@@ -1,5 +1,6 @@
-// gt_adj.cu -- tangent-linear model, discrete adjoint and the checkpointed gradient driver of
-// the Lawson RK2 step with the LCG forcing kick (no counterpart in the reference).
+// gt_adj.cu -- tangent-linear model and discrete adjoint of the Lawson RK2 step, discrete
+// adjoint of the Lawson RK4 step, both with the LCG forcing kick, and the checkpointed gradient
+// driver (no counterpart in the reference).
 //
 // Objective: J(z) = sum over kmin <= |k| <= kmax of fac |z|^2 / |k|^alpha, the reference's
 // energy weights (fac = 1/2 on the kx=0 and Nyquist columns, src/diagnostics.f90:150-156).
@@ -103,6 +104,38 @@ __global__ void k_forcing_dot(const double2* __restrict__ lam, int nh, int nf, c
   if (threadIdx.x == 0) *out = red[0];
 }
 
+// Elementwise parts of the adjoint of one Lawson RK4 step (e = emk, the half-step factor;
+// L = the gradient after the step with the (0,0) mode removed, g = the last transposed term):
+//   mode 0: L = P0 L (in place), mu = dt/6 L,            acc = e^2 L
+//   mode 1: mu = dt e g + dt/3 e L,                      acc += e^2 g
+//   mode 2: mu = dt/2 g + dt/3 e L,                      acc += e g
+//   mode 3: mu = dt/2 e g + dt/6 e^2 L,                  acc += e g
+__global__ void k_adj_rk4_combo(int mode, double2* __restrict__ L, const double2* __restrict__ g,
+                                double2* __restrict__ mu, double2* __restrict__ acc,
+                                const double* __restrict__ emk, size_t count, double dt) {
+  for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < count;
+       o += (size_t)gridDim.x * blockDim.x) {
+    const double e = emk[o];
+    const double2 l = (mode == 0 && o == 0) ? make_double2(0.0, 0.0) : L[o];
+    double cl, cg, ca;  // mu = cg g + cl L; acc (+)= ca (g or L)
+    switch (mode) {
+      case 0: {
+        L[o] = l;
+        mu[o] = make_double2(dt / 6.0 * l.x, dt / 6.0 * l.y);
+        acc[o] = make_double2(e * e * l.x, e * e * l.y);
+        continue;
+      }
+      case 1: cg = dt * e; cl = dt / 3.0 * e; ca = e * e; break;
+      case 2: cg = 0.5 * dt; cl = dt / 3.0 * e; ca = e; break;
+      default: cg = 0.5 * dt * e; cl = dt / 6.0 * e * e; ca = e; break;
+    }
+    const double2 gv = g[o];
+    mu[o] = make_double2(fma(cg, gv.x, cl * l.x), fma(cg, gv.y, cl * l.y));
+    const double2 av = acc[o];
+    acc[o] = make_double2(fma(ca, gv.x, av.x), fma(ca, gv.y, av.y));
+  }
+}
+
 }  // namespace gt
 
 namespace {
@@ -119,10 +152,18 @@ int acuda(gt_handle* h, cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return acuda(h, e_, #call);   \
   } while (0)
 
-int check_adj(gt_handle* h) {
+// grid size within the adjoint kernels' range (RK2 and RK4)
+int check_adj_size(gt_handle* h) {
   if (!h) return afail(nullptr, GT_ERR_ARG, "null handle");
   const gt_params* p = gt::handle_params(h);
   if (p->n > GT_ADJ_MAX_N) return afail(h, GT_ERR_ARG, "adjoint / tangent-linear: n must be <= GT_ADJ_MAX_N (4096)");
+  return GT_OK;
+}
+
+// the RK2-only entry points (tangent-linear model and the single-step adjoint calls)
+int check_adj(gt_handle* h) {
+  const int rc = check_adj_size(h);
+  if (rc) return rc;
   if (gt::handle_rko(h) != 2) return afail(h, GT_ERR_ARG, "adjoint / tangent-linear: RK2 only");
   return GT_OK;
 }
@@ -250,6 +291,23 @@ gt::AdjArgs adj_args(const gt_handle* h) {
   return a;
 }
 
+// lam = dF(x)^T lin (mode ADJ_PLAIN) or lam += dF(x)^T lin (ADJ_STAGE_A); work: q, u, v, a, b
+int adj_term(gt_handle* h, int mode, const double* x, const double* lin, double* lam, double* const* work) {
+  gt::GtOp op = op_of(h, gt::OP_ADJ_COLINV);
+  gt::AdjArgs a = adj_args(h);
+  a.q = reinterpret_cast<double2*>(work[0]);
+  a.u = reinterpret_cast<double2*>(work[1]);
+  a.v = reinterpret_cast<double2*>(work[2]);
+  a.a = reinterpret_cast<double2*>(work[3]);
+  a.b = reinterpret_cast<double2*>(work[4]);
+  a.mode = mode;
+  a.x = reinterpret_cast<const double2*>(x);
+  a.lin = reinterpret_cast<const double2*>(lin);
+  a.lam = reinterpret_cast<double2*>(lam);
+  op.adj = a;
+  return run3(h, op, gt::OP_ADJ_COLINV);
+}
+
 // one adjoint step (without the forcing dot), work: q, u, v, a, b, rho; pz, pw: the physical
 // fields of the forward evaluations at z and w when the caller kept them
 int adj_step(gt_handle* h, const double* z, const double* w, double* lam, double* const* work,
@@ -282,6 +340,69 @@ int adj_step(gt_handle* h, const double* z, const double* w, double* lam, double
   return run3(h, op, gt::OP_ADJ_COLINV);
 }
 
+// Stage k (0..3) of the Lawson RK4 step from z (src/rkstep.f90:91-128, the fused passes with
+// epilogues EPI_RK4A..D): evaluates N at zin (z, w1, w2, w3), writes the next stage state (w1,
+// w2, w3, or the new state for k = 3) to out and accumulates znew. work: q, u, v scratch
+// distinct from zin, out and z.
+int rk4_stage(gt_handle* h, int k, const double* z, const double* zin, double* out, double* znew,
+              double* const* work) {
+  gt::GtOp op = op_of(h, gt::OP_NLT_COLINV);
+  op.nlt = gt::handle_nlt_args(h, zin, work[0], work[1], work[2], gt::handle_flag(h));
+  op.nlt.epi.mode = gt::EPI_RK4A + k;
+  op.nlt.epi.out = reinterpret_cast<double2*>(out);
+  op.nlt.epi.znew = reinterpret_cast<double2*>(znew);
+  op.nlt.epi.z = reinterpret_cast<const double2*>(z);
+  return run3(h, op, gt::OP_NLT_COLINV);
+}
+
+// One RK4 step of z in place keeping its stage states w1, w2, w3 (work: q, u, v scratch).
+int rk4_step_keep(gt_handle* h, double* z, double* w1, double* w2, double* w3, double* znew,
+                  double* const* work) {
+  int rc = rk4_stage(h, 0, z, z, w1, znew, work);
+  if (!rc) rc = rk4_stage(h, 1, z, w1, w2, znew, work);
+  if (!rc) rc = rk4_stage(h, 2, z, w2, w3, znew, work);
+  if (!rc) rc = rk4_stage(h, 3, z, w3, z, znew, work);  // stage D reads znew, not z
+  return rc;
+}
+
+// Adjoint of one Lawson RK4 step (stage states z, w1, w2, w3 of the step; the forcing kick is
+// additive and its adjoint is the identity): lam = dJ/d(state after the step) on entry, dJ/dz on
+// return. With L = P0 lam (the step's last stage zeroes the (0,0) mode):
+//   mu4 = dt/6 L                   g4 = dF(w3)^T mu4
+//   mu3 = dt e g4 + dt/3 e L        g3 = dF(w2)^T mu3
+//   mu2 = dt/2 g3 + dt/3 e L        g2 = dF(w1)^T mu2
+//   mu1 = dt/2 e g2 + dt/6 e^2 L    g1 = dF(z)^T mu1
+//   dJ/dz = e^2 L + e^2 g4 + e g3 + e g2 + g1
+// work: q, u, v, a, b, g, mu, acc (8 fields).
+int adj_step_rk4(gt_handle* h, const double* z, const double* w1, const double* w2, const double* w3,
+                 double* lam, double* const* work) {
+  const gt_params* p = gt::handle_params(h);
+  const int n = p->n, nh = n / 2 + 1;
+  const size_t count = (size_t)n * nh;
+  double2* L = reinterpret_cast<double2*>(lam);
+  double2* g = reinterpret_cast<double2*>(work[5]);
+  double2* mu = reinterpret_cast<double2*>(work[6]);
+  double2* acc = reinterpret_cast<double2*>(work[7]);
+  const double* emk = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, nullptr).epi.emk;
+  cudaStream_t s = gt::handle_stream(h);
+  const int blocks = (int)((count + 255) / 256 < 4 * 152 ? (count + 255) / 256 : 4 * 152);
+  auto combo = [&](int mode) {
+    gt::k_adj_rk4_combo<<<blocks, 256, 0, s>>>(mode, L, g, mu, acc, emk, count, p->dt);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GT_OK : acuda(h, e, "adjoint RK4 update");
+  };
+  const double* ws[3] = {w3, w2, w1};
+  int rc = combo(0);
+  for (int k = 0; k < 3 && !rc; ++k) {
+    rc = adj_term(h, gt::ADJ_PLAIN, ws[k], work[6], work[5], work);
+    if (!rc) rc = combo(k + 1);
+  }
+  if (!rc) rc = adj_term(h, gt::ADJ_STAGE_A, z, work[6], work[7], work);
+  if (rc) return rc;
+  GA_CUDA(h, cudaMemcpyAsync(lam, work[7], sizeof(double2) * count, cudaMemcpyDeviceToDevice, s));
+  return GT_OK;
+}
+
 struct DevPool {
   std::vector<void*> ptrs;
   ~DevPool() {
@@ -294,6 +415,98 @@ struct DevPool {
     return static_cast<double*>(p);
   }
 };
+
+// gt_adj_gradient for the RK4 integrator: checkpoints every K steps, the last segment kept by
+// the forward sweep, each earlier segment recomputed with its stage states (z, w1, w2, w3).
+int gradient_rk4(gt_handle* h, const double* z0, int nsteps, int32_t seed, int K, double kmin, double kmax,
+                 double* J, double* grad_z0, double* grad_famp, double* zT, double* times_ms) {
+  cudaStream_t s = gt::handle_stream(h);
+  const size_t fb = field_bytes(h);
+  const int n = gt::handle_params(h)->n;
+  const int ncp = (nsteps + K - 1) / K;
+  DevPool pool;
+  std::vector<double*> cp(ncp), zs(K), w1(K), w2(K), w3(K), work(8);
+  for (auto* v : {&cp, &zs, &w1, &w2, &w3, &work})
+    for (auto& q : *v) q = pool.field(fb);
+  double* z = pool.field(fb);
+  double* znew = pool.field(fb);
+  double* lam = pool.field(fb);
+  double* scal = pool.field(sizeof(double) * ((size_t)nsteps + n + 2));
+  if (pool.ptrs.size() != (size_t)(ncp + 4 * K + 8 + 4))
+    return afail(h, GT_ERR_NOMEM, "gt_adj_gradient: cudaMalloc of the checkpoint storage failed");
+  double* dots = scal;
+  double* rows = scal + nsteps;
+  cudaEvent_t e0, e1, e2;
+  GA_CUDA(h, cudaEventCreate(&e0));
+  GA_CUDA(h, cudaEventCreate(&e1));
+  GA_CUDA(h, cudaEventCreate(&e2));
+  std::vector<int32_t> seeds(nsteps);
+  GA_CUDA(h, cudaEventRecord(e0, s));
+  GA_CUDA(h, cudaMemcpyAsync(z, z0, fb, cudaMemcpyDeviceToDevice, s));
+  const int last0 = (ncp - 1) * K;
+  int32_t sd = seed;
+  int rc = GT_OK;
+  for (int st = 0; st < nsteps; ++st) {
+    if (st % K == 0) GA_CUDA(h, cudaMemcpyAsync(cp[st / K], z, fb, cudaMemcpyDeviceToDevice, s));
+    seeds[st] = sd;
+    const int r = st >= last0 ? st - last0 : 0;  // earlier steps use slot 0 as scratch
+    if (st >= last0) GA_CUDA(h, cudaMemcpyAsync(zs[r], z, fb, cudaMemcpyDeviceToDevice, s));
+    rc = rk4_step_keep(h, z, w1[r], w2[r], w3[r], znew, work.data());
+    if (!rc) rc = gt_forcing(h, z, &sd);
+    if (rc) return rc;
+  }
+  if (zT) GA_CUDA(h, cudaMemcpyAsync(zT, z, fb, cudaMemcpyDeviceToDevice, s));
+  rc = objective_dev(h, z, kmin, kmax, lam, rows, rows + n);
+  if (rc) return rc;
+  GA_CUDA(h, cudaEventRecord(e1, s));
+  for (int c = ncp - 1; c >= 0; --c) {
+    const int s0 = c * K, s1 = (s0 + K < nsteps) ? s0 + K : nsteps;
+    if (c != ncp - 1) {  // recompute the segment's stage states from its checkpoint
+      GA_CUDA(h, cudaMemcpyAsync(zs[0], cp[c], fb, cudaMemcpyDeviceToDevice, s));
+      for (int st = s0; st < s1; ++st) {
+        const int r = st - s0;
+        rc = rk4_stage(h, 0, zs[r], zs[r], w1[r], znew, work.data());
+        if (!rc) rc = rk4_stage(h, 1, zs[r], w1[r], w2[r], znew, work.data());
+        if (!rc) rc = rk4_stage(h, 2, zs[r], w2[r], w3[r], znew, work.data());
+        if (!rc && st + 1 < s1) {
+          rc = rk4_stage(h, 3, zs[r], w3[r], zs[r + 1], znew, work.data());
+          int32_t sk = seeds[st];
+          if (!rc) rc = gt_forcing(h, zs[r + 1], &sk);
+        }
+        if (rc) return rc;
+      }
+    }
+    for (int st = s1 - 1; st >= s0; --st) {
+      const int r = st - s0;
+      rc = forcing_dot_dev(h, lam, (uint32_t)seeds[st], dots + st);
+      if (!rc) rc = adj_step_rk4(h, zs[r], w1[r], w2[r], w3[r], lam, work.data());
+      if (rc) return rc;
+    }
+  }
+  GA_CUDA(h, cudaEventRecord(e2, s));
+  GA_CUDA(h, cudaMemcpyAsync(grad_z0, lam, fb, cudaMemcpyDeviceToDevice, s));
+  std::vector<double> host(nsteps + 1);
+  GA_CUDA(h, cudaMemcpyAsync(host.data(), dots, sizeof(double) * nsteps, cudaMemcpyDeviceToHost, s));
+  GA_CUDA(h, cudaMemcpyAsync(host.data() + nsteps, rows + n, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GA_CUDA(h, cudaStreamSynchronize(s));
+  *J = host[nsteps];
+  if (grad_famp) {
+    double g = 0.0;
+    for (int st = 0; st < nsteps; ++st) g += host[st];
+    *grad_famp = g;
+  }
+  if (times_ms) {
+    float f = 0.f, b = 0.f;
+    cudaEventElapsedTime(&f, e0, e1);
+    cudaEventElapsedTime(&b, e1, e2);
+    times_ms[0] = f;
+    times_ms[1] = b;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  return GT_OK;
+}
 
 }  // namespace
 
@@ -380,9 +593,11 @@ int gt_adj_step_rk2(gt_handle* h, const double* z, const double* w, double* lam,
 
 int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed, int32_t K, double kmin,
                     double kmax, double* J, double* grad_z0, double* grad_famp, double* zT, double* times_ms) {
-  int rc = check_adj(h);
+  int rc = check_adj_size(h);
   if (rc) return rc;
   if (!z0 || !J || !grad_z0 || nsteps < 1 || K < 1) return afail(h, GT_ERR_ARG, "gt_adj_gradient: bad argument");
+  if (gt::handle_rko(h) == 4)
+    return gradient_rk4(h, z0, nsteps, seed, K, kmin, kmax, J, grad_z0, grad_famp, zT, times_ms);
   cudaStream_t s = gt::handle_stream(h);
   const size_t fb = field_bytes(h);
   const int n = gt::handle_params(h)->n;

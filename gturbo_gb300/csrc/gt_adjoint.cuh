@@ -245,10 +245,13 @@ __device__ __forceinline__ void tlm_colfwd_tile(const TlmArgs& a, int tile) {
 //       lam = e e P0 l' + e P0 lw          rho = dt/2 e P0 lw
 //   ADJ_STAGE_A: input lin = rho, linearisation point x = z:
 //       lam += dF(z)^T rho
+// The RK4 adjoint combines plain transposed terms with elementwise updates:
+//   ADJ_PLAIN:   lam = dF(x)^T lin
 // ---------------------------------------------------------------------------------------
 enum AdjMode : int {
   ADJ_STAGE_B = 0,
   ADJ_STAGE_A = 1,
+  ADJ_PLAIN = 2,
 };
 
 struct AdjArgs {
@@ -505,6 +508,8 @@ __device__ __forceinline__ void adj_colfwd_tile(const AdjArgs& a, int tile) {
       const double2 l = a.lin[o];
       a.lam[o] = origin ? czero() : make_double2(e * (e * l.x + g.x), e * (e * l.y + g.y));
       a.rho[o] = origin ? czero() : make_double2(a.dt2 * e * g.x, a.dt2 * e * g.y);
+    } else if (a.mode == ADJ_PLAIN) {
+      a.lam[o] = g;
     } else {
       const double2 l = a.lam[o];
       a.lam[o] = make_double2(l.x + g.x, l.y + g.y);

@@ -174,7 +174,7 @@ const char* gt_ens_last_error(const gt_ens* e);
 
 /* ---- tangent-linear model and discrete adjoint (no counterpart in the reference) ----
  * For the Lawson RK2 step (split or not) followed by the LCG kick, on grids
- * n <= GT_ADJ_MAX_N. The state space is the stored half-spectrum with the real
+ * n <= GT_ADJ_MAX_N; gt_adj_gradient also takes handles of the Lawson RK4 step. The state space is the stored half-spectrum with the real
  * inner product <a, b> = sum Re(conj(a) b); the parameters are the state and
  * the forcing amplitude famp (the phases follow the reference's LCG). */
 #define GT_ADJ_MAX_N 4096
@@ -195,15 +195,17 @@ int gt_adj_stage(gt_handle* h, const double* z, double* w, double* const* work);
  * is added to *gfamp (host; synchronous). work: 6 device fields. */
 int gt_adj_step_rk2(gt_handle* h, const double* z, const double* w, double* lam, int32_t seed,
                     double* gfamp, double* const* work);
-/* Gradient of J(z after nsteps of RK2 + kick from seed) with respect to z0 and
- * famp: a forward sweep that stores a checkpoint every K steps, then a backward
- * sweep that recomputes each segment's (z_s, w_s) from its checkpoint and runs
- * gt_adj_step_rk2 back over it. Outputs: J and *grad_famp (host), grad_z0 and
- * zT (device; zT may be NULL), times_ms[2] = forward / backward sweep times
- * (may be NULL). Allocates ceil(nsteps/K) + 2K + 8 fields with cudaMalloc for
- * the duration of the call, and, when the memory is there, the physical u+iv and
- * q of the 2K recomputed stages of a segment (24 N^2 bytes each), which spare the
- * adjoint passes three of their transforms. Synchronous. */
+/* Gradient of J(z after nsteps of RK2 or RK4 + kick from seed, the handle's
+ * integrator) with respect to z0 and famp: a forward sweep that stores a
+ * checkpoint every K steps, then a backward sweep that recomputes each
+ * segment's stage states from its checkpoint and runs the step adjoint back
+ * over it. Outputs: J and *grad_famp (host), grad_z0 and zT (device; zT may be
+ * NULL), times_ms[2] = forward / backward sweep times (may be NULL). Allocates
+ * with cudaMalloc for the duration of the call: RK2 ceil(nsteps/K) + 2K + 8
+ * fields and, when the memory is there, the physical u+iv and q of the 2K
+ * recomputed stages of a segment (24 N^2 bytes each), which spare the adjoint
+ * passes three of their transforms; RK4 ceil(nsteps/K) + 4K + 12 fields.
+ * Synchronous. */
 int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed, int32_t K,
                     double kmin, double kmax, double* J, double* grad_z0, double* grad_famp,
                     double* zT, double* times_ms);

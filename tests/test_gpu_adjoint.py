@@ -112,12 +112,13 @@ def test_autograd_function_wrapper():
 
 
 def test_adjoint_limits():
+    """The tangent-linear entry points are RK2 only (the RK4 gradient is tested below)."""
     from gturbo_gb300 import _lib
-    from gturbo_gb300.adjoint import gradient
+    from gturbo_gb300.adjoint import tlm_run
     from gturbo_gb300.solver import Solver
     sol = Solver(Params(n=64, rko=4))
     with pytest.raises(_lib.GturboError):
-        gradient(sol, sol.field(), 2, SEED, KMIN, KMAX)
+        tlm_run(sol, sol.field(), sol.field(), 0.0, 2, SEED, KMIN, KMAX)
 
 
 @pytest.mark.parametrize("n", [128, 1024])
@@ -176,3 +177,52 @@ def test_gradient_driver_matches_step_by_step_adjoint(n, variant):
     torch.cuda.synchronize()
     assert float((gz - lam).norm() / lam.norm()) < 1e-13
     assert gf == pytest.approx(gfamp.value, rel=1e-12)
+
+
+def _setup_rk4(n=128, nsteps=8):
+    from gturbo_gb300.ic import random_phase_ic
+    from gturbo_gb300.params import famp_for_injection, nu8_scaled
+    from gturbo_gb300.solver import Solver
+    p = Params(n=n, alpv=2.0, rko=4, dt=1e-3, nu=nu8_scaled(n), alpnu=8.0, mu=0.05, k1f=10.0, k2f=12.0)
+    p = p.replace(famp=famp_for_injection(p, 1.0))
+    sol = Solver(p)
+    z0 = torch.from_numpy(random_phase_ic(p, 5.0, 0.5, seed=9)).cuda()
+    return p, sol, z0, nsteps
+
+
+def test_rk4_gradient_against_central_differences():
+    """The RK4 adjoint (gt_adj_gradient on an RK4 handle) against FP64 central differences
+    (h = 1e-6) along random directions, in z0 and in famp; J equals the plain RK4 run's."""
+    from gturbo_gb300.adjoint import forward_objective, gradient
+    from gturbo_gb300.solver import Solver
+    p, sol, z0, ns = _setup_rk4()
+    J, gz, gf, _, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=3)
+    assert J == pytest.approx(forward_objective(sol, z0, ns, SEED, KMIN, KMAX), rel=1e-14)
+    h = 1e-6
+    for seed in range(1, 5):
+        dz = _direction(z0, 300 + seed, truncated_only=(seed % 2 == 0))
+        Jp = forward_objective(sol, z0 + h * dz, ns, SEED, KMIN, KMAX)
+        Jm = forward_objective(sol, z0 - h * dz, ns, SEED, KMIN, KMAX)
+        fd = (Jp - Jm) / (2 * h)
+        adj = float((gz * dz).sum().item())
+        assert adj == pytest.approx(fd, rel=1e-6, abs=1e-9 * abs(J)), seed
+    sp, sm = Solver(p.replace(famp=p.famp + h)), Solver(p.replace(famp=p.famp - h))
+    fd = (forward_objective(sp, z0, ns, SEED, KMIN, KMAX) - forward_objective(sm, z0, ns, SEED, KMIN, KMAX)) / (2 * h)
+    assert gf == pytest.approx(fd, rel=1e-6, abs=1e-9 * abs(J))
+
+
+@pytest.mark.parametrize("n", [64, 256])
+def test_rk4_gradient_independent_of_checkpointing(n):
+    """Checkpoint interval and launch variant change the schedule, not the RK4 gradient."""
+    from gturbo_gb300.adjoint import gradient
+    p, sol, z0, ns = _setup_rk4(n=n, nsteps=7)
+    ref = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=1)
+    for k in (2, 3, 7, 20):
+        J, gz, gf, _, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=k)
+        assert J == ref[0]
+        assert float((gz - ref[1]).norm() / ref[1].norm()) < 1e-14, k
+        assert gf == pytest.approx(ref[2], rel=1e-13)
+    for v in sol.supported_variants():
+        sol.variant = v
+        J, gz, gf, _, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=3)
+        assert float((gz - ref[1]).norm() / ref[1].norm()) < 1e-12, v
