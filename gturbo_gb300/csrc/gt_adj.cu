@@ -1,6 +1,5 @@
-// gt_adj.cu -- tangent-linear model and discrete adjoint of the Lawson RK2 step, discrete
-// adjoint of the Lawson RK4 step, both with the LCG forcing kick, and the checkpointed gradient
-// driver (no counterpart in the reference).
+// gt_adj.cu -- tangent-linear model and discrete adjoint of the Lawson RK2 and RK4 steps with
+// the LCG forcing kick, and the checkpointed gradient driver (no counterpart in the reference).
 //
 // Objective: J(z) = sum over kmin <= |k| <= kmax of fac |z|^2 / |k|^alpha, the reference's
 // energy weights (fac = 1/2 on the kx=0 and Nyquist columns, src/diagnostics.f90:150-156).
@@ -133,6 +132,46 @@ __global__ void k_adj_rk4_combo(int mode, double2* __restrict__ L, const double2
     mu[o] = make_double2(fma(cg, gv.x, cl * l.x), fma(cg, gv.y, cl * l.y));
     const double2 av = acc[o];
     acc[o] = make_double2(fma(ca, gv.x, av.x), fma(ca, gv.y, av.y));
+  }
+}
+
+// Stage k of the Lawson RK4 step and of its tangent (the arithmetic of the epilogues
+// EPI_RK4A..D of the forward passes, applied to the state and to the tangent): n, dn = N and dN
+// at the stage input; z, dz the step's state (overwritten by k = 3); zn, dzn the accumulated
+// znew; w, dw the next stage input (k = 0..2).
+__global__ void k_tlm_rk4_update(int k, const double2* __restrict__ n, const double2* __restrict__ dn,
+                                 double2* __restrict__ z, double2* __restrict__ dz, double2* __restrict__ zn,
+                                 double2* __restrict__ dzn, double2* __restrict__ w, double2* __restrict__ dw,
+                                 const double* __restrict__ emk, size_t count, double dt, double dt2,
+                                 double dt3, double dt6) {
+  for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < count;
+       o += (size_t)gridDim.x * blockDim.x) {
+    const double e = emk[o];
+    const double2 a = n[o], da = dn[o];
+    if (k == 0) {
+      const double ee = e * e;
+      const double2 x = z[o], dx = dz[o];
+      zn[o] = make_double2(ee * (x.x + dt6 * a.x), ee * (x.y + dt6 * a.y));
+      dzn[o] = make_double2(ee * (dx.x + dt6 * da.x), ee * (dx.y + dt6 * da.y));
+      w[o] = make_double2(e * (x.x + dt2 * a.x), e * (x.y + dt2 * a.y));
+      dw[o] = make_double2(e * (dx.x + dt2 * da.x), e * (dx.y + dt2 * da.y));
+    } else if (k < 3) {
+      const double d3 = dt3 * e;
+      const double2 x = z[o], dx = dz[o], zz = zn[o], dzz = dzn[o];
+      zn[o] = make_double2(zz.x + d3 * a.x, zz.y + d3 * a.y);
+      dzn[o] = make_double2(dzz.x + d3 * da.x, dzz.y + d3 * da.y);
+      if (k == 1) {
+        w[o] = make_double2(e * x.x + dt2 * a.x, e * x.y + dt2 * a.y);
+        dw[o] = make_double2(e * dx.x + dt2 * da.x, e * dx.y + dt2 * da.y);
+      } else {
+        w[o] = make_double2(e * (e * x.x + dt * a.x), e * (e * x.y + dt * a.y));
+        dw[o] = make_double2(e * (e * dx.x + dt * da.x), e * (e * dx.y + dt * da.y));
+      }
+    } else {
+      const double2 zz = zn[o], dzz = dzn[o];
+      z[o] = o == 0 ? make_double2(0.0, 0.0) : make_double2(zz.x + dt6 * a.x, zz.y + dt6 * a.y);
+      dz[o] = o == 0 ? make_double2(0.0, 0.0) : make_double2(dzz.x + dt6 * da.x, dzz.y + dt6 * da.y);
+    }
   }
 }
 
@@ -400,6 +439,42 @@ int adj_step_rk4(gt_handle* h, const double* z, const double* w1, const double* 
   if (!rc) rc = adj_term(h, gt::ADJ_STAGE_A, z, work[6], work[7], work);
   if (rc) return rc;
   GA_CUDA(h, cudaMemcpyAsync(lam, work[7], sizeof(double2) * count, cudaMemcpyDeviceToDevice, s));
+  return GT_OK;
+}
+
+// One tangent-linear RK4 step + kick: z advances as gt_step_rk4 + gt_forcing(z, seed), dz by the
+// derivative of that step plus dfamp times the kick of the same draws. work: q, u, v, dq, du, dv,
+// znew, dznew, w, dw (10 fields).
+int tlm_step_rk4(gt_handle* h, double* z, double* dz, double dfamp, int32_t* seed, double* const* work) {
+  const gt::NltArgs t = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, nullptr);
+  const int n = t.n;
+  const size_t count = (size_t)n * (n / 2 + 1);
+  cudaStream_t s = gt::handle_stream(h);
+  const int blocks = (int)((count + 255) / 256 < 4 * 152 ? (count + 255) / 256 : 4 * 152);
+  auto F = [&](int k) { return reinterpret_cast<double2*>(work[k]); };
+  gt::GtOp op = op_of(h, gt::OP_TLM_COLINV);
+  gt::TlmArgs a = tlm_args(h);
+  a.q = F(0); a.u = F(1); a.v = F(2); a.dq = F(3); a.du = F(4); a.dv = F(5);
+  a.mode = gt::TLM_PLAIN;
+  double2* zz = reinterpret_cast<double2*>(z);
+  double2* dzz = reinterpret_cast<double2*>(dz);
+  for (int k = 0; k < 4; ++k) {
+    a.x = k == 0 ? zz : F(8);
+    a.dx = k == 0 ? dzz : F(9);
+    op.tlm = a;
+    int rc = run3(h, op, gt::OP_TLM_COLINV);
+    if (rc) return rc;
+    // the next stage input goes to (w, dw) = work 8, 9: stage k reads them, so stage k writes
+    // its update after its own passes (N, dN are already in u, du)
+    gt::k_tlm_rk4_update<<<blocks, 256, 0, s>>>(k, F(1), F(4), zz, dzz, F(6), F(7), F(8), F(9),
+                                                t.epi.emk, count, t.epi.dt, t.epi.dt2, t.epi.dt3, t.epi.dt6);
+    GA_CUDA(h, cudaGetLastError());
+  }
+  const uint32_t s0 = (uint32_t)(*seed);
+  GA_CUDA(h, gt::forcing_amp(h, z, s0, gt::handle_params(h)->famp));
+  GA_CUDA(h, gt::forcing_amp(h, dz, s0, dfamp));
+  const gt::ForcingView f = gt::handle_forcing(h);
+  if (f.nf > 0) *seed = (int32_t)((f.lcga_nf * s0 + f.lcgb_nf) & 0x7FFFFFFFu);
   return GT_OK;
 }
 
@@ -718,7 +793,7 @@ int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed
 
 int gt_tlm_run(gt_handle* h, const double* z0, const double* dz0, double dfamp, int32_t nsteps, int32_t seed,
                double kmin, double kmax, double* J, double* dJ) {
-  int rc = check_adj(h);
+  int rc = check_adj_size(h);
   if (rc) return rc;
   if (!z0 || !dz0 || !J || !dJ || nsteps < 0) return afail(h, GT_ERR_ARG, "gt_tlm_run: bad argument");
   cudaStream_t s = gt::handle_stream(h);
@@ -728,15 +803,16 @@ int gt_tlm_run(gt_handle* h, const double* z0, const double* dz0, double dfamp, 
   double* z = pool.field(fb);
   double* dz = pool.field(fb);
   double* grad = pool.field(fb);
-  std::vector<double*> work(8);
+  const bool rk4 = gt::handle_rko(h) == 4;
+  std::vector<double*> work(rk4 ? 10 : 8);
   for (auto& p : work) p = pool.field(fb);
   double* rows = pool.field(sizeof(double) * (2 * (size_t)n + 2));
-  if (pool.ptrs.size() != 12) return afail(h, GT_ERR_NOMEM, "gt_tlm_run: cudaMalloc failed");
+  if (pool.ptrs.size() != work.size() + 4) return afail(h, GT_ERR_NOMEM, "gt_tlm_run: cudaMalloc failed");
   GA_CUDA(h, cudaMemcpyAsync(z, z0, fb, cudaMemcpyDeviceToDevice, s));
   GA_CUDA(h, cudaMemcpyAsync(dz, dz0, fb, cudaMemcpyDeviceToDevice, s));
   int32_t sd = seed;
   for (int st = 0; st < nsteps; ++st) {
-    rc = gt_tlm_step_rk2(h, z, dz, dfamp, &sd, work.data());
+    rc = rk4 ? tlm_step_rk4(h, z, dz, dfamp, &sd, work.data()) : gt_tlm_step_rk2(h, z, dz, dfamp, &sd, work.data());
     if (rc) return rc;
   }
   rc = objective_dev(h, z, kmin, kmax, grad, rows, rows + n);

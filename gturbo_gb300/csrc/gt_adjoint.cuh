@@ -1,5 +1,5 @@
 // gt_adjoint.cuh -- tangent-linear and discrete adjoint of the nonlinear term and of the Lawson
-// RK2 step (no counterpart in the reference). Same three-pass structure and FFT engine as
+// RK2 and RK4 steps (no counterpart in the reference). Same three-pass structure and FFT engine as
 // the forward passes; N <= 4096 (the row passes keep 3 length-N rows in shared memory).
 //
 // Notation: F(q) = T o R[-i kx (u q) - i ky (v q)] with q, u, v = C2R(q^), C2R(Mu q^), C2R(Mv q^),
@@ -22,6 +22,7 @@ namespace gt {
 enum TlmMode : int {
   TLM_STAGE_A = 0,  // w = P0 e (z + dt/2 N),      dw = P0 e (dz + dt/2 dN)
   TLM_STAGE_B = 1,  // z = P0 e (e z + dt N),       dz = P0 e (e dz + dt dN)   (in place)
+  TLM_PLAIN = 2,    // N and dN left in u and du (the RK4 stages update elementwise)
 };
 
 struct TlmArgs {
@@ -219,7 +220,7 @@ __device__ __forceinline__ void tlm_colfwd_tile(const TlmArgs& a, int tile) {
       }
     }
   }
-  if (!valid) return;
+  if (!valid || a.mode == TLM_PLAIN) return;
 #pragma unroll
   for (int s = 0; s < R; ++s) {
     const int j = t + s * T;

@@ -174,7 +174,8 @@ const char* gt_ens_last_error(const gt_ens* e);
 
 /* ---- tangent-linear model and discrete adjoint (no counterpart in the reference) ----
  * For the Lawson RK2 step (split or not) followed by the LCG kick, on grids
- * n <= GT_ADJ_MAX_N; gt_adj_gradient also takes handles of the Lawson RK4 step. The state space is the stored half-spectrum with the real
+ * n <= GT_ADJ_MAX_N; gt_adj_gradient and gt_tlm_run also take handles of the
+ * Lawson RK4 step (the single-step calls below are RK2 only). The state space is the stored half-spectrum with the real
  * inner product <a, b> = sum Re(conj(a) b); the parameters are the state and
  * the forcing amplitude famp (the phases follow the reference's LCG). */
 #define GT_ADJ_MAX_N 4096
@@ -209,7 +210,8 @@ int gt_adj_step_rk2(gt_handle* h, const double* z, const double* w, double* lam,
 int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed, int32_t K,
                     double kmin, double kmax, double* J, double* grad_z0, double* grad_famp,
                     double* zT, double* times_ms);
-/* Tangent-linear run: J and its derivative dJ along (dz0, dfamp) after nsteps. */
+/* Tangent-linear run: J and its derivative dJ along (dz0, dfamp) after nsteps
+ * of the handle's integrator (RK2 or RK4) + kick. */
 int gt_tlm_run(gt_handle* h, const double* z0, const double* dz0, double dfamp, int32_t nsteps,
                int32_t seed, double kmin, double kmax, double* J, double* dJ);
 

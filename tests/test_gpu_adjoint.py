@@ -112,13 +112,19 @@ def test_autograd_function_wrapper():
 
 
 def test_adjoint_limits():
-    """The tangent-linear entry points are RK2 only (the RK4 gradient is tested below)."""
+    """The single-step tangent-linear / adjoint calls are RK2 only (RK4 goes through
+    gt_tlm_run and gt_adj_gradient, tested below)."""
+    import ctypes
     from gturbo_gb300 import _lib
-    from gturbo_gb300.adjoint import tlm_run
     from gturbo_gb300.solver import Solver
     sol = Solver(Params(n=64, rko=4))
+    work = [sol.field() for _ in range(8)]
+    wk = (ctypes.c_void_p * 8)(*[w.data_ptr() for w in work])
+    s = ctypes.c_int32(SEED)
+    rc = sol.lib.gt_tlm_step_rk2(sol.h, sol._ptr(work[0]), sol._ptr(work[1]), 0.0, ctypes.byref(s), wk)
+    assert rc == 1
     with pytest.raises(_lib.GturboError):
-        tlm_run(sol, sol.field(), sol.field(), 0.0, 2, SEED, KMIN, KMAX)
+        sol._check(rc)
 
 
 @pytest.mark.parametrize("n", [128, 1024])
@@ -226,3 +232,19 @@ def test_rk4_gradient_independent_of_checkpointing(n):
         sol.variant = v
         J, gz, gf, _, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=3)
         assert float((gz - ref[1]).norm() / ref[1].norm()) < 1e-12, v
+
+
+@pytest.mark.parametrize("k", [1, 4])
+def test_rk4_dot_product_adjoint_vs_tlm(k):
+    """RK4: <dJ/dz0, dz0> + dJ/dfamp dfamp from the adjoint equals the tangent-linear dJ
+    (the same discrete map differentiated two ways: agreement to roundoff)."""
+    from gturbo_gb300.adjoint import gradient, tlm_run
+    p, sol, z0, ns = _setup_rk4(nsteps=6)
+    J, gz, gf, _, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=k)
+    for seed in (1, 2):
+        dz = _direction(z0, 400 + seed)
+        dfamp = 0.2 * seed
+        J2, dJ = tlm_run(sol, z0, dz, dfamp, ns, SEED, KMIN, KMAX)
+        adj = float((gz * dz).sum().item()) + gf * dfamp
+        assert J2 == pytest.approx(J, rel=1e-14)
+        assert adj == pytest.approx(dJ, rel=1e-11, abs=1e-14 * abs(J))
