@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 def _members(rko=4):
     from gturbo_gb300.ensemble import Member
     from gturbo_gb300.params import famp_for_injection
-    spec = [(128, 1.0), (256, 2.0), (128, 3.0), (512, 0.5), (256, 2.0), (1024, 1.0)]
+    spec = [(128, 1.0), (256, 2.0), (128, 3.0), (512, 0.5), (256, 2.0), (1024, 1.0), (2048, 3.0)]
     out = []
     for m, (n, a) in enumerate(spec):
         p = Params(n=n, alpv=a, rko=rko, dt=0.1 / n, nu=1e-30, alpnu=8.0, mu=0.05,
@@ -30,7 +30,7 @@ def _members(rko=4):
 
 @pytest.mark.parametrize("rko", [4, 2])
 @pytest.mark.parametrize("graph", [True, False])
-def test_batched_equals_plain_loop_bitwise(rko, graph):
+def test_batched_equals_plain_loop(rko, graph):
     from gturbo_gb300.ensemble import Ensemble, PlainLoop
     members = _members(rko)
     ens = Ensemble(members, use_graph=graph)

@@ -173,14 +173,17 @@ def test_nlt_untruncated_input(n):
 
 @pytest.mark.parametrize("n", [32, 256])
 def test_nlt_no_dealiasing(n):
+    """truncate=0: every column is transformed and kept, in every launch variant."""
     p = _params(n, truncate=0)
     orc, sol = Oracle(p), _solver(p)
     a = rand_field(orc, 8, truncate=False)
     ref = a.copy()
     orc.nlt(ref)
-    z, u, v = _dev(a), sol.field(), sol.field()
-    sol.nlt(z, u, v)
-    assert rel_l2(_host(z), ref) < TOL
+    for v in sol.supported_variants():
+        sol.variant = v
+        z, u, vv = _dev(a), sol.field(), sol.field()
+        sol.nlt(z, u, vv)
+        assert rel_l2(_host(z), ref) < TOL, v
 
 
 @pytest.mark.parametrize("n,rko,alpv", [(32, 2, 1.0), (64, 4, 2.0), (256, 2, 1.0), (256, 4, 2.0),
@@ -204,9 +207,12 @@ def test_step_split_rk2():
     a = rand_field(orc, 10)
     ref = a.copy()
     orc.rk_step(ref)
-    z = _dev(a)
-    sol.rk_step(z, sol.work())
-    assert rel_l2(_host(z), ref) < TOL
+    for c in sol.supported_variants():  # every column variant, with each row variant in turn
+        for r in sol.supported_row_variants():
+            sol.variants = (c, r)
+            z = _dev(a)
+            sol.rk_step(z, sol.work())
+            assert rel_l2(_host(z), ref) < TOL, (c, r)
 
 
 @pytest.mark.parametrize("n,k1,k2", [(64, 3.0, 5.0), (256, 10.0, 12.0), (2048, 20.0, 22.0)])
