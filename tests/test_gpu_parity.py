@@ -252,6 +252,25 @@ def test_diag(n, alpv):
         assert np.abs(out[k] - ref[k]).max() <= 1e-12 * scale, k
 
 
+@pytest.mark.parametrize("n,alpv", [(128, 1.0), (512, 2.0), (2048, 1.0)])
+def test_nonlinear_transfer_conserves_invariants_on_gpu(n, alpv):
+    """Known answer: with 2/3 dealiasing the nonlinear term moves energy and enstrophy between
+    shells without creating or destroying them, so the fluxes at the first shell (the total
+    transfers, computed by the GPU's own nlt and diagnostics) vanish to roundoff."""
+    p = _params(n, alpv=alpv)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 13)
+    z = _dev(a)
+    znl, u, v = z.clone(), sol.field(), sol.field()
+    sol.nlt(znl, u, v)
+    out = sol.diag(z, znl)
+    zs, ns = spec(a), spec(_host(znl))
+    scale = np.abs(zs * ns.conj()).sum()
+    assert abs(out["flz"][0]) < 1e-12 * scale
+    assert abs(out["fle"][0]) < 1e-12 * scale
+    assert np.abs(out["flz"]).max() > 1e-6 * scale  # the transfer itself is not trivial
+
+
 def test_main_loop_10_steps():
     """10 iterations of the main loop (step, diagnostics every 5, forcing) at 256^2, RK4."""
     from gturbo_gb300.params import config
