@@ -44,6 +44,7 @@ def load(path: str | None = None):
         raise ImportError(f"gturbo_gb300 CUDA library not built: {path} is missing "
                           "(run gturbo_gb300.build.build())")
     lib = ctypes.CDLL(path)
+    lib._gt_path = path
     P = ctypes.c_void_p
     D = ctypes.c_void_p  # device pointers are passed as integers
     H = ctypes.POINTER(ctypes.c_double)

@@ -174,14 +174,17 @@ class Solver:
     def autotune(self, steps: int = 20, cache: str | None = "default") -> dict:
         """Pick the fastest launch variant of the nonlinear-term passes (gt_autotune).
 
-        With a cache file (JSON, keyed by device name, N and integrator order), a stored
-        choice is reused without timing; None disables the cache. Returns
+        With a cache file (JSON, keyed by device name, N, integrator order and the library
+        file's size and time), a stored choice is reused without timing; None disables it. Returns
         {"variant": column variant, "row_variant": row variant, "ms_per_step": per column
         variant or None, "cached": bool}.
         """
         if cache == "default":
             cache = _tune_cache_default()
-        key = f"{torch.cuda.get_device_name(self.device)}|n={self.n}|rko={self.info.rko}"
+        # the library's identity (size, mtime) is part of the key: a rebuilt library re-times
+        st = os.stat(getattr(self.lib, "_gt_path", _lib.LIB_PATH))
+        key = (f"{torch.cuda.get_device_name(self.device)}|n={self.n}|rko={self.info.rko}"
+               f"|lib={st.st_size}-{int(st.st_mtime)}")
         table = _read_cache(cache)
         hit = table.get(key)
         if (hit and hit.get("variant") in self.supported_variants()
