@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip e2e / cpu / ref-equivalent legs")
     ap.add_argument("--variant", type=int, default=None,
                     help="launch variant of the nonlinear-term passes (default: autotuned)")
+    ap.add_argument("--adjoint-rk", type=int, choices=[2, 4], default=2,
+                    help="integrator of the --only adjoint leg (the bench's own leg is RK2)")
     ap.add_argument("--only", choices=["ensemble", "adjoint"], default=None,
                     help="run one secondary leg alone and print its JSON object (profiling)")
     return ap.parse_args()
@@ -466,8 +468,9 @@ def ours_arm(args):
     return 0
 
 
-def adjoint_run(torch):
-    """The 1024^2 gradient workload: 200 RK2 steps with the LCG kick (alpha=1, dt=5e-5), J =
+def adjoint_run(torch, rko=2):
+    """The 1024^2 gradient workload: 200 RK2 (or, with rko=4, RK4) steps with the LCG kick
+    (alpha=1, dt=5e-5), J =
     energy in the shells 4 <= |k| <= 8 at the final time, gradients with respect to the initial
     field and famp by the checkpointed adjoint (checkpoint every 20 steps). Reports the backward
     sweep against the plain forward run, and checks the gradient against the tangent-linear
@@ -478,6 +481,8 @@ def adjoint_run(torch):
     from gturbo_gb300.solver import Solver
 
     p = config("c5")
+    if rko == 4:
+        p = p.replace(rko=4)
     nsteps, K, kmin, kmax = 200, 20, 4.0, 8.0
     sol = Solver(p)
     z0 = torch.from_numpy(random_phase_ic(p, IC_K0["c5"], 0.5, seed=1)).cuda()
@@ -499,7 +504,7 @@ def adjoint_run(torch):
     h = 1e-6
     fd = (forward_objective(sol, z0 + h * dz, nsteps, SEED, kmin, kmax)
           - forward_objective(sol, z0 - h * dz, nsteps, SEED, kmin, kmax)) / (2 * h)
-    return {"workload": f"{p.n}^2 alpha={p.alpv:g} RK2 dt={p.dt:g}, {nsteps} steps, LCG kick, "
+    return {"workload": f"{p.n}^2 alpha={p.alpv:g} RK{p.rko} dt={p.dt:g}, {nsteps} steps, LCG kick, "
                         f"J = energy in {kmin:g}<=|k|<={kmax:g}, checkpoint every {K}",
             "forward_ms": t_fwd, "adjoint_forward_sweep_ms": tf, "adjoint_backward_sweep_ms": tb,
             "backward_over_forward": tb / t_fwd, "gradient_over_forward": (tf + tb) / t_fwd,
@@ -630,7 +635,7 @@ def main():
             if world > 1:
                 dist.destroy_process_group()
         elif rank == 0:
-            res = adjoint_run(torch)
+            res = adjoint_run(torch, args.adjoint_rk)
         else:
             return 0
         if rank == 0:

@@ -331,9 +331,12 @@ gt::AdjArgs adj_args(const gt_handle* h) {
 }
 
 // lam = dF(x)^T lin (mode ADJ_PLAIN) or lam += dF(x)^T lin (ADJ_STAGE_A); work: q, u, v, a, b
-int adj_term(gt_handle* h, int mode, const double* x, const double* lin, double* lam, double* const* work) {
+int adj_term(gt_handle* h, int mode, const double* x, const double* lin, double* lam, double* const* work,
+             Phys px = Phys()) {
   gt::GtOp op = op_of(h, gt::OP_ADJ_COLINV);
   gt::AdjArgs a = adj_args(h);
+  a.phys_uv = px.uv;  // the physical fields of the forward evaluation at x, when kept
+  a.phys_q = px.q;
   a.q = reinterpret_cast<double2*>(work[0]);
   a.u = reinterpret_cast<double2*>(work[1]);
   a.v = reinterpret_cast<double2*>(work[2]);
@@ -384,9 +387,11 @@ int adj_step(gt_handle* h, const double* z, const double* w, double* lam, double
 // w2, w3, or the new state for k = 3) to out and accumulates znew. work: q, u, v scratch
 // distinct from zin, out and z.
 int rk4_stage(gt_handle* h, int k, const double* z, const double* zin, double* out, double* znew,
-              double* const* work) {
+              double* const* work, Phys keep = Phys()) {
   gt::GtOp op = op_of(h, gt::OP_NLT_COLINV);
   op.nlt = gt::handle_nlt_args(h, zin, work[0], work[1], work[2], gt::handle_flag(h));
+  op.nlt.phys_uv = keep.uv;
+  op.nlt.phys_q = keep.q;
   op.nlt.epi.mode = gt::EPI_RK4A + k;
   op.nlt.epi.out = reinterpret_cast<double2*>(out);
   op.nlt.epi.znew = reinterpret_cast<double2*>(znew);
@@ -395,12 +400,15 @@ int rk4_stage(gt_handle* h, int k, const double* z, const double* zin, double* o
 }
 
 // One RK4 step of z in place keeping its stage states w1, w2, w3 (work: q, u, v scratch).
+// keep: the physical fields of the evaluations at z, w1, w2, w3 (null entries: not kept).
 int rk4_step_keep(gt_handle* h, double* z, double* w1, double* w2, double* w3, double* znew,
-                  double* const* work) {
-  int rc = rk4_stage(h, 0, z, z, w1, znew, work);
-  if (!rc) rc = rk4_stage(h, 1, z, w1, w2, znew, work);
-  if (!rc) rc = rk4_stage(h, 2, z, w2, w3, znew, work);
-  if (!rc) rc = rk4_stage(h, 3, z, w3, z, znew, work);  // stage D reads znew, not z
+                  double* const* work, const Phys* keep = nullptr) {
+  const Phys none;
+  auto kp = [&](int k) { return keep ? keep[k] : none; };
+  int rc = rk4_stage(h, 0, z, z, w1, znew, work, kp(0));
+  if (!rc) rc = rk4_stage(h, 1, z, w1, w2, znew, work, kp(1));
+  if (!rc) rc = rk4_stage(h, 2, z, w2, w3, znew, work, kp(2));
+  if (!rc) rc = rk4_stage(h, 3, z, w3, z, znew, work, kp(3));  // stage D reads znew, not z
   return rc;
 }
 
@@ -414,7 +422,9 @@ int rk4_step_keep(gt_handle* h, double* z, double* w1, double* w2, double* w3, d
 //   dJ/dz = e^2 L + e^2 g4 + e g3 + e g2 + g1
 // work: q, u, v, a, b, g, mu, acc (8 fields).
 int adj_step_rk4(gt_handle* h, const double* z, const double* w1, const double* w2, const double* w3,
-                 double* lam, double* const* work) {
+                 double* lam, double* const* work, const Phys* keep = nullptr) {
+  const Phys none;
+  auto kp = [&](int k) { return keep ? keep[k] : none; };  // at z, w1, w2, w3
   const gt_params* p = gt::handle_params(h);
   const int n = p->n, nh = n / 2 + 1;
   const size_t count = (size_t)n * nh;
@@ -433,10 +443,10 @@ int adj_step_rk4(gt_handle* h, const double* z, const double* w1, const double* 
   const double* ws[3] = {w3, w2, w1};
   int rc = combo(0);
   for (int k = 0; k < 3 && !rc; ++k) {
-    rc = adj_term(h, gt::ADJ_PLAIN, ws[k], work[6], work[5], work);
+    rc = adj_term(h, gt::ADJ_PLAIN, ws[k], work[6], work[5], work, kp(3 - k));
     if (!rc) rc = combo(k + 1);
   }
-  if (!rc) rc = adj_term(h, gt::ADJ_STAGE_A, z, work[6], work[7], work);
+  if (!rc) rc = adj_term(h, gt::ADJ_STAGE_A, z, work[6], work[7], work, kp(0));
   if (rc) return rc;
   GA_CUDA(h, cudaMemcpyAsync(lam, work[7], sizeof(double2) * count, cudaMemcpyDeviceToDevice, s));
   return GT_OK;
@@ -511,6 +521,24 @@ int gradient_rk4(gt_handle* h, const double* z0, int nsteps, int32_t seed, int K
     return afail(h, GT_ERR_NOMEM, "gt_adj_gradient: cudaMalloc of the checkpoint storage failed");
   double* dots = scal;
   double* rows = scal + nsteps;
+  // the physical u+iv and q of the 4K stage evaluations of a segment (24 N^2 bytes each), read
+  // by the transposed terms; without the memory for them those terms transform x themselves
+  DevPool phys_pool;
+  std::vector<Phys> keep(4 * (size_t)K);
+  {
+    const size_t uvb = sizeof(double2) * (size_t)n * n, qb = sizeof(double2) * (size_t)n * (n / 2);
+    bool ok = true;
+    for (auto& k : keep) {
+      if (!ok) break;
+      k.uv = reinterpret_cast<double2*>(phys_pool.field(uvb));
+      k.q = reinterpret_cast<double2*>(phys_pool.field(qb));
+      ok = k.uv && k.q;
+    }
+    if (!ok) {
+      cudaGetLastError();  // clear the failed allocation
+      for (auto& k : keep) k = Phys();
+    }
+  }
   cudaEvent_t e0, e1, e2;
   GA_CUDA(h, cudaEventCreate(&e0));
   GA_CUDA(h, cudaEventCreate(&e1));
@@ -526,7 +554,7 @@ int gradient_rk4(gt_handle* h, const double* z0, int nsteps, int32_t seed, int K
     seeds[st] = sd;
     const int r = st >= last0 ? st - last0 : 0;  // earlier steps use slot 0 as scratch
     if (st >= last0) GA_CUDA(h, cudaMemcpyAsync(zs[r], z, fb, cudaMemcpyDeviceToDevice, s));
-    rc = rk4_step_keep(h, z, w1[r], w2[r], w3[r], znew, work.data());
+    rc = rk4_step_keep(h, z, w1[r], w2[r], w3[r], znew, work.data(), st >= last0 ? &keep[4 * r] : nullptr);
     if (!rc) rc = gt_forcing(h, z, &sd);
     if (rc) return rc;
   }
@@ -540,11 +568,12 @@ int gradient_rk4(gt_handle* h, const double* z0, int nsteps, int32_t seed, int K
       GA_CUDA(h, cudaMemcpyAsync(zs[0], cp[c], fb, cudaMemcpyDeviceToDevice, s));
       for (int st = s0; st < s1; ++st) {
         const int r = st - s0;
-        rc = rk4_stage(h, 0, zs[r], zs[r], w1[r], znew, work.data());
-        if (!rc) rc = rk4_stage(h, 1, zs[r], w1[r], w2[r], znew, work.data());
-        if (!rc) rc = rk4_stage(h, 2, zs[r], w2[r], w3[r], znew, work.data());
+        const Phys* kr = &keep[4 * (size_t)r];
+        rc = rk4_stage(h, 0, zs[r], zs[r], w1[r], znew, work.data(), kr[0]);
+        if (!rc) rc = rk4_stage(h, 1, zs[r], w1[r], w2[r], znew, work.data(), kr[1]);
+        if (!rc) rc = rk4_stage(h, 2, zs[r], w2[r], w3[r], znew, work.data(), kr[2]);
         if (!rc && st + 1 < s1) {
-          rc = rk4_stage(h, 3, zs[r], w3[r], zs[r + 1], znew, work.data());
+          rc = rk4_stage(h, 3, zs[r], w3[r], zs[r + 1], znew, work.data(), kr[3]);
           int32_t sk = seeds[st];
           if (!rc) rc = gt_forcing(h, zs[r + 1], &sk);
         }
@@ -554,7 +583,10 @@ int gradient_rk4(gt_handle* h, const double* z0, int nsteps, int32_t seed, int K
     for (int st = s1 - 1; st >= s0; --st) {
       const int r = st - s0;
       rc = forcing_dot_dev(h, lam, (uint32_t)seeds[st], dots + st);
-      if (!rc) rc = adj_step_rk4(h, zs[r], w1[r], w2[r], w3[r], lam, work.data());
+      // a recomputed segment's last stage D was not evaluated: its term transforms w3 itself
+      Phys kr[4] = {keep[4 * (size_t)r], keep[4 * (size_t)r + 1], keep[4 * (size_t)r + 2], keep[4 * (size_t)r + 3]};
+      if (c != ncp - 1 && st + 1 == s1) kr[3] = Phys();
+      if (!rc) rc = adj_step_rk4(h, zs[r], w1[r], w2[r], w3[r], lam, work.data(), kr);
       if (rc) return rc;
     }
   }

@@ -205,7 +205,8 @@ int gt_adj_step_rk2(gt_handle* h, const double* z, const double* w, double* lam,
  * with cudaMalloc for the duration of the call: RK2 ceil(nsteps/K) + 2K + 8
  * fields and, when the memory is there, the physical u+iv and q of the 2K
  * recomputed stages of a segment (24 N^2 bytes each), which spare the adjoint
- * passes three of their transforms; RK4 ceil(nsteps/K) + 4K + 12 fields.
+ * passes three of their transforms; RK4 ceil(nsteps/K) + 4K + 12 fields and,
+ * likewise, the physical fields of its 4K recomputed stage evaluations.
  * Synchronous. */
 int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed, int32_t K,
                     double kmin, double kmax, double* J, double* grad_z0, double* grad_famp,
