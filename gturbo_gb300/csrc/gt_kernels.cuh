@@ -122,17 +122,25 @@ struct Shape {
 
 __device__ __forceinline__ double2 czero() { return make_double2(0.0, 0.0); }
 
-// Minimum resident CTAs per SM requested from ptxas (register budget) for N >= 1024.
+// Minimum resident CTAs per SM requested from ptxas (register budget) for N >= 1024: up to
+// GT_*_MINB, but never so many that a thread gets fewer registers than its pass needs without
+// spilling (about 248 for the row pass, 168 for the column passes, at 16 values per thread).
+// The CTA grows with N (N/16 threads per row or column), so from 4096^2 up one CTA per SM is
+// requested and the register file bounds the rest (128 registers at 512 threads).
 #ifndef GT_ROW_MINB
 #define GT_ROW_MINB 2
 #endif
 #ifndef GT_COL_MINB
 #define GT_COL_MINB 3
 #endif
+constexpr int min_blocks(int cap, int threads, int regs) {
+  const int fit = 65536 / (threads * regs);
+  return fit < 1 ? 1 : (fit < cap ? fit : cap);
+}
 template <int N>
 struct MinBlocks {
-  static constexpr int ROW = N >= 1024 ? GT_ROW_MINB : 1;
-  static constexpr int COL = N >= 1024 ? GT_COL_MINB : 1;
+  static constexpr int ROW = N >= 1024 ? min_blocks(GT_ROW_MINB, Shape<N>::ROW_THREADS, 248) : 1;
+  static constexpr int COL = N >= 1024 ? min_blocks(GT_COL_MINB, Shape<N>::COL_THREADS, 168) : 1;
 };
 
 // ---------------------------------------------------------------------------------------
