@@ -133,14 +133,20 @@ __device__ __forceinline__ double2 czero() { return make_double2(0.0, 0.0); }
 #ifndef GT_COL_MINB
 #define GT_COL_MINB 3
 #endif
+#ifndef GT_ROW_REGS
+#define GT_ROW_REGS 248
+#endif
+#ifndef GT_COL_REGS
+#define GT_COL_REGS 168
+#endif
 constexpr int min_blocks(int cap, int threads, int regs) {
   const int fit = 65536 / (threads * regs);
   return fit < 1 ? 1 : (fit < cap ? fit : cap);
 }
 template <int N>
 struct MinBlocks {
-  static constexpr int ROW = N >= 1024 ? min_blocks(GT_ROW_MINB, Shape<N>::ROW_THREADS, 248) : 1;
-  static constexpr int COL = N >= 1024 ? min_blocks(GT_COL_MINB, Shape<N>::COL_THREADS, 168) : 1;
+  static constexpr int ROW = N >= 1024 ? min_blocks(GT_ROW_MINB, Shape<N>::ROW_THREADS, GT_ROW_REGS) : 1;
+  static constexpr int COL = N >= 1024 ? min_blocks(GT_COL_MINB, Shape<N>::COL_THREADS, GT_COL_REGS) : 1;
 };
 
 // ---------------------------------------------------------------------------------------
