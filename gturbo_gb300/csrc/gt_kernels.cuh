@@ -123,10 +123,11 @@ struct Shape {
 __device__ __forceinline__ double2 czero() { return make_double2(0.0, 0.0); }
 
 // Minimum resident CTAs per SM requested from ptxas (register budget) for N >= 1024: up to
-// GT_*_MINB, but never so many that a thread gets fewer registers than its pass needs without
-// spilling (about 248 for the row pass, 168 for the column passes, at 16 values per thread).
-// The CTA grows with N (N/16 threads per row or column), so from 4096^2 up one CTA per SM is
-// requested and the register file bounds the rest (128 registers at 512 threads).
+// GT_*_MINB, but never so many that a thread gets fewer than GT_*_REGS registers. The CTA grows
+// with N (N/16 threads per row or column): 3 column / 2 row CTAs at 2048^2 (168 / 255
+// registers), 2 at 4096^2 (128 registers: a few spills, but faster on GB300 than one CTA with
+// 254), 1 at 8192^2 (the register file allows 128 at 512 threads). Requesting the 2048^2
+// counts at 4096^2 and 8192^2 capped the kernels at 40-85 registers, and they spilled heavily.
 #ifndef GT_ROW_MINB
 #define GT_ROW_MINB 2
 #endif
@@ -134,10 +135,10 @@ __device__ __forceinline__ double2 czero() { return make_double2(0.0, 0.0); }
 #define GT_COL_MINB 3
 #endif
 #ifndef GT_ROW_REGS
-#define GT_ROW_REGS 248
+#define GT_ROW_REGS 128
 #endif
 #ifndef GT_COL_REGS
-#define GT_COL_REGS 168
+#define GT_COL_REGS 128
 #endif
 constexpr int min_blocks(int cap, int threads, int regs) {
   const int fit = 65536 / (threads * regs);

@@ -345,10 +345,10 @@ int gt_create(const gt_params* p, gt_handle** out) {
   h->dispatch = dispatch_for(N);
   // The launch variants that timed fastest on GB300 for this grid size (RK2 and RK4 alike).
   // Columns: grouped with 4 values per thread up to 256^2, 4 values per thread at 512^2, 8 at
-  // 1024^2 and 4096^2, 16 at 2048^2 and 8192^2. Rows: grouped with 4 values per thread up to
+  // 1024^2, 16 from 2048^2 up. Rows: grouped with 4 values per thread up to
   // 128^2, 4 values per thread at 256^2, 8 at 512^2 and 1024^2, 16 from 2048^2 up.
   // gt_autotune re-times.
-  h->variant = N <= 256 ? 3 : N == 512 ? 2 : (N == 1024 || N == 4096) ? 1 : 0;
+  h->variant = N <= 256 ? 3 : N == 512 ? 2 : N == 1024 ? 1 : 0;
   h->row_variant = N <= 128 ? 3 : N == 256 ? 2 : N <= 1024 ? 1 : 0;
   // inieuler.f90:22-36, 237-244
   int split = 0;
