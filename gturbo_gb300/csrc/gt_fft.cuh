@@ -10,7 +10,9 @@
 //     in registers in the same x[t + s*T] pattern, so the callers load from and store to HBM
 //     without an extra shared-memory round trip and fuse their own pre/post arithmetic;
 //   * twiddles come from a precomputed table (no FP64 sin/cos), butterflies are written so
-//     that nvcc contracts the multiplies into FMAs;
+//     that nvcc contracts the multiplies into FMAs, and the upper half of each twiddled
+//     butterfly's inputs uses the Linzer-Feig form c (1 + i t) of its twiddle, whose c folds into
+//     the first additions (a radix-16 pass: 188 instead of 212 FP64 instructions per thread);
 //   * shared memory is padded one slot in 16 (padix) so the stride-R stores of the early
 //     passes hit distinct banks.
 #pragma once
@@ -65,62 +67,52 @@ GT_HD_INL double2 w8_3_unscaled(double2 a) {
 // e + s c P and e - s c P (s = +-1 folded into c)
 GT_HD_INL double2 fma_c(double c, double2 p, double2 e) { return make_double2(fma(c, p.x, e.x), fma(c, p.y, e.y)); }
 
+// a (1 + i t): the twiddle c (1 + i t) without its real factor c, as two FMAs (Linzer and Feig,
+// "Modified FFTs for fused multiply-add architectures", Math. Comp. 60 (1993)). The factor c is
+// folded into the additions that follow (e +- c y), so a twiddle costs two FMAs instead of four
+// operations.
+GT_HD_INL double2 mul_1pit(double2 a, double t) { return make_double2(fma(-t, a.y, a.x), fma(t, a.x, a.y)); }
+
+// W16^1 = c16 (1 - i t16) and W16^3 = c16 (t16 - i), t16 = tan(pi/8); conjugates for the inverse.
+constexpr double kC16 = 0.92387953251128675613;  // cos(pi/8)
+constexpr double kT16 = 0.41421356237309504880;  // tan(pi/8) = sqrt(2) - 1
+// a (1 - i t16) forward, a (1 + i t16) inverse
 template <bool INV>
-GT_HD_INL void dft2(double2& a0, double2& a1) {
-  double2 t = a0;
-  a0 = cadd(t, a1);
-  a1 = csub(t, a1);
+GT_HD_INL double2 w16_1_unscaled(double2 a) { return mul_1pit(a, INV ? kT16 : -kT16); }
+// a (t16 - i) forward, a (t16 + i) inverse
+template <bool INV>
+GT_HD_INL double2 w16_3_unscaled(double2 a) {
+  return INV ? make_double2(fma(kT16, a.x, -a.y), fma(kT16, a.y, a.x))
+             : make_double2(fma(kT16, a.x, a.y), fma(kT16, a.y, -a.x));
 }
 
-template <bool INV>
-GT_HD_INL void dft4(double2& a0, double2& a1, double2& a2, double2& a3) {
-  double2 t0 = cadd(a0, a2), t1 = csub(a0, a2);
-  double2 t2 = cadd(a1, a3), t3 = mul_w4<INV>(csub(a1, a3));
-  a0 = cadd(t0, t2);
-  a2 = csub(t0, t2);
-  a1 = cadd(t1, t3);
-  a3 = csub(t1, t3);
-}
+// ---- butterflies from first-level pairs -------------------------------------------------------
+// Every radix-RP butterfly starts with the sums and differences of the input pairs
+// (r, r + RP/2): s_r = a_r + a_{r+RP/2}, d_r = a_r - a_{r+RP/2}, r < RP/2. dft_pairs finishes the
+// transform from them, in natural order. The plain butterfly (dft) forms the pairs with
+// additions; the twiddled one of the Stockham passes (dft_tw) forms them with FMAs from the
+// Linzer-Feig form of the upper twiddle.
 
-// Radix-8 as 2 x radix-4: even/odd DFT4s, W8^k twiddles, radix-2 combine. Natural order.
+// Radix 16 as 4 x radix-4 with W16^(n1*k2) twiddles (b[n1][k2] = a[n1 + 4 k2] after the first
+// stage, X[k2 + 4 k1] from the second).
 template <bool INV>
-GT_HD_INL void dft8(double2* a) {
-  double2 e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6];
-  double2 o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
-  dft4<INV>(e0, e1, e2, e3);
-  dft4<INV>(o0, o1, o2, o3);
-  const double2 p1 = w8_1_unscaled<INV>(o1);
-  const double2 p3 = w8_3_unscaled<INV>(o3);
-  o2 = mul_w4<INV>(o2);
-  a[0] = cadd(e0, o0); a[4] = csub(e0, o0);
-  a[1] = fma_c(kC8, p1, e1); a[5] = fma_c(-kC8, p1, e1);
-  a[2] = cadd(e2, o2); a[6] = csub(e2, o2);
-  a[3] = fma_c(kC8, p3, e3); a[7] = fma_c(-kC8, p3, e3);
-}
-
-// Radix-16 as 4 x radix-4 with W16^(n1*k2) twiddles (b[n1][k2] = a[n1 + 4 k2] after the first
-// stage, X[k2 + 4 k1] from the second). Natural order in and out.
-template <bool INV>
-GT_HD_INL void dft16(double2* a) {
-  const double c16 = 0.92387953251128675613;  // cos(pi/8)
-  const double s16 = 0.38268343236508977173;  // sin(pi/8)
-#pragma unroll
-  for (int n1 = 0; n1 < 4; ++n1) dft4<INV>(a[n1], a[n1 + 4], a[n1 + 8], a[n1 + 12]);
+GT_HD_INL void dft16_stage2(double2* a) {
   double2 X[16];
   // k2 = 0: no twiddles
   {
-    double2 y0 = a[0], y1 = a[1], y2 = a[2], y3 = a[3];
-    dft4<INV>(y0, y1, y2, y3);
-    X[0] = y0; X[4] = y1; X[8] = y2; X[12] = y3;
+    double2 t0 = cadd(a[0], a[2]), t1 = csub(a[0], a[2]);
+    double2 t2 = cadd(a[1], a[3]), t3 = mul_w4<INV>(csub(a[1], a[3]));
+    X[0] = cadd(t0, t2); X[8] = csub(t0, t2); X[4] = cadd(t1, t3); X[12] = csub(t1, t3);
   }
-  // k2 = 1: (b0, W16^1 b1, W16^2 b2, W16^3 b3); W16^2 = W8^1 folded into t0, t1
+  // k2 = 1: (b0, W16^1 b1, W16^2 b2, W16^3 b3). W16^1 b1 + W16^3 b3 = c16 (u1 + u3) with u1, u3 the
+  // unscaled products; c16 and the c of W16^2 = W8^1 are folded into the output FMAs.
   {
-    const double2 b1 = twmul<INV>(a[5], make_double2(c16, -s16));
+    const double2 u1 = w16_1_unscaled<INV>(a[5]), u3 = w16_3_unscaled<INV>(a[7]);
     const double2 p2 = w8_1_unscaled<INV>(a[6]);
-    const double2 b3 = twmul<INV>(a[7], make_double2(s16, -c16));
     const double2 t0 = fma_c(kC8, p2, a[4]), t1 = fma_c(-kC8, p2, a[4]);
-    const double2 t2 = cadd(b1, b3), t3 = mul_w4<INV>(csub(b1, b3));
-    X[1] = cadd(t0, t2); X[9] = csub(t0, t2); X[5] = cadd(t1, t3); X[13] = csub(t1, t3);
+    const double2 sp = cadd(u1, u3), dm = mul_w4<INV>(csub(u1, u3));
+    X[1] = fma_c(kC16, sp, t0); X[9] = fma_c(-kC16, sp, t0);
+    X[5] = fma_c(kC16, dm, t1); X[13] = fma_c(-kC16, dm, t1);
   }
   // k2 = 2: (b0, W8^1 b1, W4 b2, W8^3 b3); both W8 factors share c: c (P1 +- P3)
   {
@@ -132,32 +124,93 @@ GT_HD_INL void dft16(double2* a) {
     X[2] = fma_c(kC8, sp, t0); X[10] = fma_c(-kC8, sp, t0);
     X[6] = fma_c(kC8, dm, t1); X[14] = fma_c(-kC8, dm, t1);
   }
-  // k2 = 3: (b0, W16^3 b1, W16^6 b2, W16^9 b3); W16^6 = W8^3 folded into t0, t1
+  // k2 = 3: (b0, W16^3 b1, W16^6 b2, W16^9 b3) with W16^9 = -W16^1: c16 (u3 - u1)
   {
-    const double2 b1 = twmul<INV>(a[13], make_double2(s16, -c16));
+    const double2 u3 = w16_3_unscaled<INV>(a[13]), u1 = w16_1_unscaled<INV>(a[15]);
     const double2 p2 = w8_3_unscaled<INV>(a[14]);
-    const double2 b3 = twmul<INV>(a[15], make_double2(-c16, s16));
     const double2 t0 = fma_c(kC8, p2, a[12]), t1 = fma_c(-kC8, p2, a[12]);
-    const double2 t2 = cadd(b1, b3), t3 = mul_w4<INV>(csub(b1, b3));
-    X[3] = cadd(t0, t2); X[11] = csub(t0, t2); X[7] = cadd(t1, t3); X[15] = csub(t1, t3);
+    const double2 sp = csub(u3, u1), dm = mul_w4<INV>(cadd(u3, u1));
+    X[3] = fma_c(kC16, sp, t0); X[11] = fma_c(-kC16, sp, t0);
+    X[7] = fma_c(kC16, dm, t1); X[15] = fma_c(-kC16, dm, t1);
   }
 #pragma unroll
   for (int k = 0; k < 16; ++k) a[k] = X[k];
 }
 
 template <int RP, bool INV>
+GT_HD_INL void dft_pairs(const double2* s, const double2* d, double2* a) {
+  if constexpr (RP == 2) {
+    a[0] = s[0];
+    a[1] = d[0];
+  } else if constexpr (RP == 4) {
+    const double2 t3 = mul_w4<INV>(d[1]);
+    a[0] = cadd(s[0], s[1]); a[2] = csub(s[0], s[1]);
+    a[1] = cadd(d[0], t3); a[3] = csub(d[0], t3);
+  } else if constexpr (RP == 8) {
+    // radix 8 as 2 x radix-4 (even and odd inputs), W8^k twiddles, radix-2 combine
+    const double2 we = mul_w4<INV>(d[2]), wo = mul_w4<INV>(d[3]);
+    const double2 e0 = cadd(s[0], s[2]), e2 = csub(s[0], s[2]), e1 = cadd(d[0], we), e3 = csub(d[0], we);
+    const double2 o0 = cadd(s[1], s[3]), o1 = cadd(d[1], wo), o3 = csub(d[1], wo);
+    const double2 o2 = mul_w4<INV>(csub(s[1], s[3]));
+    const double2 p1 = w8_1_unscaled<INV>(o1);
+    const double2 p3 = w8_3_unscaled<INV>(o3);
+    a[0] = cadd(e0, o0); a[4] = csub(e0, o0);
+    a[1] = fma_c(kC8, p1, e1); a[5] = fma_c(-kC8, p1, e1);
+    a[2] = cadd(e2, o2); a[6] = csub(e2, o2);
+    a[3] = fma_c(kC8, p3, e3); a[7] = fma_c(-kC8, p3, e3);
+  } else if constexpr (RP == 16) {
+    // first stage: the radix-4 of inputs (n1, n1+4, n1+8, n1+12) from pairs n1 and n1+4
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) {
+      const double2 t3 = mul_w4<INV>(d[n1 + 4]);
+      a[n1] = cadd(s[n1], s[n1 + 4]);
+      a[n1 + 8] = csub(s[n1], s[n1 + 4]);
+      a[n1 + 4] = cadd(d[n1], t3);
+      a[n1 + 12] = csub(d[n1], t3);
+    }
+    dft16_stage2<INV>(a);
+  } else {
+    static_assert(RP == 2, "unsupported radix");
+  }
+}
+
+// Plain radix-RP DFT of a[0..RP), natural order in and out.
+template <int RP, bool INV>
 GT_HD_INL void dft(double2* a) {
-  if constexpr (RP == 2) dft2<INV>(a[0], a[1]);
-  else if constexpr (RP == 4) dft4<INV>(a[0], a[1], a[2], a[3]);
-  else if constexpr (RP == 8) dft8<INV>(a);
-  else if constexpr (RP == 16) dft16<INV>(a);
-  else static_assert(RP == 1, "unsupported radix");
+  constexpr int H = RP / 2;
+  double2 s[H], d[H];
+#pragma unroll
+  for (int r = 0; r < H; ++r) {
+    s[r] = cadd(a[r], a[r + H]);
+    d[r] = csub(a[r], a[r + H]);
+  }
+  dft_pairs<RP, INV>(s, d, a);
+}
+
+// Radix-RP DFT of the twiddled inputs a_r w_r (a_r conj(w_r) for the inverse), w_0 = 1:
+//   wl[r], 0 < r < RP/2 : w_r
+//   lh[r], r < RP/2     : w_{r+RP/2} in Linzer-Feig form (c, t), w = c (1 + i t)
+// The lower twiddle is an ordinary product; the upper one is mul_1pit with its c folded into the
+// pair's sum and difference, a_r w_r +- c y.
+template <int RP, bool INV>
+GT_HD_INL void dft_tw(double2* a, const double2* wl, const double2* lh) {
+  constexpr int H = RP / 2;
+  double2 s[H], d[H];
+#pragma unroll
+  for (int r = 0; r < H; ++r) {
+    const double2 lo = (r == 0) ? a[0] : twmul<INV>(a[r], wl[r]);
+    const double2 y = mul_1pit(a[r + H], INV ? -lh[r].y : lh[r].y);
+    s[r] = fma_c(lh[r].x, y, lo);
+    d[r] = fma_c(-lh[r].x, y, lo);
+  }
+  dft_pairs<RP, INV>(s, d, a);
 }
 
 // One Stockham pass (radix RP = min(R, L/Ns)) and, recursively, the rest of the transform.
 //   v   : the thread's R values, v[s] = x[t + s*T]; on return X[t + s*T] (natural order)
 //   sm  : exchange buffer; element o lives at sm[padix(o) * SS]
-//   tw  : table exp(-2 pi i k / (L << twshift)), k in [0, L << twshift)
+//   tw  : twiddle table of n = L << twshift entries and their Linzer-Feig forms:
+//         tw[k] = exp(-2 pi i k / n) and tw[n + k] = (c, t) with tw[k] = c (1 + i t), k < n
 template <int L, int R, int Ns, bool INV, int SS>
 struct StockhamPass {
   static constexpr int RP = (L / Ns >= R) ? R : (L / Ns);
@@ -175,13 +228,17 @@ struct StockhamPass {
 #pragma unroll
       for (int r = 0; r < RP; ++r) a[r] = v[m + r * NB];
       if constexpr (Ns > 1) {
+        constexpr int H = RP / 2, STRIDE = L / (Ns * RP);
+        const double2* __restrict__ lf = tw + (L << twshift);
+        double2 wl[H], lh[H];
 #pragma unroll
-        for (int r = 1; r < RP; ++r) {
-          const double2 w = __ldg(&tw[(r * k * (L / (Ns * RP))) << twshift]);
-          a[r] = twmul<INV>(a[r], w);
-        }
+        for (int r = 1; r < H; ++r) wl[r] = __ldg(&tw[(r * k * STRIDE) << twshift]);
+#pragma unroll
+        for (int r = 0; r < H; ++r) lh[r] = __ldg(&lf[((r + H) * k * STRIDE) << twshift]);
+        dft_tw<RP, INV>(a, wl, lh);
+      } else {
+        dft<RP, INV>(a);
       }
-      dft<RP, INV>(a);
       if constexpr (LAST) {
 #pragma unroll
         for (int r = 0; r < RP; ++r) v[m + r * NB] = a[r];

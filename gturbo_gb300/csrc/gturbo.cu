@@ -172,9 +172,13 @@ bool pow2_in_range(int n) { return n >= 16 && n <= 8192 && (n & (n - 1)) == 0; }
 // The row variant that goes with column variant v in gt_set_variant: the same launch variant.
 int natural_row_variant(int v) { return v; }
 
-// exp(-2 pi i k / n) for k in [0, n), each value from an argument reduced to [0, pi/4].
+// exp(-2 pi i k / n) for k in [0, n), each value from an argument reduced to [0, pi/4], then
+// the Linzer-Feig forms tw[n + k] = (c, t) with tw[k] = c (1 + i t) that the FFT passes read for
+// the upper half of their twiddles. c = Re tw[k], except at k = n/4 and 3n/4 (Re tw[k] = 0),
+// where c = 2^-60 and t = Im tw[k] / c = -+2^60: c t is exact and Re(c (1 + i t)) = 2^-60 is far
+// below the rounding of the other entries.
 void make_twiddles(int n, std::vector<double2>& tw) {
-  tw.resize(n);
+  tw.resize(2 * (size_t)n);
   const double twopi = 2.0 * 3.14159265358979323846;
   const int q4 = n / 4;
   for (int k = 0; k < n; ++k) {
@@ -195,6 +199,10 @@ void make_twiddles(int n, std::vector<double2>& tw) {
       default: C = s; S = -c; break;
     }
     tw[k] = make_double2(C, -S);
+  }
+  for (int k = 0; k < n; ++k) {
+    const double c = tw[k].x != 0.0 ? tw[k].x : std::ldexp(1.0, -60);
+    tw[n + k] = make_double2(c, tw[k].y / c);
   }
 }
 

@@ -29,6 +29,47 @@ static double check(std::mt19937_64& rng) {
   return worst;
 }
 
+// The twiddled butterfly of the Stockham passes, dft_tw, against a naive DFT of the twiddled
+// inputs a_r w^r (conjugated for the inverse), for twiddles w = exp(-2 pi i k / n) built the way
+// the solver's table is (including the angles pi/2 and 3pi/2, whose cosine is 0).
+template <int R, bool INV>
+static double check_twiddled(std::mt19937_64& rng) {
+  std::normal_distribution<double> nd;
+  const int n = 64 * R;
+  double worst = 0.0;
+  for (int k = 0; k < 64; ++k) {
+    double2 a[R], x[R], wl[R / 2], lh[R / 2];
+    for (int r = 0; r < R; ++r) x[r] = a[r] = make_double2(nd(rng), nd(rng));
+    auto tw = [&](int m, double2& w, double2& lf) {
+      m %= n;
+      const long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)m / n;
+      double c = (m == n / 4 || m == 3 * n / 4) ? 0.0 : (double)cosl(ang);
+      double s = (m == 0 || m == n / 2) ? 0.0 : (double)sinl(ang);
+      w = make_double2(c, s);
+      const double cl = c != 0.0 ? c : std::ldexp(1.0, -60);
+      lf = make_double2(cl, s / cl);
+    };
+    double2 dummy;
+    for (int r = 0; r < R / 2; ++r) {
+      tw(r * k, wl[r], dummy);
+      tw((r + R / 2) * k, dummy, lh[r]);
+    }
+    gt::dft_tw<R, INV>(a, wl, lh);
+    const long double sg = INV ? 1.0L : -1.0L, pi2 = 2.0L * 3.14159265358979323846264338327950288L;
+    for (int q = 0; q < R; ++q) {
+      long double re = 0, im = 0;
+      for (int r = 0; r < R; ++r) {
+        // twiddle w^r = exp(sg i 2 pi r k / n), then the DFT kernel exp(sg i 2 pi q r / R)
+        const long double ang = sg * pi2 * ((long double)(r * k % n) / n + (long double)((q * r) % R) / R);
+        re += x[r].x * cosl(ang) - x[r].y * sinl(ang);
+        im += x[r].x * sinl(ang) + x[r].y * cosl(ang);
+      }
+      worst = std::fmax(worst, std::hypot((double)(a[q].x - re), (double)(a[q].y - im)));
+    }
+  }
+  return worst;
+}
+
 // twmul (a w forward, a conj(w) inverse) and pack_c2r (s + i conj(w) d) against long double
 static double check_products(std::mt19937_64& rng) {
   std::normal_distribution<double> nd;
@@ -57,6 +98,14 @@ int main() {
   for (int k = 0; k < 8; ++k) {
     std::printf("radix %s max err %.3e\n", names[k], e[k]);
     if (!(e[k] < 1e-14)) bad = 1;
+  }
+  const double et[8] = {check_twiddled<2, false>(rng), check_twiddled<2, true>(rng),
+                        check_twiddled<4, false>(rng), check_twiddled<4, true>(rng),
+                        check_twiddled<8, false>(rng), check_twiddled<8, true>(rng),
+                        check_twiddled<16, false>(rng), check_twiddled<16, true>(rng)};
+  for (int k = 0; k < 8; ++k) {
+    std::printf("twiddled radix %s max err %.3e\n", names[k], et[k]);
+    if (!(et[k] < 1e-14)) bad = 1;
   }
   const double ep = check_products(rng);
   std::printf("twmul / pack_c2r max err %.3e\n", ep);
