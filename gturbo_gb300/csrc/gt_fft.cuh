@@ -174,15 +174,29 @@ GT_HD_INL void dft_pairs(const double2* s, const double2* d, double2* a) {
   }
 }
 
-// Plain radix-RP DFT of a[0..RP), natural order in and out.
-template <int RP, bool INV>
+// The zero band of a first radix pass: inputs a[r] = x[t + r T] (T = L/RP) with r T in
+// [3L/8, 5L/8). A spectrum cut below 3L/8 on both sides of L/2 (the 2/3 rule keeps |k| <= L/3) is
+// zero there for every t: r in [6, 10) for RP = 16, [3, 5) for RP = 8, none below.
+__host__ __device__ constexpr bool in_zband(int rp, int r) { return 8 * r >= 3 * rp && 8 * (r + 1) <= 5 * rp; }
+
+// Plain radix-RP DFT of a[0..RP), natural order in and out. ZB: the zero-band inputs are known
+// to be zero, and their additions are left out (16 of the 144 FP64 instructions of radix 16).
+template <int RP, bool INV, bool ZB = false>
 GT_HD_INL void dft(double2* a) {
   constexpr int H = RP / 2;
   double2 s[H], d[H];
 #pragma unroll
   for (int r = 0; r < H; ++r) {
-    s[r] = cadd(a[r], a[r + H]);
-    d[r] = csub(a[r], a[r + H]);
+    if (ZB && in_zband(RP, r + H)) {
+      s[r] = a[r];
+      d[r] = a[r];
+    } else if (ZB && in_zband(RP, r)) {
+      s[r] = a[r + H];
+      d[r] = make_double2(-a[r + H].x, -a[r + H].y);
+    } else {
+      s[r] = cadd(a[r], a[r + H]);
+      d[r] = csub(a[r], a[r + H]);
+    }
   }
   dft_pairs<RP, INV>(s, d, a);
 }
@@ -219,7 +233,8 @@ struct StockhamPass {
   static constexpr int NB = R / RP;
 
   __device__ __forceinline__ static void run(double2 (&v)[R], double2* sm, int t,
-                                             const double2* __restrict__ tw, int twshift) {
+                                             const double2* __restrict__ tw, int twshift,
+                                             bool zband) {
 #pragma unroll
     for (int m = 0; m < NB; ++m) {
       const int b = t + m * T;
@@ -236,6 +251,8 @@ struct StockhamPass {
 #pragma unroll
         for (int r = 0; r < H; ++r) lh[r] = __ldg(&lf[((r + H) * k * STRIDE) << twshift]);
         dft_tw<RP, INV>(a, wl, lh);
+      } else if (NB == 1 && zband) {
+        dft<RP, INV, true>(a);
       } else {
         dft<RP, INV>(a);
       }
@@ -253,18 +270,20 @@ struct StockhamPass {
 #pragma unroll
       for (int s = 0; s < R; ++s) v[s] = sm[padix(t + s * T) * SS];
       __syncthreads();
-      StockhamPass<L, R, Ns * RP, INV, SS>::run(v, sm, t, tw, twshift);
+      StockhamPass<L, R, Ns * RP, INV, SS>::run(v, sm, t, tw, twshift, false);
     }
   }
 };
 
 // Full transform of length L held as R values per thread (see StockhamPass). Every thread of
 // the block must call it, from the same call site (it contains __syncthreads when L > R).
+// zband (uniform over the block): the inputs x[j], j in [3L/8, 5L/8), are zero (see in_zband).
 template <int L, int R, bool INV, int SS>
 __device__ __forceinline__ void fft_regs(double2 (&v)[R], double2* sm, int t,
-                                         const double2* __restrict__ tw, int twshift) {
+                                         const double2* __restrict__ tw, int twshift,
+                                         bool zband = false) {
   static_assert((L & (L - 1)) == 0 && L >= R, "L must be a power of two >= R");
-  StockhamPass<L, R, 1, INV, SS>::run(v, sm, t, tw, twshift);
+  StockhamPass<L, R, 1, INV, SS>::run(v, sm, t, tw, twshift, zband);
 }
 
 }  // namespace gt

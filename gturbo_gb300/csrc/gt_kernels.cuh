@@ -122,6 +122,27 @@ struct Shape {
 
 __device__ __forceinline__ double2 czero() { return make_double2(0.0, 0.0); }
 
+// 1 unless both parts are +-0 (integer test of the bit patterns)
+__device__ __forceinline__ int nonzero2(double2 a) {
+  return ((__double_as_longlong(a.x) | __double_as_longlong(a.y)) << 1) != 0;
+}
+
+// Zero-band test of a column pass A: the rows j in [3N/8, 5N/8) of a truncated field are zero in
+// every column (|ky| <= N/3), so the first radix pass of the column's inverse transforms can leave
+// them out. Tested on the loaded values, because a caller may pass an untruncated field.
+template <int R>
+__device__ __forceinline__ bool column_zband(const double2 (&v)[R]) {
+  if constexpr (R < 8) {
+    return false;  // no zero band for radix 4
+  } else {
+    int bz = 0;
+#pragma unroll
+    for (int s = 0; s < R; ++s)
+      if (in_zband(R, s)) bz |= nonzero2(v[s]);
+    return !__syncthreads_or(bz);
+  }
+}
+
 // Minimum resident CTAs per SM requested from ptxas (register budget) for N >= 1024: up to
 // GT_*_MINB, but never so many that a thread gets fewer than GT_*_REGS registers. The CTA grows
 // with N (N/16 threads per row or column): 3 column / 2 row CTAs at 2048^2 (168 / 255
@@ -217,6 +238,7 @@ __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
     return;
   }
   if (nz) atomicExch(a.flag, 1);
+  const bool zb = column_zband<R>(v);
   const double kx = __ldg(&a.fkx[ic]);
   // u = i ky/|k|^a q  (nlt.f90:29-32)
 #pragma unroll
@@ -225,7 +247,7 @@ __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
     const double m = __ldg(&a.fky[j]) * __ldg(&a.kainv[(size_t)j * NH + ic]);
     v[s] = make_double2(-m * v[s].y, m * v[s].x);
   }
-  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0);
+  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
   if (valid) {
 #pragma unroll
     for (int s = 0; s < R; ++s) a.u[(size_t)(t + s * T) * NH + i] = v[s];
@@ -239,7 +261,7 @@ __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
     v[s] = make_double2(m * q.y, -m * q.x);
   }
   __syncthreads();
-  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0);
+  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
   if (valid) {
 #pragma unroll
     for (int s = 0; s < R; ++s) a.v[(size_t)(t + s * T) * NH + i] = v[s];
@@ -248,7 +270,7 @@ __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
 #pragma unroll
   for (int s = 0; s < R; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
   __syncthreads();
-  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0);
+  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
   if (valid) {
 #pragma unroll
     for (int s = 0; s < R; ++s) a.q[(size_t)(t + s * T) * NH + i] = v[s];
@@ -313,12 +335,12 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
       for (int s = 0; s < R / 2; ++s) a.phys_q[(size_t)y * M + t + s * T] = h[s];
     }
   }
-  // u + i v: inverse length-N transform
+  // u + i v: inverse length-N transform; C[k] = 0 for kl < k < N - kl
   double2 v[R];
 #pragma unroll
   for (int s = 0; s < R; ++s) v[s] = cs[padix(t + s * T)];
   __syncthreads();
-  fft_regs<N, R, true, 1>(v, cs, t, a.tw, 0);
+  fft_regs<N, R, true, 1>(v, cs, t, a.tw, 0, 8 * kl < 3 * N);
   __syncthreads();
   if (a.phys_uv) {
 #pragma unroll
@@ -453,6 +475,7 @@ __device__ __forceinline__ void colinv_grp_tile(const NltArgs& a, int tile) {
     return;
   }
   if (nz) atomicExch(a.flag, 1);
+  const bool zb = column_zband<R>(v);
   if (g == 0) {  // u = i ky/|k|^a q  (nlt.f90:29-32)
 #pragma unroll
     for (int s = 0; s < R; ++s) {
@@ -469,7 +492,7 @@ __device__ __forceinline__ void colinv_grp_tile(const NltArgs& a, int tile) {
       v[s] = make_double2(m * v[s].y, -m * v[s].x);
     }
   }
-  fft_regs<N, R, true, 1>(v, sm, t, a.tw, 0);
+  fft_regs<N, R, true, 1>(v, sm, t, a.tw, 0, zb);
   __syncthreads();  // every load of zin is done before q (which may alias it) is written
   double2* dst = g == 0 ? a.u : g == 1 ? a.v : a.q;
 #pragma unroll
@@ -564,7 +587,7 @@ __device__ __forceinline__ void row_grp_tile(const NltArgs& a, int tile) {
 #pragma unroll
   for (int s = 0; s < R; ++s) v[s] = buf[padix(t + s * T)];
   __syncthreads();
-  fft_regs<N, R, true, 1>(v, buf, t, a.tw, 0);  // both groups
+  fft_regs<N, R, true, 1>(v, buf, t, a.tw, 0, 8 * kl < 3 * N);  // both groups
   // group 0 holds u + i v, group 1 holds q (real part) at x = t + s*T
   __syncthreads();
   if (g == 1) {
