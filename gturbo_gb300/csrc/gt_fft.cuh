@@ -94,44 +94,75 @@ GT_HD_INL double2 w16_3_unscaled(double2 a) {
 // Linzer-Feig form of the upper twiddle.
 
 // Radix 16 as 4 x radix-4 with W16^(n1*k2) twiddles (b[n1][k2] = a[n1 + 4 k2] after the first
-// stage, X[k2 + 4 k1] from the second).
-template <bool INV>
-GT_HD_INL void dft16_stage2(double2* a) {
+// stage, X[k2 + 4 k1] from the second). SCALED: b[n1][k2] carries the factor c_n1 (c_0 = 1) of
+// the first stage, and sc = {c1, c2, mu = c3/c1, c2 cos(pi/4), c1 cos(pi/8), c1 cos(pi/4)} folds
+// it into the FMAs of the second stage (no extra instruction).
+template <bool INV, bool SCALED = false>
+GT_HD_INL void dft16_stage2(double2* a, const double* sc = nullptr) {
+  // multipliers of the W8 fold on b2 (k2 = 1, 3), of c16 (k2 = 1, 3) and of the W8 fold on b1, b3
+  // (k2 = 2)
+  double c1 = 1.0, c2 = 1.0, mu = 1.0, f8b2 = kC8, f16 = kC16, f8b1 = kC8;
+  if constexpr (SCALED) {
+    c1 = sc[0]; c2 = sc[1]; mu = sc[2]; f8b2 = sc[3]; f16 = sc[4]; f8b1 = sc[5];
+  }
   double2 X[16];
   // k2 = 0: no twiddles
   {
-    double2 t0 = cadd(a[0], a[2]), t1 = csub(a[0], a[2]);
-    double2 t2 = cadd(a[1], a[3]), t3 = mul_w4<INV>(csub(a[1], a[3]));
-    X[0] = cadd(t0, t2); X[8] = csub(t0, t2); X[4] = cadd(t1, t3); X[12] = csub(t1, t3);
+    double2 t0, t1, t2, t3;
+    if constexpr (SCALED) {
+      t0 = fma_c(c2, a[2], a[0]); t1 = fma_c(-c2, a[2], a[0]);
+      t2 = fma_c(mu, a[3], a[1]); t3 = mul_w4<INV>(fma_c(-mu, a[3], a[1]));
+      X[0] = fma_c(c1, t2, t0); X[8] = fma_c(-c1, t2, t0); X[4] = fma_c(c1, t3, t1); X[12] = fma_c(-c1, t3, t1);
+    } else {
+      t0 = cadd(a[0], a[2]); t1 = csub(a[0], a[2]);
+      t2 = cadd(a[1], a[3]); t3 = mul_w4<INV>(csub(a[1], a[3]));
+      X[0] = cadd(t0, t2); X[8] = csub(t0, t2); X[4] = cadd(t1, t3); X[12] = csub(t1, t3);
+    }
   }
   // k2 = 1: (b0, W16^1 b1, W16^2 b2, W16^3 b3). W16^1 b1 + W16^3 b3 = c16 (u1 + u3) with u1, u3 the
   // unscaled products; c16 and the c of W16^2 = W8^1 are folded into the output FMAs.
   {
     const double2 u1 = w16_1_unscaled<INV>(a[5]), u3 = w16_3_unscaled<INV>(a[7]);
     const double2 p2 = w8_1_unscaled<INV>(a[6]);
-    const double2 t0 = fma_c(kC8, p2, a[4]), t1 = fma_c(-kC8, p2, a[4]);
-    const double2 sp = cadd(u1, u3), dm = mul_w4<INV>(csub(u1, u3));
-    X[1] = fma_c(kC16, sp, t0); X[9] = fma_c(-kC16, sp, t0);
-    X[5] = fma_c(kC16, dm, t1); X[13] = fma_c(-kC16, dm, t1);
+    const double2 t0 = fma_c(f8b2, p2, a[4]), t1 = fma_c(-f8b2, p2, a[4]);
+    double2 sp, dm;
+    if constexpr (SCALED) {
+      sp = fma_c(mu, u3, u1); dm = mul_w4<INV>(fma_c(-mu, u3, u1));
+    } else {
+      sp = cadd(u1, u3); dm = mul_w4<INV>(csub(u1, u3));
+    }
+    X[1] = fma_c(f16, sp, t0); X[9] = fma_c(-f16, sp, t0);
+    X[5] = fma_c(f16, dm, t1); X[13] = fma_c(-f16, dm, t1);
   }
   // k2 = 2: (b0, W8^1 b1, W4 b2, W8^3 b3); both W8 factors share c: c (P1 +- P3)
   {
     const double2 p1 = w8_1_unscaled<INV>(a[9]);
     const double2 b2 = mul_w4<INV>(a[10]);
     const double2 p3 = w8_3_unscaled<INV>(a[11]);
-    const double2 t0 = cadd(a[8], b2), t1 = csub(a[8], b2);
-    const double2 sp = cadd(p1, p3), dm = mul_w4<INV>(csub(p1, p3));
-    X[2] = fma_c(kC8, sp, t0); X[10] = fma_c(-kC8, sp, t0);
-    X[6] = fma_c(kC8, dm, t1); X[14] = fma_c(-kC8, dm, t1);
+    double2 t0, t1, sp, dm;
+    if constexpr (SCALED) {
+      t0 = fma_c(c2, b2, a[8]); t1 = fma_c(-c2, b2, a[8]);
+      sp = fma_c(mu, p3, p1); dm = mul_w4<INV>(fma_c(-mu, p3, p1));
+    } else {
+      t0 = cadd(a[8], b2); t1 = csub(a[8], b2);
+      sp = cadd(p1, p3); dm = mul_w4<INV>(csub(p1, p3));
+    }
+    X[2] = fma_c(f8b1, sp, t0); X[10] = fma_c(-f8b1, sp, t0);
+    X[6] = fma_c(f8b1, dm, t1); X[14] = fma_c(-f8b1, dm, t1);
   }
   // k2 = 3: (b0, W16^3 b1, W16^6 b2, W16^9 b3) with W16^9 = -W16^1: c16 (u3 - u1)
   {
     const double2 u3 = w16_3_unscaled<INV>(a[13]), u1 = w16_1_unscaled<INV>(a[15]);
     const double2 p2 = w8_3_unscaled<INV>(a[14]);
-    const double2 t0 = fma_c(kC8, p2, a[12]), t1 = fma_c(-kC8, p2, a[12]);
-    const double2 sp = csub(u3, u1), dm = mul_w4<INV>(cadd(u3, u1));
-    X[3] = fma_c(kC16, sp, t0); X[11] = fma_c(-kC16, sp, t0);
-    X[7] = fma_c(kC16, dm, t1); X[15] = fma_c(-kC16, dm, t1);
+    const double2 t0 = fma_c(f8b2, p2, a[12]), t1 = fma_c(-f8b2, p2, a[12]);
+    double2 sp, dm;
+    if constexpr (SCALED) {
+      sp = fma_c(-mu, u1, u3); dm = mul_w4<INV>(fma_c(mu, u1, u3));
+    } else {
+      sp = csub(u3, u1); dm = mul_w4<INV>(cadd(u3, u1));
+    }
+    X[3] = fma_c(f16, sp, t0); X[11] = fma_c(-f16, sp, t0);
+    X[7] = fma_c(f16, dm, t1); X[15] = fma_c(-f16, dm, t1);
   }
 #pragma unroll
   for (int k = 0; k < 16; ++k) a[k] = X[k];
@@ -220,11 +251,114 @@ GT_HD_INL void dft_tw(double2* a, const double2* wl, const double2* lh) {
   dft_pairs<RP, INV>(s, d, a);
 }
 
+// ---- twiddled butterflies with carried scales (Linzer and Feig, every level) -------------------
+// The pass tables hold, for each base angle m of a radix-RP pass (twiddles w_r = W^(r m),
+// W = exp(-2 pi i / n), written w_r = c_r (1 + i t_r) as in the Linzer-Feig half of the twiddle
+// table, c_0 = 1, t_0 = 0), an entry of lf_entry_doubles(RP) doubles:
+//   e[r - 1]        t_r                 r = 1 .. RP-1
+//   e[RP - 1 + r]   rho_r = c_{r+H}/c_r  r < H = RP/2
+//   then RP = 16: sig_g = c_{g+4}/c_g (g < 4), c1, c2, c3/c1, c2 cos(pi/4), c1 cos(pi/8), c1 cos(pi/4)
+//        RP = 8:  c2, c1, c3/c1, c1 cos(pi/4)
+//        RP = 4:  c1
+// Every twiddle is y_r = a_r (1 + i t_r), two FMAs. The sum and difference of pair (r, r+H) are
+// y_r +- rho_r y_{r+H} and carry the factor c_r; the ratios and products above let every later
+// addition absorb those factors as an FMA multiplier. Per thread and butterfly this takes radix 16
+// from 188 to 174 FP64 instructions, radix 8 from 72 to 66 and radix 4 from 24 to 22.
+__host__ __device__ constexpr int lf_entry_doubles(int rp) { return rp == 16 ? 34 : rp == 8 ? 16 : rp == 4 ? 6 : 0; }
+// Offset (in double2) of the radix-rp pass table in the twiddle buffer of a length-n table.
+__host__ __device__ constexpr int lf_table_offset(int rp, int n) {
+  return 2 * n + (rp <= 8 ? (n / 16) * (lf_entry_doubles(16) / 2) : 0) +
+         (rp <= 4 ? (n / 8) * (lf_entry_doubles(8) / 2) : 0);
+}
+// Number of double2 in the whole twiddle buffer of a length-n table.
+__host__ __device__ constexpr int twiddle_buffer_size(int n) {
+  return lf_table_offset(4, n) + (n / 4) * (lf_entry_doubles(4) / 2);
+}
+
+// The pass-table entry of base angle m (host side): lf[j] = (c_j, t_j), j < n, the Linzer-Feig
+// half of the twiddle table. Ratios are formed in long double from the stored c.
+template <int RP>
+inline void make_lf_entry(const double2* lf, int n, int m, double* e) {
+  constexpr int H = RP / 2;
+  long double c[RP];
+  for (int r = 0; r < RP; ++r) {
+    const double2 ct = lf[(int)(((long long)r * m) % n)];
+    c[r] = ct.x;
+    if (r > 0) e[r - 1] = ct.y;
+  }
+  for (int r = 0; r < H; ++r) e[RP - 1 + r] = (double)(c[r + H] / c[r]);
+  double* x = e + RP - 1 + H;
+  if constexpr (RP == 16) {
+    for (int g = 0; g < 4; ++g) x[g] = (double)(c[g + 4] / c[g]);
+    x[4] = (double)c[1];
+    x[5] = (double)c[2];
+    x[6] = (double)(c[3] / c[1]);
+    x[7] = (double)(c[2] * (long double)kC8);
+    x[8] = (double)(c[1] * (long double)kC16);
+    x[9] = (double)(c[1] * (long double)kC8);
+    x[10] = 0.0;  // padding
+  } else if constexpr (RP == 8) {
+    x[0] = (double)c[2];
+    x[1] = (double)c[1];
+    x[2] = (double)(c[3] / c[1]);
+    x[3] = (double)(c[1] * (long double)kC8);
+    x[4] = 0.0;  // padding
+  } else if constexpr (RP == 4) {
+    x[0] = (double)c[1];
+  }
+}
+
+template <int RP, bool INV>
+GT_HD_INL void dft_lf(double2* a, const double* e) {
+  static_assert(RP == 4 || RP == 8 || RP == 16, "carried-scale butterflies exist for radix 4, 8, 16");
+  constexpr int H = RP / 2;
+  double2 s[H], d[H];
+#pragma unroll
+  for (int r = 0; r < H; ++r) {
+    const double2 lo = (r == 0) ? a[0] : mul_1pit(a[r], INV ? -e[r - 1] : e[r - 1]);
+    const double2 hi = mul_1pit(a[r + H], INV ? -e[r + H - 1] : e[r + H - 1]);
+    const double rho = e[RP - 1 + r];
+    s[r] = fma_c(rho, hi, lo);
+    d[r] = fma_c(-rho, hi, lo);
+  }
+  const double* x = e + RP - 1 + H;
+  if constexpr (RP == 4) {
+    const double c1 = x[0];
+    const double2 t3 = mul_w4<INV>(d[1]);
+    a[0] = fma_c(c1, s[1], s[0]); a[2] = fma_c(-c1, s[1], s[0]);
+    a[1] = fma_c(c1, t3, d[0]); a[3] = fma_c(-c1, t3, d[0]);
+  } else if constexpr (RP == 8) {
+    const double c2 = x[0], c1 = x[1], mu = x[2], c1k = x[3];
+    const double2 we = mul_w4<INV>(d[2]), wo = mul_w4<INV>(d[3]);
+    const double2 e0 = fma_c(c2, s[2], s[0]), e2 = fma_c(-c2, s[2], s[0]);
+    const double2 e1 = fma_c(c2, we, d[0]), e3 = fma_c(-c2, we, d[0]);
+    const double2 o0 = fma_c(mu, s[3], s[1]), o2 = mul_w4<INV>(fma_c(-mu, s[3], s[1]));
+    const double2 o1 = fma_c(mu, wo, d[1]), o3 = fma_c(-mu, wo, d[1]);
+    const double2 p1 = w8_1_unscaled<INV>(o1), p3 = w8_3_unscaled<INV>(o3);
+    a[0] = fma_c(c1, o0, e0); a[4] = fma_c(-c1, o0, e0);
+    a[2] = fma_c(c1, o2, e2); a[6] = fma_c(-c1, o2, e2);
+    a[1] = fma_c(c1k, p1, e1); a[5] = fma_c(-c1k, p1, e1);
+    a[3] = fma_c(c1k, p3, e3); a[7] = fma_c(-c1k, p3, e3);
+  } else {
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) {
+      const double sig = x[n1];
+      const double2 t3 = mul_w4<INV>(d[n1 + 4]);
+      a[n1] = fma_c(sig, s[n1 + 4], s[n1]);
+      a[n1 + 8] = fma_c(-sig, s[n1 + 4], s[n1]);
+      a[n1 + 4] = fma_c(sig, t3, d[n1]);
+      a[n1 + 12] = fma_c(-sig, t3, d[n1]);
+    }
+    dft16_stage2<INV, true>(a, x + 4);
+  }
+}
+
 // One Stockham pass (radix RP = min(R, L/Ns)) and, recursively, the rest of the transform.
 //   v   : the thread's R values, v[s] = x[t + s*T]; on return X[t + s*T] (natural order)
 //   sm  : exchange buffer; element o lives at sm[padix(o) * SS]
-//   tw  : twiddle table of n = L << twshift entries and their Linzer-Feig forms:
-//         tw[k] = exp(-2 pi i k / n) and tw[n + k] = (c, t) with tw[k] = c (1 + i t), k < n
+//   tw  : twiddle buffer of a length-n table, n = L << twshift: tw[k] = exp(-2 pi i k / n) and
+//         tw[n + k] = (c, t) with tw[k] = c (1 + i t), k < n, then the pass tables of dft_lf
+//         (lf_table_offset; twiddle_buffer_size(n) double2 in all)
 template <int L, int R, int Ns, bool INV, int SS>
 struct StockhamPass {
   static constexpr int RP = (L / Ns >= R) ? R : (L / Ns);
@@ -242,15 +376,22 @@ struct StockhamPass {
       double2 a[RP];
 #pragma unroll
       for (int r = 0; r < RP; ++r) a[r] = v[m + r * NB];
-      if constexpr (Ns > 1) {
-        constexpr int H = RP / 2, STRIDE = L / (Ns * RP);
-        const double2* __restrict__ lf = tw + (L << twshift);
-        double2 wl[H], lh[H];
+      if constexpr (Ns > 1 && RP == 2) {
+        const double2 lh = __ldg(&tw[(L << twshift) + ((k * (L / (Ns * 2))) << twshift)]);
+        dft_tw<2, INV>(a, nullptr, &lh);
+      } else if constexpr (Ns > 1) {
+        constexpr int E = lf_entry_doubles(RP), STRIDE = L / (Ns * RP);
+        const int n = L << twshift;
+        const double2* __restrict__ ent =
+            tw + lf_table_offset(RP, n) + (size_t)((k * STRIDE) << twshift) * (E / 2);
+        double e[E];
 #pragma unroll
-        for (int r = 1; r < H; ++r) wl[r] = __ldg(&tw[(r * k * STRIDE) << twshift]);
-#pragma unroll
-        for (int r = 0; r < H; ++r) lh[r] = __ldg(&lf[((r + H) * k * STRIDE) << twshift]);
-        dft_tw<RP, INV>(a, wl, lh);
+        for (int q = 0; q < E / 2; ++q) {
+          const double2 p = __ldg(&ent[q]);
+          e[2 * q] = p.x;
+          e[2 * q + 1] = p.y;
+        }
+        dft_lf<RP, INV>(a, e);
       } else if (NB == 1 && zband) {
         dft<RP, INV, true>(a);
       } else {

@@ -11,6 +11,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/gturbo.h"
@@ -172,13 +173,14 @@ bool pow2_in_range(int n) { return n >= 16 && n <= 8192 && (n & (n - 1)) == 0; }
 // The row variant that goes with column variant v in gt_set_variant: the same launch variant.
 int natural_row_variant(int v) { return v; }
 
-// exp(-2 pi i k / n) for k in [0, n), each value from an argument reduced to [0, pi/4], then
-// the Linzer-Feig forms tw[n + k] = (c, t) with tw[k] = c (1 + i t) that the FFT passes read for
-// the upper half of their twiddles. c = Re tw[k], except at k = n/4 and 3n/4 (Re tw[k] = 0),
-// where c = 2^-60 and t = Im tw[k] / c = -+2^60: c t is exact and Re(c (1 + i t)) = 2^-60 is far
-// below the rounding of the other entries.
+// The twiddle buffer of the FFT passes (gt_fft.cuh): exp(-2 pi i k / n) for k in [0, n), each
+// value from an argument reduced to [0, pi/4]; then the Linzer-Feig forms tw[n + k] = (c, t) with
+// tw[k] = c (1 + i t); then the radix-16, 8 and 4 pass tables built from those (make_lf_entry).
+// c = Re tw[k], except at k = n/4 and 3n/4 (Re tw[k] = 0), where c = 2^-60 and
+// t = Im tw[k] / c = -+2^60: c t is exact and Re(c (1 + i t)) = 2^-60 is far below the rounding
+// of the other entries.
 void make_twiddles(int n, std::vector<double2>& tw) {
-  tw.resize(2 * (size_t)n);
+  tw.assign((size_t)gt::twiddle_buffer_size(n), make_double2(0.0, 0.0));
   const double twopi = 2.0 * 3.14159265358979323846;
   const int q4 = n / 4;
   for (int k = 0; k < n; ++k) {
@@ -204,6 +206,16 @@ void make_twiddles(int n, std::vector<double2>& tw) {
     const double c = tw[k].x != 0.0 ? tw[k].x : std::ldexp(1.0, -60);
     tw[n + k] = make_double2(c, tw[k].y / c);
   }
+  const double2* lf = tw.data() + n;
+  auto fill = [&](auto rp_tag) {
+    constexpr int RP = decltype(rp_tag)::value;
+    constexpr int E = gt::lf_entry_doubles(RP);
+    double* base = reinterpret_cast<double*>(tw.data() + gt::lf_table_offset(RP, n));
+    for (int m = 0; m < n / RP; ++m) gt::make_lf_entry<RP>(lf, n, m, base + (size_t)m * E);
+  };
+  fill(std::integral_constant<int, 16>());
+  fill(std::integral_constant<int, 8>());
+  fill(std::integral_constant<int, 4>());
 }
 
 template <typename T>

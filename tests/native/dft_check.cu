@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdio>
 #include <random>
+#include <vector>
 
 #include "../../gturbo_gb300/csrc/gt_fft.cuh"
 
@@ -70,6 +71,42 @@ static double check_twiddled(std::mt19937_64& rng) {
   return worst;
 }
 
+// The carried-scale butterflies dft_lf against a naive DFT of the twiddled inputs a_r w^(r m),
+// with the pass-table entries made by the solver's own make_lf_entry from a Linzer-Feig table
+// (c, t) built like the solver's, over every base angle m of a length-n table.
+template <int R, bool INV>
+static double check_lf(std::mt19937_64& rng, int n) {
+  std::normal_distribution<double> nd;
+  const long double pi2 = 2.0L * 3.14159265358979323846264338327950288L;
+  std::vector<double2> lf(n);
+  for (int k = 0; k < n; ++k) {
+    const long double ang = -pi2 * (long double)k / n;
+    const double c = (k == n / 4 || k == 3 * n / 4) ? 0.0 : (double)cosl(ang);
+    const double sn = (k == 0 || k == n / 2) ? 0.0 : (double)sinl(ang);
+    const double cl = c != 0.0 ? c : std::ldexp(1.0, -60);
+    lf[k] = make_double2(cl, sn / cl);
+  }
+  double worst = 0.0;
+  for (int m = 0; m < n / R; ++m) {
+    double e[gt::lf_entry_doubles(R)];
+    gt::make_lf_entry<R>(lf.data(), n, m, e);
+    double2 a[R], x[R];
+    for (int r = 0; r < R; ++r) x[r] = a[r] = make_double2(nd(rng), nd(rng));
+    gt::dft_lf<R, INV>(a, e);
+    const long double sg = INV ? 1.0L : -1.0L;
+    for (int q = 0; q < R; ++q) {
+      long double re = 0, im = 0;
+      for (int r = 0; r < R; ++r) {
+        const long double ang = sg * pi2 * ((long double)((long long)r * m % n) / n + (long double)((q * r) % R) / R);
+        re += x[r].x * cosl(ang) - x[r].y * sinl(ang);
+        im += x[r].x * sinl(ang) + x[r].y * cosl(ang);
+      }
+      worst = std::fmax(worst, std::hypot((double)(a[q].x - re), (double)(a[q].y - im)));
+    }
+  }
+  return worst;
+}
+
 // twmul (a w forward, a conj(w) inverse) and pack_c2r (s + i conj(w) d) against long double
 static double check_products(std::mt19937_64& rng) {
   std::normal_distribution<double> nd;
@@ -107,6 +144,15 @@ int main() {
     std::printf("twiddled radix %s max err %.3e\n", names[k], et[k]);
     if (!(et[k] < 1e-14)) bad = 1;
   }
+  // every base angle of the tables of n = 64 .. 8192 (radix 16, 8, 4; forward and inverse)
+  double el = 0.0;
+  for (int n = 64; n <= 8192; n *= 2) {
+    const double v[6] = {check_lf<16, false>(rng, n), check_lf<16, true>(rng, n), check_lf<8, false>(rng, n),
+                         check_lf<8, true>(rng, n), check_lf<4, false>(rng, n), check_lf<4, true>(rng, n)};
+    for (double x : v) el = std::fmax(el, x);
+  }
+  std::printf("carried-scale radix 16/8/4 max err %.3e\n", el);
+  if (!(el < 1e-14)) bad = 1;
   const double ep = check_products(rng);
   std::printf("twmul / pack_c2r max err %.3e\n", ep);
   if (!(ep < 1e-14)) bad = 1;
