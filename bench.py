@@ -250,8 +250,10 @@ def pass_model(p, kind):
 
 # DRAM bytes (read + write) per launch of a pass, from single-kernel ncu captures
 # (dram__bytes_read.sum + dram__bytes_write.sum) of the same launch variant:
-#   2048^2, variant 0: ncu --set full -k "regex:k_nlt_(row|colfwd_inv|colinv)" -s 52 -c 3
-#                      python bench.py --steps 2 --warmup 3 --no-extras
+#   2048^2, variant 0: ncu --set full -k "regex:k_nlt_(row|colfwd_inv|colinv)" -s 4 -c 3
+#                      python bench.py --steps 2 --warmup 3 --no-extras --variant 0
+#   2048^2, variant 1: ncu --set full -k "regex:k_nltv_(row|colfwd_inv|colinv)" -s 4 -c 3
+#                      python bench.py --steps 2 --warmup 3 --no-extras --variant 1
 #   256^2, column variant 3, row variant 2:
 #                      ncu --set full --kernel-name-base demangled -k "regex:k_nltv_(row<\(int\)256,
 #                      \(int\)2>|colfwd_inv<\(int\)256, \(int\)3>|colinv<\(int\)256, \(int\)3>)" -s 8 -c 3
@@ -259,9 +261,12 @@ def pass_model(p, kind):
 # Keyed by (N, the launch variant of that kernel: the row variant for the row pass, the column
 # variant otherwise, pass).
 NCU_TRAFFIC = {
-    (2048, 0, "nlt_colinv"): 47.07e6 + 18.51e6,
-    (2048, 0, "nlt_row"): 67.99e6 + 1.53e6,
-    (2048, 0, "nlt_colfwd_inv"): 110.95e6 + 41.28e6,
+    (2048, 0, "nlt_colinv"): 50.01e6 + 47.65e6,
+    (2048, 0, "nlt_row"): 68.00e6 + 1.50e6,
+    (2048, 0, "nlt_colfwd_inv"): 111.96e6 + 55.95e6,
+    (2048, 1, "nlt_colinv"): 58.38e6 + 55.84e6,
+    (2048, 1, "nlt_row"): 67.95e6 + 1.47e6,
+    (2048, 1, "nlt_colfwd_inv"): 114.65e6 + 52.83e6,
     (256, 3, "nlt_colinv"): 0.757e6,
     (256, 2, "nlt_row"): 1.177e6,
     (256, 3, "nlt_colfwd_inv"): 1.828e6,

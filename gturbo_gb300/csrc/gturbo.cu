@@ -364,12 +364,12 @@ int gt_create(const gt_params* p, gt_handle** out) {
   h->NBIN = N / 2;
   h->dispatch = dispatch_for(N);
   // The launch variants that timed fastest on GB300 for this grid size (RK2 and RK4 alike).
-  // Columns: grouped with 4 values per thread up to 256^2, 4 values per thread at 512^2, 8 at
-  // 1024^2, 16 from 2048^2 up. Rows: grouped with 4 values per thread up to
-  // 128^2, 4 values per thread at 256^2, 8 at 512^2 and 1024^2, 16 from 2048^2 up.
+  // Columns: grouped with 4 values per thread up to 256^2, 4 values per thread at 512^2 and
+  // 1024^2, 8 at 2048^2, 16 from 4096^2 up. Rows: grouped with 4 values per thread up to
+  // 128^2, 4 values per thread at 256^2 and 512^2, 8 at 1024^2 and 2048^2, 16 from 4096^2 up.
   // gt_autotune re-times.
-  h->variant = N <= 256 ? 3 : N == 512 ? 2 : N == 1024 ? 1 : 0;
-  h->row_variant = N <= 128 ? 3 : N == 256 ? 2 : N <= 1024 ? 1 : 0;
+  h->variant = N <= 256 ? 3 : N <= 1024 ? 2 : N == 2048 ? 1 : 0;
+  h->row_variant = N <= 128 ? 3 : N <= 512 ? 2 : N <= 2048 ? 1 : 0;
   // inieuler.f90:22-36, 237-244
   int split = 0;
   if (p->alpnu < 1.0005 && p->alpnu > 0.9995 && p->alpmu < 0.0005 && p->alpmu > -0.0005) split = 1;
