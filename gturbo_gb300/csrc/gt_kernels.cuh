@@ -293,30 +293,48 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
   const double2* qrow = a.q + (size_t)y * NH;
   const double2* urow = a.u + (size_t)y * NH;
   const double2* vrow = a.v + (size_t)y * NH;
-  // C[k] = U[k] + i V[k], C[N-k] = conj U[k] + i conj V[k]; Im of U, V at k=0, N/2 dropped
+  // C[k] = U[k] + i V[k], C[N-k] = conj U[k] + i conj V[k]; Im of U, V at k=0, N/2 dropped.
+  // Beyond kl the inputs are zero: the branches (uniform within all but one warp) store zeros
+  // without the FP64 additions.
 #pragma unroll
   for (int s = 0; s <= R / 2; ++s) {
     const int k = t + s * T;
     if (k <= M) {
-      const double2 U = (k <= kl) ? urow[k] : czero();
-      const double2 V = (k <= kl) ? vrow[k] : czero();
-      if (k == 0 || k == M) {
-        cs[padix(k)] = make_double2(U.x, V.x);
+      if (k > kl) {
+        cs[padix(k)] = czero();
+        cs[padix(N - k)] = czero();
       } else {
-        cs[padix(k)] = make_double2(U.x - V.y, U.y + V.x);
-        cs[padix(N - k)] = make_double2(U.x + V.y, V.x - U.y);
+        const double2 U = urow[k];
+        const double2 V = vrow[k];
+        if (k == 0 || k == M) {
+          cs[padix(k)] = make_double2(U.x, V.x);
+        } else {
+          cs[padix(k)] = make_double2(U.x - V.y, U.y + V.x);
+          cs[padix(N - k)] = make_double2(U.x + V.y, V.x - U.y);
+        }
       }
     }
   }
-  // Z[k] = (Q[k] + conj Q[M-k]) + i W^-k (Q[k] - conj Q[M-k]), k < M; Im Q[0], Q[M] dropped
+  // Z[k] = (Q[k] + conj Q[M-k]) + i W^-k (Q[k] - conj Q[M-k]), k < M; Im Q[0], Q[M] dropped.
+  // Where only one of Q[k], Q[M-k] lies within kl, the sum and difference need no additions.
 #pragma unroll
   for (int s = 0; s < R / 2; ++s) {
     const int k = t + s * T;
-    double2 p = (k <= kl) ? qrow[k] : czero();
-    double2 b = (M - k <= kl) ? qrow[M - k] : czero();
+    const bool hp = k <= kl, hb = M - k <= kl;
+    double2 p = hp ? qrow[k] : czero();
+    double2 b = hb ? qrow[M - k] : czero();
     if (k == 0) { p.y = 0.0; b.y = 0.0; }
-    const double2 sm_ = make_double2(p.x + b.x, p.y - b.y);
-    const double2 d = make_double2(p.x - b.x, p.y + b.y);
+    double2 sm_, d;
+    if (hp && hb) {
+      sm_ = make_double2(p.x + b.x, p.y - b.y);
+      d = make_double2(p.x - b.x, p.y + b.y);
+    } else if (hp) {
+      sm_ = p;
+      d = p;
+    } else {
+      sm_ = make_double2(b.x, -b.y);
+      d = make_double2(-b.x, b.y);
+    }
     zs[padix(k)] = pack_c2r(sm_, d, __ldg(&a.tw[k]));
   }
   __syncthreads();

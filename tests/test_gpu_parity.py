@@ -446,9 +446,10 @@ def test_variant_rejected_when_unsupported():
     from gturbo_gb300._lib import GturboError
     sol = _solver(_params(2048))
     assert sol.supported_variants() == [0, 1]
+    before = sol.variants
     with pytest.raises(GturboError):
         sol.variant = 2
-    assert sol.variant == 0
+    assert sol.variants == before  # a rejected variant leaves the handle's pair unchanged
 
 
 def test_autotune_and_cache(tmp_path):
