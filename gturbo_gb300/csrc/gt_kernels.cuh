@@ -114,10 +114,6 @@ struct Shape {
   static constexpr int COL_THREADS = COLS * T;
   static constexpr int COL_CTAS = (NH + COLS - 1) / COLS;
   static constexpr size_t COL_SMEM = (size_t)padded(N) * COLS * sizeof(double2);
-  // The nonlinear-term column kernels also keep a stash of COLS*N values (colinv_tile) up to
-  // 2048^2, where three CTAs per SM still fit in shared memory.
-  static constexpr bool STASH = N <= 2048;
-  static constexpr size_t COL_SMEM_NLT = COL_SMEM + (STASH ? (size_t)N * COLS * sizeof(double2) : 0);
   static constexpr int ROWS = (T >= 128) ? 1 : (128 / T > N ? N : 128 / T);
   static constexpr int ROW_THREADS = ROWS * T;
   static constexpr int ROW_CTAS = N / ROWS;
@@ -204,16 +200,9 @@ struct NltArgs {
   double2* phys_q;
 };
 
-// Pass A: inverse y-transforms of u, v and q. zin may alias q, as the reference destroys z;
-// every thread reads and writes the same elements, so it only has to load its values before it
-// stores q.
-//   STASH = false: u, v, q in that order, each re-reading its input from zin and kainv.
-//   STASH = true : psi = q/|k|^a is formed once and kept in the thread's own slots of a
-//                  shared-memory stash (C*N values after the exchange buffer); q is transformed
-//                  first from the registers, then u = i ky psi and v = -i kx psi from the stash.
-//                  The column's strided global loads (16 B of every row) happen once instead of
-//                  three times (zin) and twice (kainv).
-template <int N, int C, int R = 16, bool STASH = false>
+// Pass A: inverse y-transforms of u, v and q (in that order: zin may alias q, as the
+// reference destroys z, so q is re-read from zin before the q column is overwritten).
+template <int N, int C, int R = 16>
 __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
   constexpr int T = N / R, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
@@ -251,82 +240,40 @@ __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
   if (nz) atomicExch(a.flag, 1);
   const bool zb = column_zband<R>(v);
   const double kx = __ldg(&a.fkx[ic]);
-  if constexpr (STASH) {
-    double2* st = smem + (size_t)C * padded(N);
+  // u = i ky/|k|^a q  (nlt.f90:29-32)
 #pragma unroll
-    for (int s = 0; s < R; ++s) {
-      const int j = t + s * T;
-      const double ki = __ldg(&a.kainv[(size_t)j * NH + ic]);
-      st[(size_t)j * C + c] = make_double2(ki * v[s].x, ki * v[s].y);
-    }
-    // q (nlt.f90:41)
-    fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
-    if (valid) {
+  for (int s = 0; s < R; ++s) {
+    const int j = t + s * T;
+    const double m = __ldg(&a.fky[j]) * __ldg(&a.kainv[(size_t)j * NH + ic]);
+    v[s] = make_double2(-m * v[s].y, m * v[s].x);
+  }
+  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
+  if (valid) {
 #pragma unroll
-      for (int s = 0; s < R; ++s) a.q[(size_t)(t + s * T) * NH + i] = v[s];
-    }
-    // u = i ky psi  (nlt.f90:29-32)
+    for (int s = 0; s < R; ++s) a.u[(size_t)(t + s * T) * NH + i] = v[s];
+  }
+  // v = -i kx/|k|^a q  (nlt.f90:33-34)
 #pragma unroll
-    for (int s = 0; s < R; ++s) {
-      const int j = t + s * T;
-      const double2 p = st[(size_t)j * C + c];
-      const double ky = __ldg(&a.fky[j]);
-      v[s] = make_double2(-ky * p.y, ky * p.x);
-    }
-    __syncthreads();
-    fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
-    if (valid) {
+  for (int s = 0; s < R; ++s) {
+    const int j = t + s * T;
+    const double2 q = valid ? zin[(size_t)j * NH + ic] : czero();
+    const double m = kx * __ldg(&a.kainv[(size_t)j * NH + ic]);
+    v[s] = make_double2(m * q.y, -m * q.x);
+  }
+  __syncthreads();
+  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
+  if (valid) {
 #pragma unroll
-      for (int s = 0; s < R; ++s) a.u[(size_t)(t + s * T) * NH + i] = v[s];
-    }
-    // v = -i kx psi  (nlt.f90:33-34)
+    for (int s = 0; s < R; ++s) a.v[(size_t)(t + s * T) * NH + i] = v[s];
+  }
+  // q (nlt.f90:41)
 #pragma unroll
-    for (int s = 0; s < R; ++s) {
-      const double2 p = st[(size_t)(t + s * T) * C + c];
-      v[s] = make_double2(kx * p.y, -kx * p.x);
-    }
-    __syncthreads();
-    fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
-    if (valid) {
+  for (int s = 0; s < R; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
+  __syncthreads();
+  fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
+  if (valid) {
 #pragma unroll
-      for (int s = 0; s < R; ++s) a.v[(size_t)(t + s * T) * NH + i] = v[s];
-    }
-  } else {
-    // u = i ky/|k|^a q  (nlt.f90:29-32)
-#pragma unroll
-    for (int s = 0; s < R; ++s) {
-      const int j = t + s * T;
-      const double m = __ldg(&a.fky[j]) * __ldg(&a.kainv[(size_t)j * NH + ic]);
-      v[s] = make_double2(-m * v[s].y, m * v[s].x);
-    }
-    fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
-    if (valid) {
-#pragma unroll
-      for (int s = 0; s < R; ++s) a.u[(size_t)(t + s * T) * NH + i] = v[s];
-    }
-    // v = -i kx/|k|^a q  (nlt.f90:33-34)
-#pragma unroll
-    for (int s = 0; s < R; ++s) {
-      const int j = t + s * T;
-      const double2 q = valid ? zin[(size_t)j * NH + ic] : czero();
-      const double m = kx * __ldg(&a.kainv[(size_t)j * NH + ic]);
-      v[s] = make_double2(m * q.y, -m * q.x);
-    }
-    __syncthreads();
-    fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
-    if (valid) {
-#pragma unroll
-      for (int s = 0; s < R; ++s) a.v[(size_t)(t + s * T) * NH + i] = v[s];
-    }
-    // q (nlt.f90:41)
-#pragma unroll
-    for (int s = 0; s < R; ++s) v[s] = valid ? zin[(size_t)(t + s * T) * NH + ic] : czero();
-    __syncthreads();
-    fft_regs<N, R, true, C>(v, sm, t, a.tw, 0, zb);
-    if (valid) {
-#pragma unroll
-      for (int s = 0; s < R; ++s) a.q[(size_t)(t + s * T) * NH + i] = v[s];
-    }
+    for (int s = 0; s < R; ++s) a.q[(size_t)(t + s * T) * NH + i] = v[s];
   }
 }
 
@@ -445,10 +392,8 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
 }
 
 // Pass C: forward y-transforms of A and B, N = -i (kx A + ky B) / (2 N^2), the 2/3 mask
-// (row j of column i is kept iff min(j, N-j) <= kcut[i]) and the stage epilogue. kx*FA waits
-// for the B transform in the thread's own slots of the shared-memory stash (STASH) or in place
-// of A in global memory.
-template <int N, int C, int R = 16, bool STASH = false>
+// (row j of column i is kept iff min(j, N-j) <= kcut[i]) and the stage epilogue.
+template <int N, int C, int R = 16>
 __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
   constexpr int T = N / R, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
@@ -473,12 +418,8 @@ __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
 #pragma unroll
     for (int s = 0; s < R; ++s) v[s] = valid ? af[(size_t)(t + s * T) * NH + ic] : czero();
     fft_regs<N, R, false, C>(v, sm, t, a.tw, 0);
-    double2* st = smem + (size_t)C * padded(N);
-    if constexpr (STASH) {
-#pragma unroll
-      for (int s = 0; s < R; ++s) st[(size_t)(t + s * T) * C + c] = make_double2(kxs * v[s].x, kxs * v[s].y);
-    } else if (valid) {
-      // keep kx*FA in place of A (the same thread re-reads it below)
+    // keep kx*FA in place of A (the same thread re-reads it below)
+    if (valid) {
 #pragma unroll
       for (int s = 0; s < R; ++s)
         af[(size_t)(t + s * T) * NH + i] = make_double2(kxs * v[s].x, kxs * v[s].y);
@@ -493,7 +434,7 @@ __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
       for (int s = 0; s < R; ++s) {
         const int j = t + s * T;
         const double kys = __ldg(&a.fky[j]) * scale;
-        const double2 fa = STASH ? st[(size_t)j * C + c] : af[(size_t)j * NH + i];
+        const double2 fa = af[(size_t)j * NH + i];
         // N = -i (kx A + ky B): re = kx Im A + ky Im B, im = -(kx Re A + ky Re B)
         double2 nh = make_double2(fma(kys, v[s].y, fa.y), -fma(kys, v[s].x, fa.x));
         const int aj = min(j, N - j);
@@ -508,11 +449,11 @@ __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
 // stage value written by the epilogue is re-read by the thread that wrote it. The two
 // evaluations use different untruncated-input flags (next.flag != cur.flag): pass C clears
 // cur.flag while pass A may raise next.flag.
-template <int N, int C, int R = 16, bool STASH = false>
+template <int N, int C, int R = 16>
 __device__ __forceinline__ void colfwd_colinv_tile(const NltArgs& cur, const NltArgs& next, int tile) {
-  colfwd_tile<N, C, R, STASH>(cur, tile);
+  colfwd_tile<N, C, R>(cur, tile);
   __syncthreads();
-  colinv_tile<N, C, R, STASH>(next, tile);
+  colinv_tile<N, C, R>(next, tile);
 }
 
 // ---- grouped column tiles ------------------------------------------------------------------
@@ -721,7 +662,7 @@ __device__ __forceinline__ void colfwd_colinv_grp_tile(const NltArgs& cur, const
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
 k_nlt_colinv(NltArgs a) {
-  colinv_tile<N, Shape<N>::COLS, 16, Shape<N>::STASH>(a, blockIdx.x);
+  colinv_tile<N, Shape<N>::COLS>(a, blockIdx.x);
 }
 
 template <int N>
@@ -733,13 +674,13 @@ k_nlt_row(NltArgs a) {
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
 k_nlt_colfwd(NltArgs a) {
-  colfwd_tile<N, Shape<N>::COLS, 16, Shape<N>::STASH>(a, blockIdx.x);
+  colfwd_tile<N, Shape<N>::COLS>(a, blockIdx.x);
 }
 
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
 k_nlt_colfwd_inv(NltArgs cur, NltArgs next) {
-  colfwd_colinv_tile<N, Shape<N>::COLS, 16, Shape<N>::STASH>(cur, next, blockIdx.x);
+  colfwd_colinv_tile<N, Shape<N>::COLS>(cur, next, blockIdx.x);
 }
 
 // ---- launch variants of the nonlinear-term passes (picked per handle by gt_autotune) ------
@@ -764,8 +705,6 @@ struct Var {
   static constexpr int COL_CTAS = (NH + COLS - 1) / COLS;
   static constexpr int ROW_CTAS = N / ROWS;
   static constexpr size_t COL_SMEM = (size_t)padded(N) * (GROUPED ? kColGroups : COLS) * sizeof(double2);
-  static constexpr bool STASH = !GROUPED && N <= 2048;
-  static constexpr size_t COL_SMEM_NLT = COL_SMEM + (STASH ? (size_t)N * COLS * sizeof(double2) : 0);
   // grouped rows: two length-N exchange buffers (u + i v and q)
   static constexpr size_t ROW_SMEM = GROUPED ? (size_t)2 * padded(N) * sizeof(double2)
                                              : (size_t)(padded(N) + padded(N / 2)) * ROWS * sizeof(double2);
@@ -775,7 +714,7 @@ struct Var {
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colinv(NltArgs a) {
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colinv_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
-  else if constexpr (Var<N, V>::OK) colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R, Var<N, V>::STASH>(a, blockIdx.x);
+  else if constexpr (Var<N, V>::OK) colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_nltv_row(NltArgs a) {
@@ -785,14 +724,14 @@ __global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_nltv_row(NltArgs a) 
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd(NltArgs a) {
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colfwd_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
-  else if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R, Var<N, V>::STASH>(a, blockIdx.x);
+  else if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltArgs cur, NltArgs next) {
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED)
     colfwd_colinv_grp_tile<N, Var<N, V>::R>(cur, next, blockIdx.x);
   else if constexpr (Var<N, V>::OK)
-    colfwd_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R, Var<N, V>::STASH>(cur, next, blockIdx.x);
+    colfwd_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(cur, next, blockIdx.x);
 }
 
 // ---- ensemble kernels: one launch per pass for every member ------------------------------
@@ -800,8 +739,7 @@ __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltA
 // size (N = 128 ... 2048), alpha, dt and tables. All variants use 128-thread CTAs and the same
 // shared memory (C * N = 2048 columns-values, ROWS * N = 2048 row-values).
 constexpr int kEnsThreads = 128;
-// column tiles: exchange buffer + the colinv_tile stash (C*N = 2048 values for every size)
-constexpr size_t kEnsColSmem = (size_t)(padded(2048) + 2048) * sizeof(double2);
+constexpr size_t kEnsColSmem = (size_t)padded(2048) * sizeof(double2);
 constexpr size_t kEnsRowSmem = (size_t)(padded(2048) + padded(1024)) * sizeof(double2);
 
 struct EnsTile {
