@@ -22,61 +22,61 @@
 
 namespace gt {
 
-__global__ void __launch_bounds__(kEnsThreads)
+__global__ void __launch_bounds__(kEnsThreads, kEnsMinBlocks)
 k_ens_colinv(const NltArgs* __restrict__ args, const EnsTile* __restrict__ tiles) {
   const EnsTile w = tiles[blockIdx.x];
   const NltArgs a = args[w.member];
   switch (a.n) {
-    case 128: colinv_tile<128, 16>(a, w.tile); break;
-    case 256: colinv_tile<256, 8>(a, w.tile); break;
-    case 512: colinv_tile<512, 4>(a, w.tile); break;
-    case 1024: colinv_tile<1024, 2>(a, w.tile); break;
-    case 2048: colinv_tile<2048, 1>(a, w.tile); break;
+    case 128: colinv_tile<128, 16, 8>(a, w.tile); break;
+    case 256: colinv_tile<256, 8, 8>(a, w.tile); break;
+    case 512: colinv_tile<512, 4, 8>(a, w.tile); break;
+    case 1024: colinv_tile<1024, 2, 8>(a, w.tile); break;
+    case 2048: colinv_tile<2048, 1, 8>(a, w.tile); break;
     default: break;
   }
 }
 
-__global__ void __launch_bounds__(kEnsThreads)
+__global__ void __launch_bounds__(kEnsThreads, kEnsMinBlocks)
 k_ens_row(const NltArgs* __restrict__ args, const EnsTile* __restrict__ tiles) {
   const EnsTile w = tiles[blockIdx.x];
   const NltArgs a = args[w.member];
   switch (a.n) {
-    case 128: row_tile<128, 16>(a, w.tile); break;
-    case 256: row_tile<256, 8>(a, w.tile); break;
-    case 512: row_tile<512, 4>(a, w.tile); break;
-    case 1024: row_tile<1024, 2>(a, w.tile); break;
-    case 2048: row_tile<2048, 1>(a, w.tile); break;
+    case 128: row_tile<128, 16, 8>(a, w.tile); break;
+    case 256: row_tile<256, 8, 8>(a, w.tile); break;
+    case 512: row_tile<512, 4, 8>(a, w.tile); break;
+    case 1024: row_tile<1024, 2, 8>(a, w.tile); break;
+    case 2048: row_tile<2048, 1, 8>(a, w.tile); break;
     default: break;
   }
 }
 
-__global__ void __launch_bounds__(kEnsThreads)
+__global__ void __launch_bounds__(kEnsThreads, kEnsMinBlocks)
 k_ens_colfwd(const NltArgs* __restrict__ args, const EnsTile* __restrict__ tiles) {
   const EnsTile w = tiles[blockIdx.x];
   const NltArgs a = args[w.member];
   switch (a.n) {
-    case 128: colfwd_tile<128, 16>(a, w.tile); break;
-    case 256: colfwd_tile<256, 8>(a, w.tile); break;
-    case 512: colfwd_tile<512, 4>(a, w.tile); break;
-    case 1024: colfwd_tile<1024, 2>(a, w.tile); break;
-    case 2048: colfwd_tile<2048, 1>(a, w.tile); break;
+    case 128: colfwd_tile<128, 16, 8>(a, w.tile); break;
+    case 256: colfwd_tile<256, 8, 8>(a, w.tile); break;
+    case 512: colfwd_tile<512, 4, 8>(a, w.tile); break;
+    case 1024: colfwd_tile<1024, 2, 8>(a, w.tile); break;
+    case 2048: colfwd_tile<2048, 1, 8>(a, w.tile); break;
     default: break;
   }
 }
 
 // pass C of stage cur[m] fused with pass A of stage next[m] (same tiles)
-__global__ void __launch_bounds__(kEnsThreads)
+__global__ void __launch_bounds__(kEnsThreads, kEnsMinBlocks)
 k_ens_colfwd_inv(const NltArgs* __restrict__ cur, const NltArgs* __restrict__ next,
                  const EnsTile* __restrict__ tiles) {
   const EnsTile w = tiles[blockIdx.x];
   const NltArgs a = cur[w.member];
   const NltArgs b = next[w.member];
   switch (a.n) {
-    case 128: colfwd_colinv_tile<128, 16>(a, b, w.tile); break;
-    case 256: colfwd_colinv_tile<256, 8>(a, b, w.tile); break;
-    case 512: colfwd_colinv_tile<512, 4>(a, b, w.tile); break;
-    case 1024: colfwd_colinv_tile<1024, 2>(a, b, w.tile); break;
-    case 2048: colfwd_colinv_tile<2048, 1>(a, b, w.tile); break;
+    case 128: colfwd_colinv_tile<128, 16, 8>(a, b, w.tile); break;
+    case 256: colfwd_colinv_tile<256, 8, 8>(a, b, w.tile); break;
+    case 512: colfwd_colinv_tile<512, 4, 8>(a, b, w.tile); break;
+    case 1024: colfwd_colinv_tile<1024, 2, 8>(a, b, w.tile); break;
+    case 2048: colfwd_colinv_tile<2048, 1, 8>(a, b, w.tile); break;
     default: break;
   }
 }

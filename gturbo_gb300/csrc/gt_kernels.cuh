@@ -175,7 +175,7 @@ struct MinBlocks {
 // The three passes as tile functions. A tile is one CTA's work: C adjacent columns (passes
 // A and C) or ROWS rows (pass B) of one field. The single-field kernels run tile = blockIdx.x;
 // the ensemble kernels read (member, tile) from a work list, so members of different sizes
-// share one launch (every variant uses 128-thread CTAs from N = 128 to 2048).
+// share one launch (256-thread CTAs with 8 values per thread from N = 128 to 2048).
 // ---------------------------------------------------------------------------------------
 
 // One nonlinear-term evaluation of one field.
@@ -736,9 +736,12 @@ __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltA
 
 // ---- ensemble kernels: one launch per pass for every member ------------------------------
 // CTA b works on tile tiles[b] = (member, tile) of the member's field; members may differ in
-// size (N = 128 ... 2048), alpha, dt and tables. All variants use 128-thread CTAs and the same
-// shared memory (C * N = 2048 columns-values, ROWS * N = 2048 row-values).
-constexpr int kEnsThreads = 128;
+// size (N = 128 ... 2048), alpha, dt and tables. Every size uses 256-thread CTAs with 8 complex
+// values per thread (T = N/8 threads per column or row) and the same shared memory (C * N = 2048
+// column values, ROWS * N = 2048 row values), with at least 3 CTAs per SM (at most 85 registers
+// per thread).
+constexpr int kEnsThreads = 256;
+constexpr int kEnsMinBlocks = 3;
 constexpr size_t kEnsColSmem = (size_t)padded(2048) * sizeof(double2);
 constexpr size_t kEnsRowSmem = (size_t)(padded(2048) + padded(1024)) * sizeof(double2);
 
@@ -747,7 +750,7 @@ struct EnsTile {
   int tile;
 };
 
-// Tiles per field of each ensemble pass (128-thread CTAs).
+// Tiles per field of each ensemble pass (C = ROWS = 2048/N columns or rows per CTA).
 __host__ __device__ constexpr int ens_col_tiles(int n) { return (n / 2 + 1 + (2048 / n) - 1) / (2048 / n); }
 __host__ __device__ constexpr int ens_row_tiles(int n) { return n / (2048 / n); }
 
