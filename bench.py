@@ -339,9 +339,10 @@ def ours_arm(args):
     finite = bool(torch.isfinite(z).all().item())
     stages = 4 if p.rko == 4 else 2
     # per step: pass A of stage 1, then per stage pass B and pass C (fused with the next
-    # stage's pass A) -> 2 * stages + 1, plus the forcing kick; a diagnostics call adds one
-    # nonlinear term (3 passes) and 5 reduction kernels
-    launches = K * (2 * stages + 1 + 1) + ndiag * (3 + 5)
+    # stage's pass A) -> 2 * stages + 1, the forcing kick fused into the last pass C; a
+    # diagnostics step launches the kick separately (the diagnostics see the field before it)
+    # and adds one nonlinear term (3 passes) and 5 reduction kernels
+    launches = K * (2 * stages + 1) + ndiag * (1 + 3 + 5)
 
     extras = {}
     if rank == 0:

@@ -43,7 +43,50 @@ struct EpiArgs {
   const double* emkx;   // [NH]
   const double* emky;   // [N]
   double dt, dt2, dt3, dt6;
+  // The forcing kick of forcing.f90:16-33 added to the final stage's store (EPI_RK2B, EPI_RK4D)
+  // when fmap is set. fmap[i * fh + jj] over the window i < fwi, |ky| < fwj (jj = j for j < fwj,
+  // j - (N - fh) for the rows of negative ky) holds -1 or the mode index k, with bit 30 set
+  // where (i, j) is the conjugate partner of mode k on the kx = 0 or Nyquist column.
+  const int* fmap;
+  int fwi, fwj, fh;
+  const uint32_t* lcga;  // jump-ahead coefficients of the k-th draw
+  const uint32_t* lcgb;
+  const double2* ff;     // per-mode amplitude factors
+  uint32_t seed0;        // LCG state before the kick
+  double sf;             // sqrt(dt) * famp
 };
+
+// The kick of forced mode k added to value a: phase te = 2 pi rann of the (k+1)-th LCG draw from
+// seed0 (x -> 69069 x + 1 mod 2^31, rann rounded to real(4) as in the reference), a + sf ff
+// (cos te, +-sin te) (minus for the conjugate partner). The one definition serves the forcing
+// kernel and the fused final-stage store, so both give the same bits.
+__device__ __forceinline__ double2 forcing_kick(double2 a, int k, bool conj, const uint32_t* lcga,
+                                                const uint32_t* lcgb, const double2* ff,
+                                                uint32_t seed0, double sf) {
+  const double pi2 = 2.0 * 3.14159265358979;  // forcing.f90:10
+  const uint32_t x = (__ldg(&lcga[k]) * seed0 + __ldg(&lcgb[k])) & 0x7FFFFFFFu;
+  const float rr = (float)((double)x / 2147483647.0);
+  const double te = pi2 * (double)rr;
+  double sn, cs;
+  sincos(te, &sn, &cs);
+  const double2 f = __ldg(&ff[k]);
+  a.x = fma(sf * f.x, cs, a.x);
+  a.y = conj ? fma(-(sf * f.y), sn, a.y) : fma(sf * f.y, sn, a.y);
+  return a;
+}
+
+// The fused kick at (i, j) of an N x NH field, if (i, j) is forced.
+__device__ __forceinline__ double2 fused_kick(const EpiArgs& E, int i, int j, int NH, double2 r) {
+  if (i >= E.fwi) return r;
+  const int N = 2 * (NH - 1);
+  int jj;
+  if (j < E.fwj) jj = j;
+  else if (j >= N - (E.fh - E.fwj)) jj = j - (N - E.fh);
+  else return r;
+  const int e = __ldg(&E.fmap[i * E.fh + jj]);
+  if (e < 0) return r;
+  return forcing_kick(r, e & 0x3FFFFFFF, (e >> 30) & 1, E.lcga, E.lcgb, E.ff, E.seed0, E.sf);
+}
 
 __device__ __forceinline__ void epilogue(const EpiArgs& E, int i, int j, int NH, double2 nh) {
   const size_t o = (size_t)j * NH + i;
@@ -62,8 +105,10 @@ __device__ __forceinline__ void epilogue(const EpiArgs& E, int i, int j, int NH,
     }
     case EPI_RK2B: {
       const double2 z = E.z[o];
-      const double2 r = make_double2(e * (e * z.x + E.dt * nh.x), e * (e * z.y + E.dt * nh.y));
-      E.out[o] = origin ? make_double2(0.0, 0.0) : r;
+      double2 r = make_double2(e * (e * z.x + E.dt * nh.x), e * (e * z.y + E.dt * nh.y));
+      if (origin) r = make_double2(0.0, 0.0);
+      if (E.fmap) r = fused_kick(E, i, j, NH, r);
+      E.out[o] = r;
       break;
     }
     case EPI_RK4A: {
@@ -91,8 +136,10 @@ __device__ __forceinline__ void epilogue(const EpiArgs& E, int i, int j, int NH,
     }
     case EPI_RK4D: {
       const double2 w = E.znew[o];
-      const double2 r = make_double2(w.x + E.dt6 * nh.x, w.y + E.dt6 * nh.y);
-      E.out[o] = origin ? make_double2(0.0, 0.0) : r;
+      double2 r = make_double2(w.x + E.dt6 * nh.x, w.y + E.dt6 * nh.y);
+      if (origin) r = make_double2(0.0, 0.0);
+      if (E.fmap) r = fused_kick(E, i, j, NH, r);
+      E.out[o] = r;
       break;
     }
     default:

@@ -45,25 +45,12 @@ __global__ void k_forcing(double2* z, int nh, int nf, const int* __restrict__ ik
                           const double2* __restrict__ ff, uint32_t seed0, double sf) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nf) return;
-  const double pi2 = 2.0 * 3.14159265358979;  // forcing.f90:10
-  const uint32_t x = (lcga[k] * seed0 + lcgb[k]) & 0x7FFFFFFFu;
-  const float rr = (float)((double)x / 2147483647.0);
-  const double te = pi2 * (double)rr;
-  double cs, cc;
-  sincos(te, &cs, &cc);
   const int i = ikx[k], j = iky[k];
-  const double2 f = ff[k];
   double2* p = z + (size_t)j * nh + i;
-  double2 a = *p;
-  a.x = a.x + sf * f.x * cc;
-  a.y = a.y + sf * f.y * cs;
-  *p = a;
+  *p = forcing_kick(*p, k, false, lcga, lcgb, ff, seed0, sf);
   if (i == 0 || i == nh - 1) {
     double2* pc = z + (size_t)jc[j] * nh + i;
-    double2 b = *pc;
-    b.x = b.x + sf * f.x * cc;
-    b.y = b.y - sf * f.y * cs;
-    *pc = b;
+    *pc = forcing_kick(*pc, k, true, lcga, lcgb, ff, seed0, sf);
   }
 }
 

@@ -5,6 +5,7 @@
 // was current at gt_create. Fields are owned by the caller and passed as device pointers.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -46,6 +47,10 @@ struct gt_handle {
   std::vector<int> jc, kcut, ikxf, ikyf;
   std::vector<uint32_t> lcga, lcgb;  // index k: coefficients of the (k+1)-th draw
   uint32_t lcga_nf = 1, lcgb_nf = 0;
+  // forced-mode map of the fused kick (EpiArgs::fmap); fuse_ok = 0 when two kicks would land
+  // on one value (a self-conjugate mode), which keeps the separate forcing launch
+  std::vector<int> fmap;
+  int fwi = 0, fwj = 0, fh = 0, fuse_ok = 0;
   int device = 0;
   int variant = 0;      // launch variant of the column passes
   int row_variant = 0;  // launch variant of the row passes
@@ -57,7 +62,7 @@ struct gt_handle {
   double* d_kainv = nullptr;
   double *d_fkx = nullptr, *d_fky = nullptr, *d_fkxs = nullptr, *d_fkys = nullptr;
   double *d_emkx = nullptr, *d_emky = nullptr;
-  int *d_kcut = nullptr, *d_jc = nullptr, *d_ikxf = nullptr, *d_ikyf = nullptr;
+  int *d_kcut = nullptr, *d_jc = nullptr, *d_ikxf = nullptr, *d_ikyf = nullptr, *d_fmap = nullptr;
   uint32_t *d_lcga = nullptr, *d_lcgb = nullptr;
   double2* d_ff = nullptr;
   int* d_flag = nullptr;
@@ -266,7 +271,7 @@ void free_device(gt_handle* h) {
   void* ptrs[] = {h->d_tw, h->d_emk, h->d_kainv, h->d_fkx, h->d_fky, h->d_fkxs, h->d_fkys,
                   h->d_emkx, h->d_emky, h->d_kcut, h->d_jc, h->d_ikxf, h->d_ikyf, h->d_lcga,
                   h->d_lcgb, h->d_ff, h->d_flag, h->d_part, h->d_rowsum, h->d_bins, h->d_fl,
-                  h->d_glob};
+                  h->d_glob, h->d_fmap};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (h->h_diag) cudaFreeHost(h->h_diag);
@@ -460,6 +465,29 @@ int gt_create(const gt_params* p, gt_handle** out) {
   }
   h->lcga_nf = A;
   h->lcgb_nf = B;
+  // map of the forced values for the fused kick: mode k at (ikx, iky), and its conjugate partner
+  // (ikx, jc[iky]) on the kx = 0 and Nyquist columns (forcing.f90:21-31)
+  if (h->nf > 0) {
+    auto aky = [&](int j) { return j <= N / 2 ? j : N - j; };
+    for (int k = 0; k < h->nf; ++k) {
+      h->fwi = std::max(h->fwi, h->ikxf[k] + 1);
+      h->fwj = std::max(h->fwj, aky(h->ikyf[k]) + 1);
+    }
+    h->fh = std::min(N, 2 * h->fwj - 1);
+    h->fmap.assign((size_t)h->fwi * h->fh, -1);
+    h->fuse_ok = 1;
+    auto put = [&](int i, int j, int e) {
+      const int jj = j < h->fwj ? j : j - (N - h->fh);
+      int& slot = h->fmap[(size_t)i * h->fh + jj];
+      if (slot >= 0) h->fuse_ok = 0;
+      slot = e;
+    };
+    for (int k = 0; k < h->nf; ++k) {
+      const int i = h->ikxf[k], j = h->ikyf[k];
+      put(i, j, k);
+      if (i == 0 || i == NH - 1) put(i, h->jc[j], k | (1 << 30));
+    }
+  }
 
   // device side
   int rc = GT_OK;
@@ -489,6 +517,7 @@ int gt_create(const gt_params* p, gt_handle** out) {
   if (!rc) rc = upload(h, &h->d_lcga, h->lcga.data(), h->nf);
   if (!rc) rc = upload(h, &h->d_lcgb, h->lcgb.data(), h->nf);
   if (!rc) rc = upload(h, &h->d_ff, ff.data(), ff.size());
+  if (!rc && h->nf > 0) rc = upload(h, &h->d_fmap, h->fmap.data(), h->fmap.size());
   const int zeros2[2] = {0, 0};  // untruncated-input flags of even / odd stages
   if (!rc) rc = upload(h, &h->d_flag, zeros2, 2);
   const int ngroups = (N + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
@@ -691,6 +720,56 @@ int gt_step_rk4(gt_handle* h, double* z, double* znl, double* znew, double* u, d
                               make_epi(h, gt::EPI_RK4C, znl, znew, z), make_epi(h, gt::EPI_RK4D, z, znew, nullptr)};
   const double* zin[4] = {z, znl, znl, znl};
   return stage_chain(h, 4, zin, znl, u, v, epi);
+}
+
+// The final stage's fused kick from LCG state x0 (forcing.f90:16-33).
+static void set_fused_kick(const gt_handle* h, gt::EpiArgs& E, uint32_t x0) {
+  E.fmap = h->d_fmap;
+  E.fwi = h->fwi;
+  E.fwj = h->fwj;
+  E.fh = h->fh;
+  E.lcga = h->d_lcga;
+  E.lcgb = h->d_lcgb;
+  E.ff = h->d_ff;
+  E.seed0 = x0;
+  E.sf = h->sdt * h->p.famp;
+}
+
+int gt_step_rk2_forced(gt_handle* h, double* z, double* znl, double* u, double* v, int32_t* seed) {
+  if (!h || !z || !znl || !u || !v || !seed) return fail(h, GT_ERR_ARG, "gt_step_rk2_forced: null argument");
+  if (!(h->nf > 0 && h->fuse_ok)) {
+    const int rc = gt_step_rk2(h, z, znl, u, v);
+    return rc ? rc : gt_forcing(h, z, seed);
+  }
+  gt::EpiArgs epi[2] = {make_epi(h, gt::EPI_RK2A, znl, nullptr, z),
+                        make_epi(h, gt::EPI_RK2B, z, nullptr, z)};
+  const uint32_t x0 = (uint32_t)(*seed);
+  set_fused_kick(h, epi[1], x0);
+  const double* zin[2] = {z, znl};
+  const int rc = stage_chain(h, 2, zin, znl, u, v, epi);
+  if (rc) return rc;
+  *seed = (int32_t)((h->lcga_nf * x0 + h->lcgb_nf) & 0x7FFFFFFFu);
+  return GT_OK;
+}
+
+int gt_step_rk4_forced(gt_handle* h, double* z, double* znl, double* znew, double* u, double* v,
+                       int32_t* seed) {
+  if (!h || !z || !znl || !znew || !u || !v || !seed)
+    return fail(h, GT_ERR_ARG, "gt_step_rk4_forced: null argument");
+  if (h->split) return fail(h, GT_ERR_ARG, "gt_step_rk4_forced: the split integrator exists only for RK2");
+  if (!(h->nf > 0 && h->fuse_ok)) {
+    const int rc = gt_step_rk4(h, z, znl, znew, u, v);
+    return rc ? rc : gt_forcing(h, z, seed);
+  }
+  gt::EpiArgs epi[4] = {make_epi(h, gt::EPI_RK4A, znl, znew, z), make_epi(h, gt::EPI_RK4B, znl, znew, z),
+                        make_epi(h, gt::EPI_RK4C, znl, znew, z), make_epi(h, gt::EPI_RK4D, z, znew, nullptr)};
+  const uint32_t x0 = (uint32_t)(*seed);
+  set_fused_kick(h, epi[3], x0);
+  const double* zin[4] = {z, znl, znl, znl};
+  const int rc = stage_chain(h, 4, zin, znl, u, v, epi);
+  if (rc) return rc;
+  *seed = (int32_t)((h->lcga_nf * x0 + h->lcgb_nf) & 0x7FFFFFFFu);
+  return GT_OK;
 }
 
 float gt_rann(int32_t* seed) {

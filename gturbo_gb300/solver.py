@@ -260,6 +260,19 @@ class Solver:
         else:
             self.step(z, znl, u, v)
 
+    def rk_step_forced(self, z, work, seed: int) -> int:
+        """``rk_step`` followed by ``forcing`` with the kick fused into the final stage
+        (gt_step_rk2_forced / gt_step_rk4_forced); returns the LCG state after the kick."""
+        znl, znew, u, v = work
+        s = ctypes.c_int32(int(seed))
+        if self.info.rko == 4:
+            self._check(self.lib.gt_step_rk4_forced(self.h, self._ptr(z), self._ptr(znl), self._ptr(znew),
+                                                    self._ptr(u), self._ptr(v), ctypes.byref(s)))
+        else:
+            self._check(self.lib.gt_step_rk2_forced(self.h, self._ptr(z), self._ptr(znl), self._ptr(u),
+                                                    self._ptr(v), ctypes.byref(s)))
+        return s.value
+
     def forcing(self, z, seed: int) -> int:
         """Adds one kick; returns the LCG state after the nf draws."""
         s = ctypes.c_int32(int(seed))
@@ -288,14 +301,16 @@ class Solver:
         return out
 
     def main_step(self, z, seed: int, work, diag: bool = False):
-        """One iteration of src/main.f90:97-137 (step, diagnostics when asked, forcing)."""
+        """One iteration of src/main.f90:97-137 (step, diagnostics when asked, forcing). The
+        diagnostics see the field before the kick, so a diagnostics step keeps the separate
+        forcing launch; the others fuse the kick into the step (``rk_step_forced``)."""
+        if not diag:
+            return self.rk_step_forced(z, work, seed), None
         self.rk_step(z, work)
-        out = None
-        if diag:
-            znl, _, u, v = work
-            with torch.cuda.stream(self.stream):
-                znl.copy_(z)
-            self.nlt(znl, u, v)
-            out = self.diag(z, znl)
+        znl, _, u, v = work
+        with torch.cuda.stream(self.stream):
+            znl.copy_(z)
+        self.nlt(znl, u, v)
+        out = self.diag(z, znl)
         seed = self.forcing(z, seed)
         return seed, out

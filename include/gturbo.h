@@ -137,6 +137,16 @@ int gt_forcing(gt_handle* h, double* z, int32_t* seed);
 /* The reference's rann (src/forcing.f90:40-51) on the host: advances *seed
  * once and returns the real(4) draw. Exported for drivers and tests. */
 float gt_rann(int32_t* seed);
+/* One step followed by one kick, the body of the reference's main loop on steps
+ * without diagnostics (src/main.f90:100-106: step/step4, then forcing). The kick
+ * is added in the final stage's store instead of a separate launch, as the
+ * stage update's fused forcing injection. Results and *seed are bit-identical
+ * to gt_step_rk2/gt_step_rk4 followed by gt_forcing. A handle whose forced
+ * modes include a self-conjugate one (two kicks on one value, possible only
+ * without truncation) runs the step and gt_forcing one after the other. */
+int gt_step_rk2_forced(gt_handle* h, double* z, double* znl, double* u, double* v, int32_t* seed);
+int gt_step_rk4_forced(gt_handle* h, double* z, double* znl, double* znew, double* u, double* v,
+                       int32_t* seed);
 
 /* Counter-based forcing, no counterpart in the reference (its LCG is serial):
  * the same kick as gt_forcing, with the phase of forced mode k at step `step`

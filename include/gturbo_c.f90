@@ -105,6 +105,20 @@ module gturbo_c
       real(c_double) :: z(*)
       integer(c_int32_t) :: seed
     end function
+    ! step / step4 followed by forcing, the kick fused into the final stage (src/main.f90:100-106)
+    integer(c_int) function gt_step_rk2_forced(h, z, znl, u, v, seed) bind(C, name="gt_step_rk2_forced")
+      import :: c_int, c_ptr, c_double, c_int32_t
+      type(c_ptr), value :: h
+      real(c_double) :: z(*), znl(*), u(*), v(*)
+      integer(c_int32_t) :: seed
+    end function
+    integer(c_int) function gt_step_rk4_forced(h, z, znl, znew, u, v, seed) &
+        bind(C, name="gt_step_rk4_forced")
+      import :: c_int, c_ptr, c_double, c_int32_t
+      type(c_ptr), value :: h
+      real(c_double) :: z(*), znl(*), znew(*), u(*), v(*)
+      integer(c_int32_t) :: seed
+    end function
     ! rann (src/forcing.f90:40-51), host only
     real(c_float) function gt_rann(seed) bind(C, name="gt_rann")
       import :: c_float, c_int32_t

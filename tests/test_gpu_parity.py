@@ -215,6 +215,53 @@ def test_step_split_rk2():
             assert rel_l2(_host(z), ref) < TOL, (c, r)
 
 
+@pytest.mark.parametrize("n,rko,kw", [(64, 2, {}), (64, 4, {}), (256, 4, dict(k1f=10.0, k2f=12.0)),
+                                      (128, 2, dict(alpnu=1.0, alpmu=0.0, nu=1e-3)),
+                                      (2048, 2, dict(k1f=20.0, k2f=22.0, alpv=1.0))])
+def test_forced_step_equals_step_then_forcing(n, rko, kw):
+    """gt_step_rk*_forced (the kick fused into the final stage's store) gives the same bits and
+    the same LCG state as gt_step_rk* followed by gt_forcing, in every launch variant, and agrees
+    with the oracle's step + forcing."""
+    p = _params(n, rko=rko, famp=0.9, dt=2e-3, **kw)
+    orc, sol = Oracle(p), _solver(p)
+    assert sol.info.nf > 0
+    a = rand_field(orc, 23) * 20.0
+    ref = a.copy()
+    orc.rk_step(ref)
+    seed_ref = orc.forcing(ref, 481929)
+    for c in sol.supported_variants():
+        for r in sol.supported_row_variants():
+            sol.variants = (c, r)
+            z1, z2 = _dev(a), _dev(a)
+            sol.rk_step(z1, sol.work())
+            s1 = sol.forcing(z1, 481929)
+            s2 = sol.rk_step_forced(z2, sol.work(), 481929)
+            assert s1 == s2 == seed_ref, (c, r)
+            assert torch.equal(z1, z2), (c, r)
+            assert rel_l2(_host(z2), ref) < TOL, (c, r)
+
+
+def test_forced_step_self_conjugate_mode():
+    """Without truncation a forced mode can be its own conjugate partner (kx = 0, ky = N/2 or
+    the Nyquist column): two kicks on one value. The forced step then runs the step and the
+    forcing launch one after the other, with the same result."""
+    p = _params(16, rko=2, truncate=0, rtrunc=1.0, k1f=7.5, k2f=8.5, famp=0.8, dt=1e-3)
+    orc, sol = Oracle(p), _solver(p)
+    ik, jk = sol.forcing_modes()
+    assert any((i == 0 and j == 8) or (i == 8 and j in (0, 8)) for i, j in zip(ik, jk))
+    a = rand_field(orc, 24, truncate=False)
+    ref = a.copy()
+    orc.rk_step(ref)
+    seed_ref = orc.forcing(ref, 1234)
+    z1, z2 = _dev(a), _dev(a)
+    sol.rk_step(z1, sol.work())
+    s1 = sol.forcing(z1, 1234)
+    s2 = sol.rk_step_forced(z2, sol.work(), 1234)
+    assert s1 == s2 == seed_ref
+    assert torch.equal(z1, z2)
+    assert rel_l2(_host(z2), ref) < TOL
+
+
 @pytest.mark.parametrize("n,k1,k2", [(64, 3.0, 5.0), (256, 10.0, 12.0), (2048, 20.0, 22.0)])
 def test_forcing(n, k1, k2):
     p = _params(n, k1f=k1, k2f=k2, famp=0.7)
