@@ -88,6 +88,9 @@ __device__ __forceinline__ double2 fused_kick(const EpiArgs& E, int i, int j, in
   return forcing_kick(r, e & 0x3FFFFFFF, (e >> 30) & 1, E.lcga, E.lcgb, E.ff, E.seed0, E.sf);
 }
 
+// KICK: the fused forcing kick is compiled in (the final stage's pass C only; the intermediate
+// stages' kernels stay free of its registers).
+template <bool KICK = false>
 __device__ __forceinline__ void epilogue(const EpiArgs& E, int i, int j, int NH, double2 nh) {
   const size_t o = (size_t)j * NH + i;
   if (E.mode == EPI_NLT) {
@@ -107,7 +110,7 @@ __device__ __forceinline__ void epilogue(const EpiArgs& E, int i, int j, int NH,
       const double2 z = E.z[o];
       double2 r = make_double2(e * (e * z.x + E.dt * nh.x), e * (e * z.y + E.dt * nh.y));
       if (origin) r = make_double2(0.0, 0.0);
-      if (E.fmap) r = fused_kick(E, i, j, NH, r);
+      if (KICK && E.fmap) r = fused_kick(E, i, j, NH, r);
       E.out[o] = r;
       break;
     }
@@ -138,7 +141,7 @@ __device__ __forceinline__ void epilogue(const EpiArgs& E, int i, int j, int NH,
       const double2 w = E.znew[o];
       double2 r = make_double2(w.x + E.dt6 * nh.x, w.y + E.dt6 * nh.y);
       if (origin) r = make_double2(0.0, 0.0);
-      if (E.fmap) r = fused_kick(E, i, j, NH, r);
+      if (KICK && E.fmap) r = fused_kick(E, i, j, NH, r);
       E.out[o] = r;
       break;
     }
@@ -440,7 +443,7 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
 
 // Pass C: forward y-transforms of A and B, N = -i (kx A + ky B) / (2 N^2), the 2/3 mask
 // (row j of column i is kept iff min(j, N-j) <= kcut[i]) and the stage epilogue.
-template <int N, int C, int R = 16>
+template <int N, int C, int R = 16, bool KICK = false>
 __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
   constexpr int T = N / R, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
@@ -453,7 +456,7 @@ __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
     // no retained mode in this tile: N = 0
     if (valid) {
 #pragma unroll
-      for (int s = 0; s < R; ++s) epilogue(a.epi, i, t + s * T, NH, czero());
+      for (int s = 0; s < R; ++s) epilogue<KICK>(a.epi, i, t + s * T, NH, czero());
     }
   } else {
     double2* sm = smem + c;
@@ -486,7 +489,7 @@ __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
         double2 nh = make_double2(fma(kys, v[s].y, fa.y), -fma(kys, v[s].x, fa.x));
         const int aj = min(j, N - j);
         if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
-        epilogue(a.epi, i, j, NH, nh);
+        epilogue<KICK>(a.epi, i, j, NH, nh);
       }
     }
   }
@@ -567,7 +570,7 @@ __device__ __forceinline__ void colinv_grp_tile(const NltArgs& a, int tile) {
 // Pass C: group 0 transforms A, group 1 transforms B, group 2 zeros; group 0 hands kx*FA to
 // group 1 through its exchange buffer (free once fft_regs has returned), and group 1 forms N
 // and runs the epilogue.
-template <int N, int R>
+template <int N, int R, bool KICK = false>
 __device__ __forceinline__ void colfwd_grp_tile(const NltArgs& a, int tile) {
   constexpr int T = N / R, NH = N / 2 + 1;
   extern __shared__ double2 smem[];
@@ -578,7 +581,7 @@ __device__ __forceinline__ void colfwd_grp_tile(const NltArgs& a, int tile) {
     // no retained mode in this column: N = 0
     if (g == 0) {
 #pragma unroll
-      for (int s = 0; s < R; ++s) epilogue(a.epi, i, t + s * T, NH, czero());
+      for (int s = 0; s < R; ++s) epilogue<KICK>(a.epi, i, t + s * T, NH, czero());
     }
   } else {
     double2* sm = smem + (size_t)g * padded(N);
@@ -606,7 +609,7 @@ __device__ __forceinline__ void colfwd_grp_tile(const NltArgs& a, int tile) {
         double2 nh = make_double2(fma(kys, v[s].y, f.y), -fma(kys, v[s].x, f.x));
         const int aj = min(j, N - j);
         if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
-        epilogue(a.epi, i, j, NH, nh);
+        epilogue<KICK>(a.epi, i, j, NH, nh);
       }
     }
   }
@@ -721,7 +724,7 @@ k_nlt_row(NltArgs a) {
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
 k_nlt_colfwd(NltArgs a) {
-  colfwd_tile<N, Shape<N>::COLS>(a, blockIdx.x);
+  colfwd_tile<N, Shape<N>::COLS, 16, true>(a, blockIdx.x);
 }
 
 template <int N>
@@ -770,8 +773,8 @@ __global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_nltv_row(NltArgs a) 
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd(NltArgs a) {
-  if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colfwd_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
-  else if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
+  if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colfwd_grp_tile<N, Var<N, V>::R, true>(a, blockIdx.x);
+  else if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R, true>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltArgs cur, NltArgs next) {
