@@ -260,6 +260,17 @@ def pass_model(p, kind):
 #                      python bench.py --config c1 --steps 2 --warmup 3 --no-extras --variant 3
 # Keyed by (N, the launch variant of that kernel: the row variant for the row pass, the column
 # variant otherwise, pass).
+# FP64 instructions (thread level) per launch of a pass, from ncu's
+# smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum of the same launch variant:
+#   2048^2, variant 1: ncu --metrics <those> -k "regex:k_nltv_(row|colfwd_inv|colinv)" -s 4 -c 3
+#                      python bench.py --steps 2 --warmup 3 --no-extras --variant 1
+# The FP64 pipe issues 2 such operations per clock per SM (152 SMs).
+NCU_FP64_OPS = {
+    (2048, 1, "nlt_colinv"): 23.080e6 + 92.320e6 + 8.393e6,
+    (2048, 1, "nlt_row"): 65.704e6 + 247.464e6 + 4.194e6,
+    (2048, 1, "nlt_colfwd_inv"): 44.064e6 + 159.461e6 + 17.137e6,
+}
+
 NCU_TRAFFIC = {
     (2048, 0, "nlt_colinv"): 50.01e6 + 47.65e6,
     (2048, 0, "nlt_row"): 68.00e6 + 1.50e6,
@@ -373,6 +384,16 @@ def ours_arm(args):
         roof["frac"] = roof["achieved"] / fp64 if roof["achieved"] else None
         if roof["hbm_achieved_gbs"] and roof["hbm_peak_gbs"]:
             roof["hbm_frac"] = roof["hbm_achieved_gbs"] / roof["hbm_peak_gbs"]
+        # the same kernel against the FP64 pipe itself: counted instructions per launch over
+        # 2 per clock per SM at the SM clock sampled during the timed region
+        ops = NCU_FP64_OPS.get((p.n, sol.variants[1] if top == "nlt_row" else sol.variants[0], top))
+        mhz = clk.get("sm_mhz") if isinstance(clk, dict) else None
+        if ops and mhz:
+            pipe_peak = 2.0 * torch.cuda.get_device_properties(dev).multi_processor_count * mhz * 1e6
+            roof["fp64_pipe"] = {"ops_per_launch": ops, "ops_source": "ncu smsp__sass_thread_inst_executed_op_"
+                                 "{dfma,dadd,dmul}_pred_on.sum (same kernel and launch variant)",
+                                 "achieved_gops": ops / (ms / 1e3) / 1e9, "peak_gops": pipe_peak / 1e9,
+                                 "frac": ops / (ms / 1e3) / pipe_peak}
         extras["roofline"] = roof
         extras["kernels"] = kernels
         step_bytes = (26 if p.rko == 2 else 57) * 16 * p.n * (p.n // 2 + 1)
