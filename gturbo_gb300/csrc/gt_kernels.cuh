@@ -248,6 +248,9 @@ struct NltArgs {
   // backward sweep keeps them from the recomputed forward stages instead of transforming again.
   double2* phys_uv;
   double2* phys_q;
+  // Per-column counters (NH ints, zero between launches) of the field-split pass C: the second
+  // of a column's two CTAs runs its epilogue.
+  int* colcnt;
 };
 
 // Pass A: inverse y-transforms of u, v and q (in that order: zin may alias q, as the
@@ -708,6 +711,117 @@ __device__ __forceinline__ void colfwd_colinv_grp_tile(const NltArgs& cur, const
   colinv_grp_tile<N, R>(next, tile);
 }
 
+// ---- field-split column tiles --------------------------------------------------------------
+// One field of one column per CTA (C = 1, T = N/R threads), so that a column pass has 3 (pass A)
+// or 2 (pass C) work units per column instead of one: 683 active columns at 2048^2 are 4.5 per
+// SM, and the last SMs to finish would otherwise idle for up to a whole column.
+
+// Pass A, field g of column i: unit = 3 i + g (g = 0: u, 1: v, 2: q). q must not alias zin: the
+// caller passes a q buffer of its own (the three units of a column run in different CTAs).
+template <int N, int R>
+__device__ __forceinline__ void colinv_field_tile(const NltArgs& a, int unit) {
+  constexpr int T = N / R, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  const int i = unit / 3, g = unit % 3, t = threadIdx.x;
+  double2 v[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = a.zin[(size_t)(t + s * T) * NH + i];
+  // beyond the 2/3 ellipse: zeros without a transform for an all-zero column, else raise the
+  // untruncated-input flag (see colinv_tile)
+  int nz = 0;
+  if (i > a.kxlim) {
+#pragma unroll
+    for (int s = 0; s < R; ++s) nz |= nonzero2(v[s]);
+  }
+  const bool skip = (i > a.kxlim) ? !__syncthreads_or(nz) : false;
+  double2* dst = g == 0 ? a.u : g == 1 ? a.v : a.q;
+  if (skip) {
+#pragma unroll
+    for (int s = 0; s < R; ++s) dst[(size_t)(t + s * T) * NH + i] = czero();
+    return;
+  }
+  if (nz) atomicExch(a.flag, 1);
+  const bool zb = column_zband<R>(v);
+  if (g == 0) {  // u = i ky/|k|^a q  (nlt.f90:29-32)
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int j = t + s * T;
+      const double m = __ldg(&a.fky[j]) * __ldg(&a.kainv[(size_t)j * NH + i]);
+      v[s] = make_double2(-m * v[s].y, m * v[s].x);
+    }
+  } else if (g == 1) {  // v = -i kx/|k|^a q  (nlt.f90:33-34)
+    const double kx = __ldg(&a.fkx[i]);
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int j = t + s * T;
+      const double m = kx * __ldg(&a.kainv[(size_t)j * NH + i]);
+      v[s] = make_double2(m * v[s].y, -m * v[s].x);
+    }
+  }
+  fft_regs<N, R, true, 1>(v, smem, t, a.tw, 0, zb);
+#pragma unroll
+  for (int s = 0; s < R; ++s) dst[(size_t)(t + s * T) * NH + i] = v[s];
+}
+
+// Units of the field-split pass C: two per column up to kxlim, then one per column beyond it
+// (N = 0 there: the epilogue only).
+__host__ __device__ inline int colfwd_split_units(int nh, int kxlim) { return 2 * (kxlim + 1) + (nh - 1 - kxlim); }
+
+// Pass C, unit 2 i + g (g = 0: A, 1: B) of column i <= kxlim: the forward transform of the
+// field, written back in place (kx*FA for A). The second of the column's two CTAs to finish
+// (a per-column counter, no waiting) reads the other field and runs the epilogue. Its
+// loads of the other CTA's column go through L2 (__ldcg) after that CTA's __threadfence.
+template <int N, int R, bool KICK>
+__device__ __forceinline__ void colfwd_field_tile(const NltArgs& a, int unit) {
+  constexpr int T = N / R, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  __shared__ int last;
+  const int t = threadIdx.x;
+  if (unit == 0 && t == 0) *a.flag = 0;  // pass B of this nlt is complete
+  const int nact = 2 * (a.kxlim + 1);
+  if (unit >= nact) {
+    const int i = a.kxlim + 1 + (unit - nact);
+#pragma unroll
+    for (int s = 0; s < R; ++s) epilogue<KICK>(a.epi, i, t + s * T, NH, czero());
+    return;
+  }
+  const int i = unit >> 1, g = unit & 1;
+  const double scale = 0.5 / ((double)N * (double)N);
+  double2* own = g == 0 ? a.u : a.v;
+  double2 v[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = own[(size_t)(t + s * T) * NH + i];
+  fft_regs<N, R, false, 1>(v, smem, t, a.tw, 0);
+  if (g == 0) {
+    const double kxs = __ldg(&a.fkx[i]) * scale;
+#pragma unroll
+    for (int s = 0; s < R; ++s) v[s] = make_double2(kxs * v[s].x, kxs * v[s].y);
+  }
+#pragma unroll
+  for (int s = 0; s < R; ++s) own[(size_t)(t + s * T) * NH + i] = v[s];
+  __threadfence();
+  __syncthreads();
+  if (t == 0) last = atomicAdd(&a.colcnt[i], 1) == 1;
+  __syncthreads();
+  if (!last) return;
+  if (t == 0) a.colcnt[i] = 0;  // ready for the next launch
+  const double2* other = g == 0 ? a.v : a.u;
+  const int kc = a.truncate ? __ldg(&a.kcut[i]) : N;
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    const int j = t + s * T;
+    const double2 o = __ldcg(&other[(size_t)j * NH + i]);
+    const double2 fa = g == 0 ? v[s] : o;
+    const double2 fb = g == 0 ? o : v[s];
+    const double kys = __ldg(&a.fky[j]) * scale;
+    // N = -i (kx A + ky B): re = kx Im A + ky Im B, im = -(kx Re A + ky Re B)
+    double2 nh = make_double2(fma(kys, fb.y, fa.y), -fma(kys, fb.x, fa.x));
+    const int aj = min(j, N - j);
+    if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
+    epilogue<KICK>(a.epi, i, j, NH, nh);
+  }
+}
+
 // ---- single-field kernels ---------------------------------------------------------------
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
@@ -782,6 +896,26 @@ __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltA
     colfwd_colinv_grp_tile<N, Var<N, V>::R>(cur, next, blockIdx.x);
   else if constexpr (Var<N, V>::OK)
     colfwd_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(cur, next, blockIdx.x);
+}
+
+// Field-split column kernels (variants with one column per CTA and no thread groups).
+// At least 3 CTAs per SM (at most 80 registers per thread) for the 8- and 4-value variants, as
+// the fused kernels of those variants reach without a bound.
+template <int N, int V>
+struct SplitVar {
+  static constexpr bool OK = Var<N, V>::OK && !Var<N, V>::GROUPED && Var<N, V>::COLS == 1;
+  static constexpr int THREADS = N / Var<N, V>::R;
+  static constexpr int MINB = V == 0 ? MinBlocks<N>::COL : min_blocks(3, THREADS, 80);
+  static constexpr size_t SMEM = (size_t)padded(N) * sizeof(double2);
+};
+template <int N, int V>
+__global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_nlt_colinv_fs(NltArgs a) {
+  if constexpr (SplitVar<N, V>::OK) colinv_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
+}
+// KICK: the final stage with the fused forcing kick
+template <int N, int V, bool KICK>
+__global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_nlt_colfwd_fs(NltArgs a) {
+  if constexpr (SplitVar<N, V>::OK) colfwd_field_tile<N, Var<N, V>::R, KICK>(a, blockIdx.x);
 }
 
 // ---- ensemble kernels: one launch per pass for every member ------------------------------

@@ -27,6 +27,8 @@ enum OpKind : int {
   OP_NLT_COLFWD_INV = 13,  // pass C of stage nlt + pass A of stage nlt2
   OP_ROW_C2R_F32 = 14,     // row C2R of `a` written as floats to `f32` (dumps)
   OP_ROW_R2C_F32 = 15,     // row R2C of the floats `f32` into `a` (restarts)
+  OP_NLT_COLINV_FS = 16,   // pass A split by field (q must not alias zin)
+  OP_NLT_COLFWD_FS = 17,   // pass C split by field, epilogue by the column's second CTA
 };
 
 struct GtOp {

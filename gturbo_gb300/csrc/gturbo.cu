@@ -66,6 +66,11 @@ struct gt_handle {
   uint32_t *d_lcga = nullptr, *d_lcgb = nullptr;
   double2* d_ff = nullptr;
   int* d_flag = nullptr;
+  // field-split column passes (N <= 2048): q goes to the handle's own field, and pass C's
+  // two CTAs per column meet at a per-column counter
+  double2* d_qscr = nullptr;
+  int* d_colcnt = nullptr;
+  int col_split = 1;  // use them where the column variant allows (gt_set_col_split)
   // diagnostics scratch
   double *d_part = nullptr, *d_rowsum = nullptr, *d_bins = nullptr, *d_fl = nullptr, *d_glob = nullptr;
   double* h_diag = nullptr;  // pinned: bins [nbin*4] + fl [nbin*2] + glob [6]
@@ -97,6 +102,7 @@ NltArgs handle_nlt_args(const gt_handle* h, const double* zin, double* q, double
   a.kin = a.kxlim;
   a.kout = a.kxlim;
   a.flag = flag;
+  a.colcnt = h->d_colcnt;
   a.epi.split = h->split;
   a.epi.emk = h->d_emk;
   a.epi.emkx = h->d_emkx;
@@ -271,7 +277,7 @@ void free_device(gt_handle* h) {
   void* ptrs[] = {h->d_tw, h->d_emk, h->d_kainv, h->d_fkx, h->d_fky, h->d_fkxs, h->d_fkys,
                   h->d_emkx, h->d_emky, h->d_kcut, h->d_jc, h->d_ikxf, h->d_ikyf, h->d_lcga,
                   h->d_lcgb, h->d_ff, h->d_flag, h->d_part, h->d_rowsum, h->d_bins, h->d_fl,
-                  h->d_glob, h->d_fmap};
+                  h->d_glob, h->d_fmap, h->d_qscr, h->d_colcnt};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (h->h_diag) cudaFreeHost(h->h_diag);
@@ -312,6 +318,8 @@ int op_class(int kind) {
     case gt::OP_NLT_ROW: return GT_PROF_NLT_ROW;
     case gt::OP_NLT_COLFWD: return GT_PROF_NLT_COLFWD;
     case gt::OP_NLT_COLFWD_INV: return GT_PROF_NLT_COLFWD_INV;
+    case gt::OP_NLT_COLINV_FS: return GT_PROF_NLT_COLINV;
+    case gt::OP_NLT_COLFWD_FS: return GT_PROF_NLT_COLFWD;
     default: return GT_PROF_OTHER;
   }
 }
@@ -324,11 +332,31 @@ int run(gt_handle* h, const GtOp& op) {
   return GT_OK;
 }
 
+// The field-split column passes run when the handle has their scratch (N <= 2048), the user
+// has not turned them off, and the column variant has one column per CTA without thread groups.
+bool split_active(const gt_handle* h) {
+  const bool one_col = (h->variant == 0 && h->N >= 1024) || h->variant == 1 || h->variant == 2;
+  return h->col_split && h->d_qscr && one_col;
+}
+
 // One nonlinear-term evaluation: input zin, work fields (qbuf receives the transformed q;
-// it may alias zin), u, v; pass C applies the epilogue `epi`.
+// it may alias zin), u, v; pass C applies the epilogue `epi`. The field-split passes put q in
+// the handle's own field instead.
 int nlt_passes(gt_handle* h, const double* zin, double* qbuf, double* u, double* v,
                const gt::EpiArgs& epi) {
   GtOp op = base_op(h);
+  if (split_active(h)) {
+    op.nlt = gt::handle_nlt_args(h, zin, reinterpret_cast<double*>(h->d_qscr), u, v, h->d_flag);
+    op.nlt.epi = epi;
+    op.kind = gt::OP_NLT_COLINV_FS;
+    int rc = run(h, op);
+    if (rc) return rc;
+    op.kind = gt::OP_NLT_ROW;
+    rc = run(h, op);
+    if (rc) return rc;
+    op.kind = gt::OP_NLT_COLFWD_FS;
+    return run(h, op);
+  }
   op.nlt = gt::handle_nlt_args(h, zin, qbuf, u, v, h->d_flag);
   op.nlt.epi = epi;
   op.kind = gt::OP_NLT_COLINV;
@@ -518,6 +546,11 @@ int gt_create(const gt_params* p, gt_handle** out) {
   if (!rc) rc = upload(h, &h->d_lcgb, h->lcgb.data(), h->nf);
   if (!rc) rc = upload(h, &h->d_ff, ff.data(), ff.size());
   if (!rc && h->nf > 0) rc = upload(h, &h->d_fmap, h->fmap.data(), h->fmap.size());
+  if (!rc && N <= 2048) {
+    const std::vector<int> zeros(NH, 0);
+    rc = upload<double2>(h, &h->d_qscr, nullptr, (size_t)N * NH);
+    if (!rc) rc = upload(h, &h->d_colcnt, zeros.data(), NH);
+  }
   const int zeros2[2] = {0, 0};  // untruncated-input flags of even / odd stages
   if (!rc) rc = upload(h, &h->d_flag, zeros2, 2);
   const int ngroups = (N + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
@@ -681,11 +714,34 @@ int gt_nlt(gt_handle* h, double* z, double* u, double* v) {
 int stage_chain(gt_handle* h, int nst, const double* const* zin, double* znl, double* u, double* v,
                 const gt::EpiArgs* epi) {
   GtOp op = base_op(h);
+  const bool split = split_active(h);
+  double* qbuf = split ? reinterpret_cast<double*>(h->d_qscr) : znl;
   auto stage = [&](int k) {
-    gt::NltArgs a = gt::handle_nlt_args(h, zin[k], znl, u, v, h->d_flag + (k & 1));
+    gt::NltArgs a = gt::handle_nlt_args(h, zin[k], qbuf, u, v, h->d_flag + (k & 1));
     a.epi = epi[k];
     return a;
   };
+  if (split) {
+    // pass A of stage 1, then per stage: pass B, pass C, pass A of the next stage
+    op.nlt = stage(0);
+    op.kind = gt::OP_NLT_COLINV_FS;
+    int rc = run(h, op);
+    for (int k = 0; k < nst && !rc; ++k) {
+      op.nlt = stage(k);
+      op.kind = gt::OP_NLT_ROW;
+      rc = run(h, op);
+      if (!rc) {
+        op.kind = gt::OP_NLT_COLFWD_FS;
+        rc = run(h, op);
+      }
+      if (!rc && k + 1 < nst) {
+        op.nlt = stage(k + 1);
+        op.kind = gt::OP_NLT_COLINV_FS;
+        rc = run(h, op);
+      }
+    }
+    return rc;
+  }
   op.nlt = stage(0);
   op.kind = gt::OP_NLT_COLINV;
   int rc = run(h, op);
@@ -880,6 +936,18 @@ int gt_profile_read(gt_handle* h, double* ms, int64_t* launches) {
     launches[h->ev_kind[p]] += 1;
   }
   h->ev_kind.clear();
+  return GT_OK;
+}
+
+int gt_set_col_split(gt_handle* h, int32_t on) {
+  if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_col_split: null handle");
+  h->col_split = on ? 1 : 0;
+  return GT_OK;
+}
+
+int gt_get_col_split(const gt_handle* h, int32_t* active) {
+  if (!h || !active) return fail(nullptr, GT_ERR_ARG, "gt_get_col_split: null argument");
+  *active = split_active(h) ? 1 : 0;
   return GT_OK;
 }
 

@@ -165,6 +165,17 @@ class Solver:
     def variants(self, cr) -> None:
         self._check(self.lib.gt_set_variants(self.h, int(cr[0]), int(cr[1])))
 
+    @property
+    def col_split(self) -> bool:
+        """Whether the field-split column passes run (gt_get_col_split)."""
+        a = ctypes.c_int32()
+        self._check(self.lib.gt_get_col_split(self.h, ctypes.byref(a)))
+        return bool(a.value)
+
+    @col_split.setter
+    def col_split(self, on: bool) -> None:
+        self._check(self.lib.gt_set_col_split(self.h, int(bool(on))))
+
     def supported_variants(self) -> list[int]:
         return [v for v in range(self.NVARIANTS) if self.lib.gt_variant_supported(self.n, v)]
 

@@ -6,7 +6,8 @@
  * interface, arrays `present` on the device) and keeps its argument meaning:
  * the caller owns every field, passes DEVICE pointers to them (Fortran:
  * `!$acc host_data use_device(z,...)`), and the library owns only its tables
- * (wavenumbers, integrating factor, forcing list, twiddles).
+ * (wavenumbers, integrating factor, forcing list, twiddles) and, up to N = 2048,
+ * one spectral scratch field for the field-split column passes.
  *
  * Memory layout of a field (identical to the reference):
  *   spectral  complex(8) z(N/2+1, N)  -> C: double z[N][N/2+1][2], kx fastest
@@ -307,6 +308,14 @@ int gt_get_variant(const gt_handle* h, int32_t* variant);
 /* Select the column and row variants separately. */
 int gt_set_variants(gt_handle* h, int32_t col_variant, int32_t row_variant);
 int gt_get_variants(const gt_handle* h, int32_t* col_variant, int32_t* row_variant);
+/* Field-split column passes (N <= 2048, column variants with one column per CTA and no
+ * thread groups: 0 from N = 1024, 1, 2): each CTA transforms one field of one column, so a
+ * column pass has 3 (pass A) or 2 (pass C) work units per column and the SMs finish together;
+ * q then lives in the handle's scratch field. On by default; gt_set_col_split(h, 0) returns to
+ * one CTA per column. gt_get_col_split reports whether the split passes run with the handle's
+ * current size and column variant. Results are the same to rounding. */
+int gt_set_col_split(gt_handle* h, int32_t on);
+int gt_get_col_split(const gt_handle* h, int32_t* active);
 /* Time `steps` steps of the handle's integrator (RK2 or RK4) on zero fields of its own
  * (allocated and freed here, 5 fields; nothing when only one variant exists): first every
  * supported column variant with its own row tiles, then the other row variants under the

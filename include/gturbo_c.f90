@@ -151,6 +151,12 @@ module gturbo_c
       type(c_ptr), value :: h
       integer(c_int32_t), value :: col_variant, row_variant
     end function
+    ! field-split column passes (on by default where they apply)
+    integer(c_int) function gt_set_col_split(h, on) bind(C, name="gt_set_col_split")
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: h
+      integer(c_int32_t), value :: on
+    end function
     integer(c_int) function gt_autotune(h, steps, ms_per_step, best) bind(C, name="gt_autotune")
       import :: c_int, c_ptr, c_int32_t, c_double
       type(c_ptr), value :: h

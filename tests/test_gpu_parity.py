@@ -241,6 +241,36 @@ def test_forced_step_equals_step_then_forcing(n, rko, kw):
             assert rel_l2(_host(z2), ref) < TOL, (c, r)
 
 
+@pytest.mark.parametrize("n,rko,variant", [(512, 4, 2), (512, 2, 1), (1024, 2, 0), (1024, 4, 2),
+                                           (2048, 2, 1), (2048, 2, 0)])
+def test_col_split_equals_one_cta_per_column(n, rko, variant):
+    """The field-split column passes (one field of one column per CTA, q in the handle's scratch,
+    pass C's epilogue by the column's second CTA) give the same bits as one CTA per column, for
+    steps, forced steps, the nonlinear term of an untruncated field and the split integrator."""
+    kw = dict(alpnu=1.0, alpmu=0.0, nu=1e-3) if (rko == 2 and n == 512) else {}
+    p = _params(n, rko=rko, dt=1e-3, famp=0.5, **kw)
+    orc, sol = Oracle(p), _solver(p)
+    sol.variants = (variant, 1 if variant == 0 and n >= 2048 else variant)
+    a = rand_field(orc, 25) * 20.0
+    out = {}
+    for split in (True, False):
+        sol.col_split = split
+        assert sol.col_split == split
+        z = _dev(a)
+        sol.rk_step(z, sol.work())
+        z2 = _dev(a)
+        s2 = sol.rk_step_forced(z2, sol.work(), 777)
+        zu = _dev(rand_field(orc, 26, truncate=False))
+        u, v = sol.field(), sol.field()
+        sol.nlt(zu, u, v)
+        out[split] = (_host(z), _host(z2), s2, _host(zu))
+    for k in range(4):
+        assert np.array_equal(out[True][k], out[False][k]), k
+    ref = a.copy()
+    orc.rk_step(ref)
+    assert rel_l2(out[True][0], ref) < TOL
+
+
 def test_forced_step_self_conjugate_mode():
     """Without truncation a forced mode can be its own conjugate partner (kx = 0, ky = N/2 or
     the Nyquist column): two kicks on one value. The forced step then runs the step and the
