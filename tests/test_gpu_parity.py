@@ -245,8 +245,10 @@ def test_forced_step_equals_step_then_forcing(n, rko, kw):
                                            (2048, 2, 1), (2048, 2, 0)])
 def test_col_split_equals_one_cta_per_column(n, rko, variant):
     """The field-split column passes (one field of one column per CTA, q in the handle's scratch,
-    pass C's epilogue by the column's second CTA) give the same bits as one CTA per column, for
-    steps, forced steps, the nonlinear term of an untruncated field and the split integrator."""
+    pass C's epilogue by the column's second CTA) agree with one CTA per column to rounding, for
+    steps, forced steps, the nonlinear term of an untruncated field and the split integrator.
+    The arithmetic is the same, but nvcc may contract a stage update into FMAs differently in
+    the two kernels, so the bits may differ by an ulp."""
     kw = dict(alpnu=1.0, alpmu=0.0, nu=1e-3) if (rko == 2 and n == 512) else {}
     p = _params(n, rko=rko, dt=1e-3, famp=0.5, **kw)
     orc, sol = Oracle(p), _solver(p)
@@ -264,8 +266,9 @@ def test_col_split_equals_one_cta_per_column(n, rko, variant):
         u, v = sol.field(), sol.field()
         sol.nlt(zu, u, v)
         out[split] = (_host(z), _host(z2), s2, _host(zu))
-    for k in range(4):
-        assert np.array_equal(out[True][k], out[False][k]), k
+    assert out[True][2] == out[False][2]
+    for k in (0, 1, 3):
+        assert rel_l2(out[True][k], out[False][k]) < 1e-14, k
     ref = a.copy()
     orc.rk_step(ref)
     assert rel_l2(out[True][0], ref) < TOL
