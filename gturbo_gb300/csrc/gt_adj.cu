@@ -217,9 +217,16 @@ gt::GtOp op_of(const gt_handle* h, int kind) {
   return op;
 }
 
+// The three passes of one evaluation from kind k0 (pass A, B, C). The forward passes take the
+// field-split column kernels where the handle runs them; their q buffer (work[0]) never
+// aliases the input here.
 int run3(gt_handle* h, gt::GtOp op, int k0) {
+  const bool split = k0 == gt::OP_NLT_COLINV && gt::handle_col_split(h) &&
+                     static_cast<const void*>(op.nlt.zin) != static_cast<const void*>(op.nlt.q);
   for (int k = 0; k < 3; ++k) {
     op.kind = k0 + k;
+    if (split && k == 0) op.kind = gt::OP_NLT_COLINV_FS;
+    if (split && k == 2) op.kind = gt::OP_NLT_COLFWD_FS;
     const cudaError_t e = gt::handle_dispatch(h, op);
     if (e != cudaSuccess) return acuda(h, e, "adjoint launch");
   }

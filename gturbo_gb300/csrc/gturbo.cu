@@ -380,6 +380,10 @@ gt::EpiArgs make_epi(const gt_handle* h, int mode, double* out, double* znew, co
 
 }  // namespace
 
+namespace gt {
+bool handle_col_split(const gt_handle* h) { return split_active(h); }
+}  // namespace gt
+
 extern "C" {
 
 int gt_create(const gt_params* p, gt_handle** out) {
