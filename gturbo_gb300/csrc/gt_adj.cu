@@ -221,12 +221,16 @@ gt::GtOp op_of(const gt_handle* h, int kind) {
 // field-split column kernels where the handle runs them; their q buffer (work[0]) never
 // aliases the input here.
 int run3(gt_handle* h, gt::GtOp op, int k0) {
-  const bool split = k0 == gt::OP_NLT_COLINV && gt::handle_col_split(h) &&
-                     static_cast<const void*>(op.nlt.zin) != static_cast<const void*>(op.nlt.q);
+  const bool fwd = k0 == gt::OP_NLT_COLINV && gt::handle_col_split(h) &&
+                   static_cast<const void*>(op.nlt.zin) != static_cast<const void*>(op.nlt.q);
+  // the transposed passes likewise (their inputs x and lin never alias the scratch outputs)
+  const bool adj = k0 == gt::OP_ADJ_COLINV && gt::handle_col_split(h);
   for (int k = 0; k < 3; ++k) {
     op.kind = k0 + k;
-    if (split && k == 0) op.kind = gt::OP_NLT_COLINV_FS;
-    if (split && k == 2) op.kind = gt::OP_NLT_COLFWD_FS;
+    if (fwd && k == 0) op.kind = gt::OP_NLT_COLINV_FS;
+    if (fwd && k == 2) op.kind = gt::OP_NLT_COLFWD_FS;
+    if (adj && k == 0) op.kind = gt::OP_ADJ_COLINV_FS;
+    if (adj && k == 2) op.kind = gt::OP_ADJ_COLFWD_FS;
     const cudaError_t e = gt::handle_dispatch(h, op);
     if (e != cudaSuccess) return acuda(h, e, "adjoint launch");
   }
@@ -333,7 +337,9 @@ gt::AdjArgs adj_args(const gt_handle* h) {
   a.split = t.split;
   a.dt = t.dt;
   a.dt2 = t.dt2;
-  a.kxlim = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, nullptr).kxlim;
+  const gt::NltArgs nl = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, nullptr);
+  a.kxlim = nl.kxlim;
+  a.colcnt = nl.colcnt;
   return a;
 }
 

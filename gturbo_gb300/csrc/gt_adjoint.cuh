@@ -281,6 +281,7 @@ struct AdjArgs {
   const double* emky;
   int split;
   double dt, dt2;
+  int* colcnt;         // per-column counters of the field-split transposed pass C (NH ints, zero)
 };
 
 template <int N, int C, int R = 16>
@@ -518,6 +519,113 @@ __device__ __forceinline__ void adj_colfwd_tile(const AdjArgs& a, int tile) {
   }
 }
 
+// ---- field-split transposed column tiles (one field of one column per CTA, C = 1) ---------------
+
+// Fields of the transposed pass A: q, u, v from x (f = 0, 1, 2) and a, b from lin (3, 4); with
+// the physical fields of x only a and b, on the columns up to kxlim.
+__host__ __device__ inline int adj_colinv_split_units(int nh, int kxlim, bool phys) {
+  return phys ? 2 * (kxlim + 1) : 5 * nh;
+}
+
+template <int N, int R>
+__device__ __forceinline__ void adj_colinv_field_tile(const AdjArgs& a, int unit) {
+  constexpr int T = N / R, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  const bool phys = a.phys_uv != nullptr;
+  const int nfield = phys ? 2 : 5;
+  const int i = unit / nfield, f = (phys ? 3 : 0) + unit % nfield, t = threadIdx.x;
+  const double kx = __ldg(&a.fkx[i]);
+  const int kc = a.truncate ? __ldg(&a.kcut[i]) : N;
+  const double wcol = (i == 0 || i == NH - 1) ? 1.0 : 0.5;
+  double2* dst = f == 0 ? a.q : f == 1 ? a.u : f == 2 ? a.v : f == 3 ? a.a : a.b;
+  double2 v[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    const int j = t + s * T;
+    const size_t o = (size_t)j * NH + i;
+    if (f < 3) {
+      const double2 q = a.x[o];
+      if (f == 0) {
+        v[s] = q;
+      } else if (f == 1) {
+        const double m = __ldg(&a.fky[j]) * __ldg(&a.kainv[o]);
+        v[s] = make_double2(-m * q.y, m * q.x);
+      } else {
+        const double m = kx * __ldg(&a.kainv[o]);
+        v[s] = make_double2(m * q.y, -m * q.x);
+      }
+    } else {
+      double2 l = a.lin[o];
+      if (a.mode == ADJ_STAGE_B) {
+        const double e = stage_e(a.emk, a.emkx, a.emky, a.split, i, j, NH) * a.dt;
+        l = (i == 0 && j == 0) ? czero() : make_double2(e * l.x, e * l.y);
+      }
+      if (min(j, N - j) > kc || (i == 0 && j == 0 && a.truncate)) l = czero();
+      // w o (i k) l
+      const double k = (f == 3 ? kx : __ldg(&a.fky[j])) * wcol;
+      v[s] = make_double2(-k * l.y, k * l.x);
+    }
+  }
+  fft_regs<N, R, true, 1>(v, smem, t, a.tw, 0);
+#pragma unroll
+  for (int s = 0; s < R; ++s) dst[(size_t)(t + s * T) * NH + i] = v[s];
+}
+
+// Transposed pass C, field f of column i (unit 3 i + f; f = 0, 1, 2: q, u, v): the forward
+// transform written back in place; the third of the column's CTAs to finish (a per-column
+// counter, no waiting) reads the other two through L2, forms the accumulated gradient in the
+// order q, u, v of adj_colfwd_tile and runs the stage update.
+template <int N, int R>
+__device__ __forceinline__ void adj_colfwd_field_tile(const AdjArgs& a, int unit) {
+  constexpr int T = N / R, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  __shared__ int last;
+  const int i = unit / 3, f = unit % 3, t = threadIdx.x;
+  double2* own = f == 0 ? a.q : f == 1 ? a.u : a.v;
+  double2 v[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = own[(size_t)(t + s * T) * NH + i];
+  fft_regs<N, R, false, 1>(v, smem, t, a.tw, 0);
+#pragma unroll
+  for (int s = 0; s < R; ++s) own[(size_t)(t + s * T) * NH + i] = v[s];
+  __threadfence();
+  __syncthreads();
+  if (t == 0) last = atomicAdd(&a.colcnt[i], 1) == 2;
+  __syncthreads();
+  if (!last) return;
+  if (t == 0) a.colcnt[i] = 0;  // ready for the next launch
+  const double kx = __ldg(&a.fkx[i]);
+  // c o (.)/2: the row pass delivered 2 FFT(s); c = 1 on kx=0 and Nyquist, 2 inside
+  const double cw = (i == 0 || i == NH - 1) ? 0.5 : 1.0;
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    const int j = t + s * T;
+    const size_t o = (size_t)j * NH + i;
+    const double2 fq = f == 0 ? v[s] : __ldcg(&a.q[o]);
+    const double2 fu = f == 1 ? v[s] : __ldcg(&a.u[o]);
+    const double2 fv = f == 2 ? v[s] : __ldcg(&a.v[o]);
+    // conj(Mu) = -i ky/|k|^a, conj(Mv) = +i kx/|k|^a
+    double2 g = make_double2(cw * fq.x, cw * fq.y);
+    const double mu = -__ldg(&a.fky[j]) * __ldg(&a.kainv[o]) * cw;
+    g = make_double2(fma(-mu, fu.y, g.x), fma(mu, fu.x, g.y));
+    const double mv = kx * __ldg(&a.kainv[o]) * cw;
+    g = make_double2(fma(-mv, fv.y, g.x), fma(mv, fv.x, g.y));
+    a.q[o] = g;
+    if (a.mode == ADJ_STAGE_B) {
+      const double e = stage_e(a.emk, a.emkx, a.emky, a.split, i, j, NH);
+      const bool origin = (i == 0 && j == 0);
+      const double2 l = a.lin[o];
+      a.lam[o] = origin ? czero() : make_double2(e * (e * l.x + g.x), e * (e * l.y + g.y));
+      a.rho[o] = origin ? czero() : make_double2(a.dt2 * e * g.x, a.dt2 * e * g.y);
+    } else if (a.mode == ADJ_PLAIN) {
+      a.lam[o] = g;
+    } else {
+      const double2 l = a.lam[o];
+      a.lam[o] = make_double2(l.x + g.x, l.y + g.y);
+    }
+  }
+}
+
 // ---- kernels ------------------------------------------------------------------------------
 template <int N>
 struct AdjShape {
@@ -585,6 +693,20 @@ __global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_adjv_row(AdjArgs a) 
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_adjv_colfwd(AdjArgs a) {
   if constexpr (AdjVar<N, V>::OK) adj_colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
+}
+
+// the field-split transposed column passes (variants with one column per CTA, no groups)
+template <int N, int V>
+struct AdjSplitVar {
+  static constexpr bool OK = SplitVar<N, V>::OK && AdjShape<N>::OK;
+};
+template <int N, int V>
+__global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_adj_colinv_fs(AdjArgs a) {
+  if constexpr (AdjSplitVar<N, V>::OK) adj_colinv_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
+}
+template <int N, int V>
+__global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_adj_colfwd_fs(AdjArgs a) {
+  if constexpr (AdjSplitVar<N, V>::OK) adj_colfwd_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
 }
 
 }  // namespace gt

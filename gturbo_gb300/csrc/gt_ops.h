@@ -29,6 +29,8 @@ enum OpKind : int {
   OP_ROW_R2C_F32 = 15,     // row R2C of the floats `f32` into `a` (restarts)
   OP_NLT_COLINV_FS = 16,   // pass A split by field (q must not alias zin)
   OP_NLT_COLFWD_FS = 17,   // pass C split by field, epilogue by the column's second CTA
+  OP_ADJ_COLINV_FS = 18,   // transposed pass A split by field
+  OP_ADJ_COLFWD_FS = 19,   // transposed pass C split by field, update by the column's third CTA
 };
 
 struct GtOp {
