@@ -16,6 +16,8 @@
 // without transforming, and pass A stores zeros without transforming for any such column
 // block whose input is entirely zero. A device flag tells pass B whether any column beyond
 // kxlim carried data (an untruncated input); only then does pass B read those columns.
+// Up to 2048^2 the column passes A and C also exist split by field (one field of one column per
+// CTA, the *_field_tile functions), which evens out the SMs' share of the 2/3-rule columns.
 #pragma once
 
 #include "gt_fft.cuh"
