@@ -713,8 +713,10 @@ int gt_nlt(gt_handle* h, double* z, double* u, double* v) {
 
 // The stages of one Runge-Kutta step: stage k evaluates N at zin[k] (the first from z, the
 // others from znl, where the previous stage's epilogue left its value) and applies epi[k].
-// Pass C of stage k and pass A of stage k+1 run as one column kernel; the stages alternate
-// between the handle's two untruncated-input flags.
+// Pass C of stage k and pass A of stage k+1 run as one column kernel, or, with the field-split
+// column passes, as two (q then goes to the handle's scratch field, since znl is both the next
+// stage's input and, in the fused kernel, its q output). The stages alternate between the
+// handle's two untruncated-input flags.
 int stage_chain(gt_handle* h, int nst, const double* const* zin, double* znl, double* u, double* v,
                 const gt::EpiArgs* epi) {
   GtOp op = base_op(h);
