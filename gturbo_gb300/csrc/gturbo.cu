@@ -1065,6 +1065,13 @@ int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best)
         best_r = r;
       }
     }
+    // stage 3: the best pair with one CTA per column, where the field-split passes ran
+    h->variant = best_c;
+    if (!rc && h->col_split && split_active(h)) {
+      h->col_split = 0;
+      const double t = time_pair(best_c, best_r);
+      if (rc || !(t < best_ms)) h->col_split = 1;
+    }
     if (buf) {
       cudaStreamSynchronize(h->stream);
       cudaFree(buf);

@@ -187,8 +187,8 @@ class Solver:
 
         With a cache file (JSON, keyed by device name, N, integrator order and the library
         file's size and time), a stored choice is reused without timing; None disables it. Returns
-        {"variant": column variant, "row_variant": row variant, "ms_per_step": per column
-        variant or None, "cached": bool}.
+        {"variant": column variant, "row_variant": row variant, "col_split": whether the
+        field-split column passes run, "ms_per_step": per column variant or None, "cached": bool}.
         """
         if cache == "default":
             cache = _tune_cache_default()
@@ -201,15 +201,19 @@ class Solver:
         if (hit and hit.get("variant") in self.supported_variants()
                 and hit.get("row_variant") in self.supported_row_variants()):
             self.variants = (hit["variant"], hit["row_variant"])
+            if "col_split" in hit:
+                self.col_split = hit["col_split"]
             return {"variant": hit["variant"], "row_variant": hit["row_variant"],
-                    "ms_per_step": hit.get("ms_per_step"), "cached": True}
+                    "col_split": self.col_split, "ms_per_step": hit.get("ms_per_step"), "cached": True}
         ms = (ctypes.c_double * self.NVARIANTS)()
         best = ctypes.c_int32()
         self._check(self.lib.gt_autotune(self.h, int(steps), ms, ctypes.byref(best)))
         col, row = self.variants
-        res = {"variant": col, "row_variant": row, "ms_per_step": list(ms), "cached": False}
+        split = self.col_split
+        res = {"variant": col, "row_variant": row, "col_split": split, "ms_per_step": list(ms),
+               "cached": False}
         if cache is not None:
-            table[key] = {"variant": col, "row_variant": row, "ms_per_step": list(ms)}
+            table[key] = {"variant": col, "row_variant": row, "col_split": split, "ms_per_step": list(ms)}
             _write_cache(cache, table)
         return res
 

@@ -319,7 +319,9 @@ int gt_get_col_split(const gt_handle* h, int32_t* active);
 /* Time `steps` steps of the handle's integrator (RK2 or RK4) on zero fields of its own
  * (allocated and freed here, 5 fields; nothing when only one variant exists): first every
  * supported column variant with its own row tiles, then the other row variants under the
- * fastest column variant. Keeps the fastest pair; returns ms per step of each column variant
+ * fastest column variant, then (where the field-split column passes ran) that pair with one
+ * CTA per column, turning the split off if that is faster. Keeps the fastest pair; returns ms
+ * per step of each column variant
  * in ms_per_step[GT_NVARIANTS] (-1 for unsupported variants) and the column choice in *best
  * (either pointer may be null; gt_get_variants gives the pair). Synchronous. */
 int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best);
