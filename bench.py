@@ -485,7 +485,7 @@ def ours_arm(args):
                 "config": {"workload": desc, "n": p.n, "alpha": p.alpv, "rk": p.rko,
                            "imix": p.imix, "diag_calls_timed": ndiag,
                            "launch_variant": tune["variant"],
-                           "row_variant": sol.variants[1],
+                           "row_variant": sol.variants[1], "col_split": sol.col_split,
                            "autotune_ms_per_step": tune["ms_per_step"],
                            "parallelism": f"replicas x{world}" if world > 1 else "single",
                            "l2": "no flush: working set ~168 MB > 126 MB L2"},
