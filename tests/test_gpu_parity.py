@@ -241,19 +241,20 @@ def test_forced_step_equals_step_then_forcing(n, rko, kw):
             assert rel_l2(_host(z2), ref) < TOL, (c, r)
 
 
-@pytest.mark.parametrize("n,rko,variant", [(512, 4, 2), (512, 2, 1), (1024, 2, 0), (1024, 4, 2),
-                                           (2048, 2, 1), (2048, 2, 0)])
-def test_col_split_equals_one_cta_per_column(n, rko, variant):
+@pytest.mark.parametrize("n,rko,variant,truncate", [(512, 4, 2, 1), (512, 2, 1, 1), (1024, 2, 0, 1),
+                                                    (1024, 4, 2, 1), (2048, 2, 1, 1), (2048, 2, 0, 1),
+                                                    (1024, 2, 2, 0), (512, 4, 1, 0)])
+def test_col_split_equals_one_cta_per_column(n, rko, variant, truncate):
     """The field-split column passes (one field of one column per CTA, q in the handle's scratch,
     pass C's epilogue by the column's second CTA) agree with one CTA per column to rounding, for
     steps, forced steps, the nonlinear term of an untruncated field and the split integrator.
     The arithmetic is the same, but nvcc may contract a stage update into FMAs differently in
     the two kernels, so the bits may differ by an ulp."""
     kw = dict(alpnu=1.0, alpmu=0.0, nu=1e-3) if (rko == 2 and n == 512) else {}
-    p = _params(n, rko=rko, dt=1e-3, famp=0.5, **kw)
+    p = _params(n, rko=rko, dt=1e-3, famp=0.5, truncate=truncate, **kw)
     orc, sol = Oracle(p), _solver(p)
     sol.variants = (variant, 1 if variant == 0 and n >= 2048 else variant)
-    a = rand_field(orc, 25) * 20.0
+    a = rand_field(orc, 25, truncate=bool(truncate)) * 20.0
     out = {}
     for split in (True, False):
         sol.col_split = split
