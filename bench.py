@@ -6,7 +6,7 @@ Workload (default ``--config c2``): the 2048^2 SQG-like run -- alpha=1, Lawson R
 hyperviscosity (2/3 N/2)^-16 k^16, drag mu=0.1, stochastic forcing on 20 < |k| <= 22 with
 injection rate 1 (the reference's LCG, seed 481929), diagnostics (spectra, fluxes, budgets) every
 100 steps, random-phase initial field with E(k) ~ k^4 exp(-(k/10)^2), E=0.5. Inputs are synthetic
-and resident in HBM; the working set (4 fields + 2 tables, ~168 MB) exceeds the 126 MB L2, so no
+and resident in HBM; the working set (4 fields + 2 tables + the q scratch, ~202 MB) exceeds the 126 MB L2, so no
 flush is needed between steps.
 
 A "step" is one iteration of the reference's main loop (src/main.f90:97-137): the RK step,
@@ -488,7 +488,7 @@ def ours_arm(args):
                            "row_variant": sol.variants[1], "col_split": sol.col_split,
                            "autotune_ms_per_step": tune["ms_per_step"],
                            "parallelism": f"replicas x{world}" if world > 1 else "single",
-                           "l2": "no flush: working set ~168 MB > 126 MB L2"},
+                           "l2": "no flush: working set ~202 MB > 126 MB L2"},
                 "gpu_launches": launches, "finite": finite, "clocks": clk}
         line.update(extras)
         print(json.dumps(line), flush=True)
