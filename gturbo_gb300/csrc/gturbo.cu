@@ -527,6 +527,7 @@ int gt_create(const gt_params* p, gt_handle** out) {
   if (e != cudaSuccess) rc = cuda_fail(h, e, "cudaGetDevice");
   if (!rc) {
     e = prepare_for(N);
+    if (e == cudaSuccess && N >= 4096) e = gt::diag_prepare();
     if (e != cudaSuccess) rc = cuda_fail(h, e, "cudaFuncSetAttribute");
   }
   std::vector<double2> tw;
@@ -557,7 +558,7 @@ int gt_create(const gt_params* p, gt_handle** out) {
   }
   const int zeros2[2] = {0, 0};  // untruncated-input flags of even / odd stages
   if (!rc) rc = upload(h, &h->d_flag, zeros2, 2);
-  const int ngroups = (N + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
+  const int ngroups = gt::diag_groups(N);
   if (!rc) rc = upload<double>(h, &h->d_part, nullptr, (size_t)ngroups * h->NBIN * 4);
   if (!rc) rc = upload<double>(h, &h->d_rowsum, nullptr, (size_t)N * 6);
   if (!rc) rc = upload<double>(h, &h->d_bins, nullptr, (size_t)h->NBIN * 4);
@@ -876,6 +877,8 @@ int gt_diag(gt_handle* h, const double* z, const double* znl, double* sp, double
   D.mu = h->p.mu;
   D.alpnu = h->p.alpnu;
   D.alpmu = h->p.alpmu;
+  D.inu = gt::diag_int_exponent(h->p.alpnu);
+  D.imu = gt::diag_int_exponent(h->p.alpmu);
   D.part = h->d_part;
   D.rowsum = h->d_rowsum;
   const int nb = h->NBIN;
@@ -885,21 +888,19 @@ int gt_diag(gt_handle* h, const double* z, const double* znl, double* sp, double
   const bool want_bins = sp || sz || fle || flz;
   const int pair = prof_begin(h, GT_PROF_DIAG);
   if (want_bins) {
-    const int ngroups = (h->N + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
-    const int nthr = ngroups * nb;
-    gt::k_diag_bins<<<(nthr + 127) / 128, 128, 0, h->stream>>>(D);
+    gt::diag_launch_bins(D, h->stream);
     gt::k_diag_bins_final<<<(nb + 127) / 128, 128, 0, h->stream>>>(D, h->d_bins);
     GT_CUDA(h, cudaGetLastError());
     GT_CUDA(h, cudaMemcpyAsync(hb, h->d_bins, sizeof(double) * nb * 4, cudaMemcpyDeviceToHost, h->stream));
     if (znl) {
-      gt::k_diag_suffix<<<(nb + 127) / 128, 128, 0, h->stream>>>(h->d_bins, h->d_fl, nb);
+      gt::k_diag_suffix<<<1, gt::kDiagThreads, gt::diag_suffix_smem(h->N), h->stream>>>(h->d_bins, h->d_fl, nb);
       GT_CUDA(h, cudaGetLastError());
       GT_CUDA(h, cudaMemcpyAsync(hf, h->d_fl, sizeof(double) * nb * 2, cudaMemcpyDeviceToHost, h->stream));
     }
   }
   if (glob) {
     gt::k_diag_glob_rows<<<h->N, 256, 0, h->stream>>>(D);
-    gt::k_diag_glob_final<<<1, 32, 0, h->stream>>>(D, h->d_glob);
+    gt::k_diag_glob_final<<<1, 192, 0, h->stream>>>(D, h->d_glob);
     GT_CUDA(h, cudaGetLastError());
     GT_CUDA(h, cudaMemcpyAsync(hg, h->d_glob, sizeof(double) * 6, cudaMemcpyDeviceToHost, h->stream));
   }
@@ -1113,7 +1114,7 @@ namespace {
 constexpr int kStaticMaxN = GT_DIAG_STATIC_MAX_N;
 constexpr int kStaticMaxNH = kStaticMaxN / 2 + 1;
 constexpr int kStaticMaxBin = kStaticMaxN / 2;
-constexpr int kStaticGroups = (kStaticMaxN + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
+constexpr int kStaticGroups = gt::diag_groups(kStaticMaxN);
 constexpr size_t kOffFkxs = 0;
 constexpr size_t kOffFkys = kOffFkxs + ((kStaticMaxNH + 31) / 32) * 32;
 constexpr size_t kOffPart = kOffFkys + kStaticMaxN;
@@ -1196,22 +1197,23 @@ extern "C" int gt_diag_static(const gt_params* p, const double* z, const double*
   D.mu = p->mu;
   D.alpnu = p->alpnu;
   D.alpmu = p->alpmu;
+  D.inu = gt::diag_int_exponent(p->alpnu);
+  D.imu = gt::diag_int_exponent(p->alpmu);
   D.part = base + kOffPart;
   D.rowsum = base + kOffRows;
   const double dky = 2.0 * 3.14159265358979323846 / p->xly;
   D.unit_k = (D.dk == 1.0 && dky == 1.0) ? 1 : 0;
   k_static_k2<<<(n + 127) / 128, 128, 0, s>>>(base + kOffFkxs, base + kOffFkys, n, D.dk, dky);
   if (sp || sz || fle || flz) {
-    const int ngroups = (n + gt::kDiagRowGroup - 1) / gt::kDiagRowGroup;
-    gt::k_diag_bins<<<(ngroups * nb + 127) / 128, 128, 0, s>>>(D);
+    gt::diag_launch_bins(D, s);
     gt::k_diag_bins_final<<<(nb + 127) / 128, 128, 0, s>>>(D, base + kOffBins);
-    if (znl) gt::k_diag_suffix<<<(nb + 127) / 128, 128, 0, s>>>(base + kOffBins, base + kOffFl, nb);
+    if (znl) gt::k_diag_suffix<<<1, gt::kDiagThreads, gt::diag_suffix_smem(n), s>>>(base + kOffBins, base + kOffFl, nb);
     k_static_scatter<<<(nb + 127) / 128, 128, 0, s>>>(base + kOffBins, base + kOffFl, sp, sz,
                                                        znl ? fle : nullptr, znl ? flz : nullptr, nb);
   }
   if (glob) {
     gt::k_diag_glob_rows<<<n, 256, 0, s>>>(D);
-    gt::k_diag_glob_final<<<1, 32, 0, s>>>(D, glob);
+    gt::k_diag_glob_final<<<1, 192, 0, s>>>(D, glob);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "gt_diag_static: launch");
