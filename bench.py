@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip e2e / cpu / ref-equivalent legs")
     ap.add_argument("--variant", type=int, default=None,
                     help="launch variant of the nonlinear-term passes (default: autotuned)")
+    ap.add_argument("--row-variant", type=int, default=None,
+                    help="with --variant: the row passes' own launch variant (default: the same)")
     ap.add_argument("--adjoint-rk", type=int, choices=[2, 4], default=2,
                     help="integrator of the --only adjoint leg (the bench's own leg is RK2)")
     ap.add_argument("--only", choices=["ensemble", "adjoint"], default=None,
@@ -314,6 +316,8 @@ def ours_arm(args):
         tune = sol.autotune(steps=50 if p.n <= 1024 else 10, cache=None)
     else:
         sol.variant = args.variant
+        if args.row_variant is not None:
+            sol.variants = (args.variant, args.row_variant)
         tune = {"variant": args.variant, "ms_per_step": None}
     stream = sol.stream
     work = sol.work()
