@@ -51,20 +51,16 @@ struct EpiArgs {
   // where (i, j) is the conjugate partner of mode k on the kx = 0 or Nyquist column.
   const int* fmap;
   int fwi, fwj, fh;
-  const uint32_t* lcga;  // jump-ahead coefficients of the k-th draw
-  const uint32_t* lcgb;
-  const double2* ff;     // per-mode amplitude factors
-  uint32_t seed0;        // LCG state before the kick
-  double sf;             // sqrt(dt) * famp
+  const double2* kick;   // this step's per-mode increments (forcing_increment)
 };
 
-// The kick of forced mode k added to value a: phase te = 2 pi rann of the (k+1)-th LCG draw from
-// seed0 (x -> 69069 x + 1 mod 2^31, rann rounded to real(4) as in the reference), a + sf ff
-// (cos te, +-sin te) (minus for the conjugate partner). The one definition serves the forcing
-// kernel and the fused final-stage store, so both give the same bits.
-__device__ __forceinline__ double2 forcing_kick(double2 a, int k, bool conj, const uint32_t* lcga,
-                                                const uint32_t* lcgb, const double2* ff,
-                                                uint32_t seed0, double sf) {
+// The kick of forced mode k: phase te = 2 pi rann of the (k+1)-th LCG draw from seed0
+// (x -> 69069 x + 1 mod 2^31, rann rounded to real(4) as in the reference); the value gains
+// sf ff (cos te, sin te), its conjugate partner sf ff (cos te, -sin te). forcing_increment and
+// add_kick are the one definition that the forcing kernel and the fused final-stage store share,
+// so both give the same bits.
+__device__ __forceinline__ double2 forcing_increment(int k, const uint32_t* lcga, const uint32_t* lcgb,
+                                                     const double2* ff, uint32_t seed0, double sf) {
   const double pi2 = 2.0 * 3.14159265358979;  // forcing.f90:10
   const uint32_t x = (__ldg(&lcga[k]) * seed0 + __ldg(&lcgb[k])) & 0x7FFFFFFFu;
   const float rr = (float)((double)x / 2147483647.0);
@@ -72,9 +68,10 @@ __device__ __forceinline__ double2 forcing_kick(double2 a, int k, bool conj, con
   double sn, cs;
   sincos(te, &sn, &cs);
   const double2 f = __ldg(&ff[k]);
-  a.x = fma(sf * f.x, cs, a.x);
-  a.y = conj ? fma(-(sf * f.y), sn, a.y) : fma(sf * f.y, sn, a.y);
-  return a;
+  return make_double2((sf * f.x) * cs, (sf * f.y) * sn);
+}
+__device__ __forceinline__ double2 add_kick(double2 a, double2 inc, bool conj) {
+  return make_double2(a.x + inc.x, conj ? a.y - inc.y : a.y + inc.y);
 }
 
 // The fused kick at (i, j) of an N x NH field, if (i, j) is forced.
@@ -87,7 +84,7 @@ __device__ __forceinline__ double2 fused_kick(const EpiArgs& E, int i, int j, in
   else return r;
   const int e = __ldg(&E.fmap[i * E.fh + jj]);
   if (e < 0) return r;
-  return forcing_kick(r, e & 0x3FFFFFFF, (e >> 30) & 1, E.lcga, E.lcgb, E.ff, E.seed0, E.sf);
+  return add_kick(r, E.kick[e & 0x3FFFFFFF], (e >> 30) & 1);
 }
 
 // KICK: the fused forcing kick is compiled in (the final stage's pass C only; the intermediate

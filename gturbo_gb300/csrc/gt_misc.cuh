@@ -46,12 +46,21 @@ __global__ void k_forcing(double2* z, int nh, int nf, const int* __restrict__ ik
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nf) return;
   const int i = ikx[k], j = iky[k];
+  const double2 inc = forcing_increment(k, lcga, lcgb, ff, seed0, sf);
   double2* p = z + (size_t)j * nh + i;
-  *p = forcing_kick(*p, k, false, lcga, lcgb, ff, seed0, sf);
+  *p = add_kick(*p, inc, false);
   if (i == 0 || i == nh - 1) {
     double2* pc = z + (size_t)jc[j] * nh + i;
-    *pc = forcing_kick(*pc, k, true, lcga, lcgb, ff, seed0, sf);
+    *pc = add_kick(*pc, inc, true);
   }
+}
+
+// This step's kick increments of the nf forced modes, for the fused final-stage store.
+__global__ void k_kick_values(double2* kick, int nf, const uint32_t* __restrict__ lcga,
+                              const uint32_t* __restrict__ lcgb, const double2* __restrict__ ff,
+                              uint32_t seed0, double sf) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nf) kick[k] = forcing_increment(k, lcga, lcgb, ff, seed0, sf);
 }
 
 // ---------------------------------------------------------------------------------------

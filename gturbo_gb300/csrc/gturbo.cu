@@ -51,6 +51,10 @@ struct gt_handle {
   // on one value (a self-conjugate mode), which keeps the separate forcing launch
   std::vector<int> fmap;
   int fwi = 0, fwj = 0, fh = 0, fuse_ok = 0;
+  // the step's kick increments, computed on a side stream while the step's first passes run
+  double2* d_kick = nullptr;
+  cudaStream_t kick_stream = nullptr;
+  cudaEvent_t kick_fork = nullptr, kick_join = nullptr;
   int device = 0;
   int variant = 0;      // launch variant of the column passes
   int row_variant = 0;  // launch variant of the row passes
@@ -277,7 +281,7 @@ void free_device(gt_handle* h) {
   void* ptrs[] = {h->d_tw, h->d_emk, h->d_kainv, h->d_fkx, h->d_fky, h->d_fkxs, h->d_fkys,
                   h->d_emkx, h->d_emky, h->d_kcut, h->d_jc, h->d_ikxf, h->d_ikyf, h->d_lcga,
                   h->d_lcgb, h->d_ff, h->d_flag, h->d_part, h->d_rowsum, h->d_bins, h->d_fl,
-                  h->d_glob, h->d_fmap, h->d_qscr, h->d_colcnt};
+                  h->d_glob, h->d_fmap, h->d_qscr, h->d_colcnt, h->d_kick};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (h->h_diag) cudaFreeHost(h->h_diag);
@@ -551,6 +555,7 @@ int gt_create(const gt_params* p, gt_handle** out) {
   if (!rc) rc = upload(h, &h->d_lcgb, h->lcgb.data(), h->nf);
   if (!rc) rc = upload(h, &h->d_ff, ff.data(), ff.size());
   if (!rc && h->nf > 0) rc = upload(h, &h->d_fmap, h->fmap.data(), h->fmap.size());
+  if (!rc && h->nf > 0) rc = upload<double2>(h, &h->d_kick, nullptr, (size_t)h->nf);
   if (!rc && N <= 2048) {
     const std::vector<int> zeros(NH, 0);
     rc = upload<double2>(h, &h->d_qscr, nullptr, (size_t)N * NH);
@@ -589,6 +594,9 @@ int gt_destroy(gt_handle* h) {
   if (!h) return GT_OK;
   cudaDeviceSynchronize();
   for (cudaEvent_t ev : h->ev_pool) cudaEventDestroy(ev);
+  if (h->kick_fork) cudaEventDestroy(h->kick_fork);
+  if (h->kick_join) cudaEventDestroy(h->kick_join);
+  if (h->kick_stream) cudaStreamDestroy(h->kick_stream);
   free_device(h);
   delete h;
   return GT_OK;
@@ -719,7 +727,13 @@ int gt_nlt(gt_handle* h, double* z, double* u, double* v) {
 // stage's input and, in the fused kernel, its q output). The stages alternate between the
 // handle's two untruncated-input flags.
 int stage_chain(gt_handle* h, int nst, const double* const* zin, double* znl, double* u, double* v,
-                const gt::EpiArgs* epi) {
+                const gt::EpiArgs* epi, cudaEvent_t join = nullptr) {
+  // the final pass C waits for `join` (the fused kick's increments) when given
+  auto await_join = [&](int k) -> int {
+    if (!join || k + 1 != nst) return GT_OK;
+    const cudaError_t e = cudaStreamWaitEvent(h->stream, join, 0);
+    return e == cudaSuccess ? GT_OK : cuda_fail(h, e, "cudaStreamWaitEvent");
+  };
   GtOp op = base_op(h);
   const bool split = split_active(h);
   double* qbuf = split ? reinterpret_cast<double*>(h->d_qscr) : znl;
@@ -737,6 +751,7 @@ int stage_chain(gt_handle* h, int nst, const double* const* zin, double* znl, do
       op.nlt = stage(k);
       op.kind = gt::OP_NLT_ROW;
       rc = run(h, op);
+      if (!rc) rc = await_join(k);
       if (!rc) {
         op.kind = gt::OP_NLT_COLFWD_FS;
         rc = run(h, op);
@@ -762,6 +777,8 @@ int stage_chain(gt_handle* h, int nst, const double* const* zin, double* znl, do
       op.kind = gt::OP_NLT_COLFWD_INV;
     } else {
       op.kind = gt::OP_NLT_COLFWD;
+      rc = await_join(k);
+      if (rc) break;
     }
     rc = run(h, op);
   }
@@ -785,17 +802,33 @@ int gt_step_rk4(gt_handle* h, double* z, double* znl, double* znew, double* u, d
   return stage_chain(h, 4, zin, znl, u, v, epi);
 }
 
-// The final stage's fused kick from LCG state x0 (forcing.f90:16-33).
-static void set_fused_kick(const gt_handle* h, gt::EpiArgs& E, uint32_t x0) {
+// The final stage's fused kick from LCG state x0 (forcing.f90:16-33): the nf increments are
+// computed on a side stream that forks from the handle's stream before the step, and the final
+// pass C waits for them (the returned event). The sincos of the phases thus stays off the
+// final pass's critical path.
+static int start_fused_kick(gt_handle* h, gt::EpiArgs& E, uint32_t x0, cudaEvent_t* join) {
+  cudaError_t e = cudaSuccess;
+  if (!h->kick_stream) {
+    e = cudaStreamCreateWithFlags(&h->kick_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->kick_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->kick_join, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(h, e, "fused kick: stream set-up");
+  }
+  e = cudaEventRecord(h->kick_fork, h->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(h->kick_stream, h->kick_fork, 0);
+  if (e != cudaSuccess) return cuda_fail(h, e, "fused kick: fork");
+  gt::k_kick_values<<<(h->nf + 127) / 128, 128, 0, h->kick_stream>>>(h->d_kick, h->nf, h->d_lcga, h->d_lcgb,
+                                                                       h->d_ff, x0, h->sdt * h->p.famp);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaEventRecord(h->kick_join, h->kick_stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "fused kick: increments");
   E.fmap = h->d_fmap;
   E.fwi = h->fwi;
   E.fwj = h->fwj;
   E.fh = h->fh;
-  E.lcga = h->d_lcga;
-  E.lcgb = h->d_lcgb;
-  E.ff = h->d_ff;
-  E.seed0 = x0;
-  E.sf = h->sdt * h->p.famp;
+  E.kick = h->d_kick;
+  *join = h->kick_join;
+  return GT_OK;
 }
 
 int gt_step_rk2_forced(gt_handle* h, double* z, double* znl, double* u, double* v, int32_t* seed) {
@@ -807,9 +840,11 @@ int gt_step_rk2_forced(gt_handle* h, double* z, double* znl, double* u, double* 
   gt::EpiArgs epi[2] = {make_epi(h, gt::EPI_RK2A, znl, nullptr, z),
                         make_epi(h, gt::EPI_RK2B, z, nullptr, z)};
   const uint32_t x0 = (uint32_t)(*seed);
-  set_fused_kick(h, epi[1], x0);
+  cudaEvent_t join = nullptr;
+  int rc = start_fused_kick(h, epi[1], x0, &join);
+  if (rc) return rc;
   const double* zin[2] = {z, znl};
-  const int rc = stage_chain(h, 2, zin, znl, u, v, epi);
+  rc = stage_chain(h, 2, zin, znl, u, v, epi, join);
   if (rc) return rc;
   *seed = (int32_t)((h->lcga_nf * x0 + h->lcgb_nf) & 0x7FFFFFFFu);
   return GT_OK;
@@ -827,9 +862,11 @@ int gt_step_rk4_forced(gt_handle* h, double* z, double* znl, double* znew, doubl
   gt::EpiArgs epi[4] = {make_epi(h, gt::EPI_RK4A, znl, znew, z), make_epi(h, gt::EPI_RK4B, znl, znew, z),
                         make_epi(h, gt::EPI_RK4C, znl, znew, z), make_epi(h, gt::EPI_RK4D, z, znew, nullptr)};
   const uint32_t x0 = (uint32_t)(*seed);
-  set_fused_kick(h, epi[3], x0);
+  cudaEvent_t join = nullptr;
+  int rc = start_fused_kick(h, epi[3], x0, &join);
+  if (rc) return rc;
   const double* zin[4] = {z, znl, znl, znl};
-  const int rc = stage_chain(h, 4, zin, znl, u, v, epi);
+  rc = stage_chain(h, 4, zin, znl, u, v, epi, join);
   if (rc) return rc;
   *seed = (int32_t)((h->lcga_nf * x0 + h->lcgb_nf) & 0x7FFFFFFFu);
   return GT_OK;
