@@ -355,11 +355,11 @@ def ours_arm(args):
     stages = 4 if p.rko == 4 else 2
     # per step: pass A of stage 1, then per stage pass B and pass C (fused with the next
     # stage's pass A) -> 2 * stages + 1; with the field-split column passes, pass C and the next
-    # pass A are separate launches -> 3 * stages. The forcing kick is fused into the last
-    # pass C; a diagnostics step launches the kick separately (the diagnostics see the field
-    # before it) and adds one nonlinear term (3 passes) and 5 reduction kernels
+    # pass A are separate launches -> 3 * stages. One more launch per step computes the kick
+    # increments (side stream) that the last pass C adds, or, on a diagnostics step, applies
+    # the kick after the diagnostics, which add one nonlinear term (3 passes) and 5 kernels
     per_step = 3 * stages if sol.col_split else 2 * stages + 1
-    launches = K * per_step + ndiag * (1 + 3 + 5)
+    launches = K * (per_step + 1) + ndiag * (3 + 5)
 
     extras = {}
     if rank == 0:
