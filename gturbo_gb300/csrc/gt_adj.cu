@@ -225,12 +225,15 @@ int run3(gt_handle* h, gt::GtOp op, int k0) {
                    static_cast<const void*>(op.nlt.zin) != static_cast<const void*>(op.nlt.q);
   // the transposed passes likewise (their inputs x and lin never alias the scratch outputs)
   const bool adj = k0 == gt::OP_ADJ_COLINV && gt::handle_col_split(h);
+  const bool tlm = k0 == gt::OP_TLM_COLINV && gt::handle_col_split(h);
   for (int k = 0; k < 3; ++k) {
     op.kind = k0 + k;
     if (fwd && k == 0) op.kind = gt::OP_NLT_COLINV_FS;
     if (fwd && k == 2) op.kind = gt::OP_NLT_COLFWD_FS;
     if (adj && k == 0) op.kind = gt::OP_ADJ_COLINV_FS;
     if (adj && k == 2) op.kind = gt::OP_ADJ_COLFWD_FS;
+    if (tlm && k == 0) op.kind = gt::OP_TLM_COLINV_FS;
+    if (tlm && k == 2) op.kind = gt::OP_TLM_COLFWD_FS;
     const cudaError_t e = gt::handle_dispatch(h, op);
     if (e != cudaSuccess) return acuda(h, e, "adjoint launch");
   }
@@ -317,6 +320,7 @@ gt::TlmArgs tlm_args(const gt_handle* h) {
   a.split = t.epi.split;
   a.dt = t.epi.dt;
   a.dt2 = t.epi.dt2;
+  a.colcnt = t.colcnt;
   return a;
 }
 

@@ -46,6 +46,7 @@ struct TlmArgs {
   const double* emky;
   int split;
   double dt, dt2;
+  int* colcnt;        // per-column counters of the field-split tangent pass C (NH ints, zero)
 };
 
 __device__ __forceinline__ double stage_e(const double* emk, const double* emkx, const double* emky,
@@ -519,6 +520,100 @@ __device__ __forceinline__ void adj_colfwd_tile(const AdjArgs& a, int tile) {
   }
 }
 
+// ---- field-split tangent-linear column tiles (one field of one column per CTA, C = 1) ------------
+
+// Tangent pass A, field f of column i (unit 6 i + f): q, Mu q, Mv q of x (f = 0, 1, 2) and of dx.
+template <int N, int R>
+__device__ __forceinline__ void tlm_colinv_field_tile(const TlmArgs& a, int unit) {
+  constexpr int T = N / R, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  const int i = unit / 6, f = unit % 6, t = threadIdx.x;
+  const double kx = __ldg(&a.fkx[i]);
+  const double2* src = f < 3 ? a.x : a.dx;
+  double2* dst = f == 0 ? a.q : f == 1 ? a.u : f == 2 ? a.v : f == 3 ? a.dq : f == 4 ? a.du : a.dv;
+  const int kind = f % 3;  // 0: q, 1: Mu q, 2: Mv q
+  double2 v[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    const int j = t + s * T;
+    const size_t o = (size_t)j * NH + i;
+    const double2 q = src[o];
+    if (kind == 0) {
+      v[s] = q;
+    } else if (kind == 1) {
+      const double m = __ldg(&a.fky[j]) * __ldg(&a.kainv[o]);
+      v[s] = make_double2(-m * q.y, m * q.x);
+    } else {
+      const double m = kx * __ldg(&a.kainv[o]);
+      v[s] = make_double2(m * q.y, -m * q.x);
+    }
+  }
+  fft_regs<N, R, true, 1>(v, smem, t, a.tw, 0);
+#pragma unroll
+  for (int s = 0; s < R; ++s) dst[(size_t)(t + s * T) * NH + i] = v[s];
+}
+
+// Tangent pass C, field f of column i (unit 4 i + f; f = 0, 1, 2, 3: A, B, dA, dB): the forward
+// transform written back in place (kx-scaled for A and dA). The fourth of the column's CTAs to
+// finish (a per-column counter, no waiting) forms N and dN as tlm_colfwd_tile does and runs the
+// stage update.
+template <int N, int R>
+__device__ __forceinline__ void tlm_colfwd_field_tile(const TlmArgs& a, int unit) {
+  constexpr int T = N / R, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  __shared__ int last;
+  const int i = unit / 4, f = unit % 4, t = threadIdx.x;
+  const double scale = 0.5 / ((double)N * (double)N);
+  double2* own = f == 0 ? a.u : f == 1 ? a.v : f == 2 ? a.du : a.dv;
+  double2 v[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = own[(size_t)(t + s * T) * NH + i];
+  fft_regs<N, R, false, 1>(v, smem, t, a.tw, 0);
+  if ((f & 1) == 0) {
+    const double kxs = __ldg(&a.fkx[i]) * scale;
+#pragma unroll
+    for (int s = 0; s < R; ++s) v[s] = make_double2(kxs * v[s].x, kxs * v[s].y);
+  }
+#pragma unroll
+  for (int s = 0; s < R; ++s) own[(size_t)(t + s * T) * NH + i] = v[s];
+  __threadfence();
+  __syncthreads();
+  if (t == 0) last = atomicAdd(&a.colcnt[i], 1) == 3;
+  __syncthreads();
+  if (!last) return;
+  if (t == 0) a.colcnt[i] = 0;  // ready for the next launch
+  const int kc = a.truncate ? __ldg(&a.kcut[i]) : N;
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    const int j = t + s * T;
+    const size_t o = (size_t)j * NH + i;
+    const double2 fa = f == 0 ? v[s] : __ldcg(&a.u[o]);
+    const double2 fb = f == 1 ? v[s] : __ldcg(&a.v[o]);
+    const double2 dfa = f == 2 ? v[s] : __ldcg(&a.du[o]);
+    const double2 dfb = f == 3 ? v[s] : __ldcg(&a.dv[o]);
+    const double kys = __ldg(&a.fky[j]) * scale;
+    double2 nh = make_double2(fma(kys, fb.y, fa.y), -fma(kys, fb.x, fa.x));
+    double2 dn = make_double2(fma(kys, dfb.y, dfa.y), -fma(kys, dfb.x, dfa.x));
+    if (min(j, N - j) > kc || (i == 0 && j == 0 && a.truncate)) {
+      nh = czero();
+      dn = czero();
+    }
+    a.u[o] = nh;   // N and dN in place of A and dA (TLM_PLAIN reads them there)
+    a.du[o] = dn;
+    if (a.mode == TLM_PLAIN) continue;
+    const double e = stage_e(a.emk, a.emkx, a.emky, a.split, i, j, NH);
+    const bool origin = (i == 0 && j == 0);
+    const double2 z = a.z[o], dz = a.dz[o];
+    if (a.mode == TLM_STAGE_A) {
+      a.w[o] = origin ? czero() : make_double2(e * (z.x + a.dt2 * nh.x), e * (z.y + a.dt2 * nh.y));
+      a.dw[o] = origin ? czero() : make_double2(e * (dz.x + a.dt2 * dn.x), e * (dz.y + a.dt2 * dn.y));
+    } else {
+      a.z[o] = origin ? czero() : make_double2(e * (e * z.x + a.dt * nh.x), e * (e * z.y + a.dt * nh.y));
+      a.dz[o] = origin ? czero() : make_double2(e * (e * dz.x + a.dt * dn.x), e * (e * dz.y + a.dt * dn.y));
+    }
+  }
+}
+
 // ---- field-split transposed column tiles (one field of one column per CTA, C = 1) ---------------
 
 // Fields of the transposed pass A: q, u, v from x (f = 0, 1, 2) and a, b from lin (3, 4); with
@@ -700,6 +795,14 @@ template <int N, int V>
 struct AdjSplitVar {
   static constexpr bool OK = SplitVar<N, V>::OK && AdjShape<N>::OK;
 };
+template <int N, int V>
+__global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_tlm_colinv_fs(TlmArgs a) {
+  if constexpr (AdjSplitVar<N, V>::OK) tlm_colinv_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
+}
+template <int N, int V>
+__global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_tlm_colfwd_fs(TlmArgs a) {
+  if constexpr (AdjSplitVar<N, V>::OK) tlm_colfwd_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
+}
 template <int N, int V>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_adj_colinv_fs(AdjArgs a) {
   if constexpr (AdjSplitVar<N, V>::OK) adj_colinv_field_tile<N, Var<N, V>::R>(a, blockIdx.x);

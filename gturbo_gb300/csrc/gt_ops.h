@@ -31,6 +31,8 @@ enum OpKind : int {
   OP_NLT_COLFWD_FS = 17,   // pass C split by field, epilogue by the column's second CTA
   OP_ADJ_COLINV_FS = 18,   // transposed pass A split by field
   OP_ADJ_COLFWD_FS = 19,   // transposed pass C split by field, update by the column's third CTA
+  OP_TLM_COLINV_FS = 20,   // tangent pass A split by field
+  OP_TLM_COLFWD_FS = 21,   // tangent pass C split by field, update by the column's fourth CTA
 };
 
 struct GtOp {
