@@ -879,8 +879,16 @@ __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colinv(NltArgs 
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colinv_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
   else if constexpr (Var<N, V>::OK) colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
 }
+// Without a CTA count ptxas keeps the 8-value row kernels at 76-80 registers (3 CTAs per SM);
+// an explicit count of 1 lets them grow to 164. GT_VROW_MINB sets a count for the 8-value rows
+// from 1024 up.
+#ifdef GT_VROW_MINB
+#define GT_VROW_BOUNDS(N, V) __launch_bounds__(Var<N, V>::ROW_THREADS, (V == 1 && N >= 1024) ? GT_VROW_MINB : 1)
+#else
+#define GT_VROW_BOUNDS(N, V) __launch_bounds__(Var<N, V>::ROW_THREADS)
+#endif
 template <int N, int V>
-__global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_nltv_row(NltArgs a) {
+__global__ void GT_VROW_BOUNDS(N, V) k_nltv_row(NltArgs a) {
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) row_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
   else if constexpr (Var<N, V>::OK) row_tile<N, Var<N, V>::ROWS, Var<N, V>::R>(a, blockIdx.x);
 }
@@ -898,13 +906,19 @@ __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltA
 }
 
 // Field-split column kernels (variants with one column per CTA and no thread groups).
-// At least 3 CTAs per SM (at most 80 registers per thread) for the 8- and 4-value variants, as
-// the fused kernels of those variants reach without a bound.
+// At least GT_SPLIT_MINB CTAs per SM (at most GT_SPLIT_REGS registers per thread) for the 8- and
+// 4-value variants: 3 and 80, as the fused kernels of those variants reach without a bound.
+#ifndef GT_SPLIT_MINB
+#define GT_SPLIT_MINB 3
+#endif
+#ifndef GT_SPLIT_REGS
+#define GT_SPLIT_REGS 80
+#endif
 template <int N, int V>
 struct SplitVar {
   static constexpr bool OK = Var<N, V>::OK && !Var<N, V>::GROUPED && Var<N, V>::COLS == 1;
   static constexpr int THREADS = N / Var<N, V>::R;
-  static constexpr int MINB = V == 0 ? MinBlocks<N>::COL : min_blocks(3, THREADS, 80);
+  static constexpr int MINB = V == 0 ? MinBlocks<N>::COL : min_blocks(GT_SPLIT_MINB, THREADS, GT_SPLIT_REGS);
   static constexpr size_t SMEM = (size_t)padded(N) * sizeof(double2);
 };
 template <int N, int V>
