@@ -55,6 +55,8 @@ def parse():
                     help="launch variant of the nonlinear-term passes (default: autotuned)")
     ap.add_argument("--row-variant", type=int, default=None,
                     help="with --variant: the row passes' own launch variant (default: the same)")
+    ap.add_argument("--no-pdl", action="store_true",
+                    help="launch the pass kernels without programmatic dependent launch")
     ap.add_argument("--adjoint-rk", type=int, choices=[2, 4], default=2,
                     help="integrator of the --only adjoint leg (the bench's own leg is RK2)")
     ap.add_argument("--only", choices=["ensemble", "adjoint"], default=None,
@@ -310,6 +312,7 @@ def ours_arm(args):
     p, k0, desc = workload(args.config)
     K, W = args.steps, max(3, args.warmup)
     sol = Solver(p, device=local)
+    sol.pdl = not args.no_pdl
     # launch variant of the nonlinear-term passes: timed per variant before the run (like a
     # cuFFT plan, outside the timed region)
     if args.variant is None:
@@ -489,7 +492,7 @@ def ours_arm(args):
                 "config": {"workload": desc, "n": p.n, "alpha": p.alpv, "rk": p.rko,
                            "imix": p.imix, "diag_calls_timed": ndiag,
                            "launch_variant": tune["variant"],
-                           "row_variant": sol.variants[1], "col_split": sol.col_split,
+                           "row_variant": sol.variants[1], "col_split": sol.col_split, "pdl": sol.pdl,
                            "autotune_ms_per_step": tune["ms_per_step"],
                            "parallelism": f"replicas x{world}" if world > 1 else "single",
                            "l2": "no flush: working set ~202 MB > 126 MB L2"},

@@ -70,6 +70,8 @@ def load(path: str | None = None):
         "gt_step_rk2_forced": ([P, D, D, D, D, I32P], ctypes.c_int),
         "gt_set_col_split": ([P, ctypes.c_int32], ctypes.c_int),
         "gt_get_col_split": ([P, I32P], ctypes.c_int),
+        "gt_set_pdl": ([P, ctypes.c_int32], ctypes.c_int),
+        "gt_get_pdl": ([P, I32P], ctypes.c_int),
         "gt_step_rk4_forced": ([P, D, D, D, D, D, I32P], ctypes.c_int),
         "gt_rann": ([I32P], ctypes.c_float),
         "gt_diag": ([P, D, D, H, H, H, H, H], ctypes.c_int),

@@ -214,6 +214,7 @@ gt::GtOp op_of(const gt_handle* h, int kind) {
   op.variant = gt::handle_variant(h);
   op.row_variant = gt::handle_row_variant(h);
   op.stream = gt::handle_stream(h);
+  op.pdl = gt::handle_pdl(h);
   return op;
 }
 

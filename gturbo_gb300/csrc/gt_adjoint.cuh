@@ -732,26 +732,32 @@ struct AdjShape {
 
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS) k_tlm_colinv(TlmArgs a) {
+  pdl_enter();
   if constexpr (AdjShape<N>::OK) tlm_colinv_tile<N, Shape<N>::COLS>(a, blockIdx.x);
 }
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::ROW_THREADS) k_tlm_row(TlmArgs a) {
+  pdl_enter();
   if constexpr (AdjShape<N>::OK) tlm_row_tile<N, Shape<N>::ROWS>(a, blockIdx.x);
 }
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS) k_tlm_colfwd(TlmArgs a) {
+  pdl_enter();
   if constexpr (AdjShape<N>::OK) tlm_colfwd_tile<N, Shape<N>::COLS>(a, blockIdx.x);
 }
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS) k_adj_colinv(AdjArgs a) {
+  pdl_enter();
   if constexpr (AdjShape<N>::OK) adj_colinv_tile<N, Shape<N>::COLS>(a, blockIdx.x);
 }
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::ROW_THREADS) k_adj_row(AdjArgs a) {
+  pdl_enter();
   if constexpr (AdjShape<N>::OK) adj_row_tile<N, Shape<N>::ROWS>(a, blockIdx.x);
 }
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS) k_adj_colfwd(AdjArgs a) {
+  pdl_enter();
   if constexpr (AdjShape<N>::OK) adj_colfwd_tile<N, Shape<N>::COLS>(a, blockIdx.x);
 }
 
@@ -767,26 +773,32 @@ struct AdjVar {
 
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_tlmv_colinv(TlmArgs a) {
+  pdl_enter();
   if constexpr (AdjVar<N, V>::OK) tlm_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_tlmv_row(TlmArgs a) {
+  pdl_enter();
   if constexpr (AdjVar<N, V>::OK) tlm_row_tile<N, Var<N, V>::ROWS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_tlmv_colfwd(TlmArgs a) {
+  pdl_enter();
   if constexpr (AdjVar<N, V>::OK) tlm_colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_adjv_colinv(AdjArgs a) {
+  pdl_enter();
   if constexpr (AdjVar<N, V>::OK) adj_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::ROW_THREADS) k_adjv_row(AdjArgs a) {
+  pdl_enter();
   if constexpr (AdjVar<N, V>::OK) adj_row_tile<N, Var<N, V>::ROWS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_adjv_colfwd(AdjArgs a) {
+  pdl_enter();
   if constexpr (AdjVar<N, V>::OK) adj_colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
 }
 
@@ -797,18 +809,22 @@ struct AdjSplitVar {
 };
 template <int N, int V>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_tlm_colinv_fs(TlmArgs a) {
+  pdl_enter();
   if constexpr (AdjSplitVar<N, V>::OK) tlm_colinv_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_tlm_colfwd_fs(TlmArgs a) {
+  pdl_enter();
   if constexpr (AdjSplitVar<N, V>::OK) tlm_colfwd_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_adj_colinv_fs(AdjArgs a) {
+  pdl_enter();
   if constexpr (AdjSplitVar<N, V>::OK) adj_colinv_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_adj_colfwd_fs(AdjArgs a) {
+  pdl_enter();
   if constexpr (AdjSplitVar<N, V>::OK) adj_colfwd_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
 }
 

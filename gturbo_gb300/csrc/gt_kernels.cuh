@@ -171,6 +171,15 @@ struct Shape {
 
 __device__ __forceinline__ double2 czero() { return make_double2(0.0, 0.0); }
 
+// Entry of a pass kernel that may be launched with programmatic dependent launch (the launch
+// overlaps the drain of the previous kernel on the stream). It waits for that kernel to complete
+// and its writes to be visible (a no-op after an ordinary launch), then allows the next kernel on
+// the stream to begin launching: that one runs the same wait before it touches memory.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // 1 unless both parts are +-0 (integer test of the bit patterns)
 __device__ __forceinline__ int nonzero2(double2 a) {
   return ((__double_as_longlong(a.x) | __double_as_longlong(a.y)) << 1) != 0;
@@ -825,24 +834,28 @@ __device__ __forceinline__ void colfwd_field_tile(const NltArgs& a, int unit) {
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
 k_nlt_colinv(NltArgs a) {
+  pdl_enter();
   colinv_tile<N, Shape<N>::COLS>(a, blockIdx.x);
 }
 
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::ROW_THREADS, MinBlocks<N>::ROW)
 k_nlt_row(NltArgs a) {
+  pdl_enter();
   row_tile<N, Shape<N>::ROWS>(a, blockIdx.x);
 }
 
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
 k_nlt_colfwd(NltArgs a) {
+  pdl_enter();
   colfwd_tile<N, Shape<N>::COLS, 16, true>(a, blockIdx.x);
 }
 
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
 k_nlt_colfwd_inv(NltArgs cur, NltArgs next) {
+  pdl_enter();
   colfwd_colinv_tile<N, Shape<N>::COLS>(cur, next, blockIdx.x);
 }
 
@@ -876,6 +889,7 @@ struct Var {
 
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colinv(NltArgs a) {
+  pdl_enter();
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colinv_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
   else if constexpr (Var<N, V>::OK) colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
 }
@@ -889,16 +903,19 @@ __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colinv(NltArgs 
 #endif
 template <int N, int V>
 __global__ void GT_VROW_BOUNDS(N, V) k_nltv_row(NltArgs a) {
+  pdl_enter();
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) row_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
   else if constexpr (Var<N, V>::OK) row_tile<N, Var<N, V>::ROWS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd(NltArgs a) {
+  pdl_enter();
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colfwd_grp_tile<N, Var<N, V>::R, true>(a, blockIdx.x);
   else if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R, true>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltArgs cur, NltArgs next) {
+  pdl_enter();
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED)
     colfwd_colinv_grp_tile<N, Var<N, V>::R>(cur, next, blockIdx.x);
   else if constexpr (Var<N, V>::OK)
@@ -923,11 +940,13 @@ struct SplitVar {
 };
 template <int N, int V>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_nlt_colinv_fs(NltArgs a) {
+  pdl_enter();
   if constexpr (SplitVar<N, V>::OK) colinv_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
 }
 // KICK: the final stage with the fused forcing kick
 template <int N, int V, bool KICK>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_nlt_colfwd_fs(NltArgs a) {
+  pdl_enter();
   if constexpr (SplitVar<N, V>::OK) colfwd_field_tile<N, Var<N, V>::R, KICK>(a, blockIdx.x);
 }
 

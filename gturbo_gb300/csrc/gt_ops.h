@@ -48,7 +48,27 @@ struct GtOp {
   float* f32;         // real(4) output of OP_ROW_C2R_F32
   const double2* tw;
   double scale;
+  bool pdl;           // launch the pass kernels with programmatic dependent launch
 };
+
+// Launches the pass kernel k on stream s. With `pdl` the launch may begin while the previous
+// kernel on s drains (programmatic dependent launch); only kernels whose first statement is
+// pdl_enter() are launched this way. The error, if any, is left for cudaGetLastError.
+template <typename... KArgs, typename... Args>
+inline void launch_pass(bool pdl, cudaStream_t s, void (*k)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                        Args... args) {
+  cudaLaunchAttribute at;
+  at.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at.val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = &at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
 
 // Per-N entry points (defined in gt_inst_<N>.cu).
 #define GT_DECLARE_N(NN)                              \

@@ -75,6 +75,7 @@ struct gt_handle {
   double2* d_qscr = nullptr;
   int* d_colcnt = nullptr;
   int col_split = 1;  // use them where the column variant allows (gt_set_col_split)
+  int pdl = 1;        // programmatic dependent launch of the pass kernels (gt_set_pdl)
   // diagnostics scratch
   double *d_part = nullptr, *d_rowsum = nullptr, *d_bins = nullptr, *d_fl = nullptr, *d_glob = nullptr;
   double* h_diag = nullptr;  // pinned: bins [nbin*4] + fl [nbin*2] + glob [6]
@@ -295,6 +296,7 @@ GtOp base_op(const gt_handle* h) {
   op.row_variant = h->row_variant;
   op.tw = h->d_tw;
   op.nlt = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, h->d_flag);
+  op.pdl = gt::handle_pdl(h);
   return op;
 }
 
@@ -386,6 +388,8 @@ gt::EpiArgs make_epi(const gt_handle* h, int mode, double* out, double* znew, co
 
 namespace gt {
 bool handle_col_split(const gt_handle* h) { return split_active(h); }
+// the per-launch timing events of the profiling mode sit between the kernels: no overlap there
+bool handle_pdl(const gt_handle* h) { return h->pdl && !h->prof; }
 }  // namespace gt
 
 extern "C" {
@@ -986,6 +990,18 @@ int gt_profile_read(gt_handle* h, double* ms, int64_t* launches) {
 int gt_set_col_split(gt_handle* h, int32_t on) {
   if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_col_split: null handle");
   h->col_split = on ? 1 : 0;
+  return GT_OK;
+}
+
+int gt_set_pdl(gt_handle* h, int32_t on) {
+  if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_pdl: null handle");
+  h->pdl = on ? 1 : 0;
+  return GT_OK;
+}
+
+int gt_get_pdl(const gt_handle* h, int32_t* on) {
+  if (!h || !on) return fail(nullptr, GT_ERR_ARG, "gt_get_pdl: null argument");
+  *on = h->pdl;
   return GT_OK;
 }
 

@@ -176,6 +176,17 @@ class Solver:
     def col_split(self, on: bool) -> None:
         self._check(self.lib.gt_set_col_split(self.h, int(bool(on))))
 
+    @property
+    def pdl(self) -> bool:
+        """Whether the pass kernels launch with programmatic dependent launch (gt_get_pdl)."""
+        a = ctypes.c_int32()
+        self._check(self.lib.gt_get_pdl(self.h, ctypes.byref(a)))
+        return bool(a.value)
+
+    @pdl.setter
+    def pdl(self, on: bool) -> None:
+        self._check(self.lib.gt_set_pdl(self.h, int(bool(on))))
+
     def supported_variants(self) -> list[int]:
         return [v for v in range(self.NVARIANTS) if self.lib.gt_variant_supported(self.n, v)]
 

@@ -316,6 +316,14 @@ int gt_get_variants(const gt_handle* h, int32_t* col_variant, int32_t* row_varia
  * current size and column variant. Results are the same to rounding. */
 int gt_set_col_split(gt_handle* h, int32_t on);
 int gt_get_col_split(const gt_handle* h, int32_t* active);
+/* Programmatic dependent launch of the pass kernels (nonlinear term, tangent-linear, adjoint):
+ * each such launch may begin while the previous kernel on the handle's stream drains, and the
+ * kernel waits for that kernel's completion before it touches memory, so results do not change.
+ * It hides the launch gap between consecutive passes. On by default; off while the handle times
+ * its launches (gt_profile). The final pass C of a step with the fused kick, which waits for the
+ * side stream's increments, always launches the ordinary way. */
+int gt_set_pdl(gt_handle* h, int32_t on);
+int gt_get_pdl(const gt_handle* h, int32_t* on);
 /* Time `steps` steps of the handle's integrator (RK2 or RK4) on zero fields of its own
  * (allocated and freed here, 5 fields; nothing when only one variant exists): first every
  * supported column variant with its own row tiles, then the other row variants under the

@@ -157,6 +157,12 @@ module gturbo_c
       type(c_ptr), value :: h
       integer(c_int32_t), value :: on
     end function
+    ! programmatic dependent launch of the pass kernels (on by default)
+    integer(c_int) function gt_set_pdl(h, on) bind(C, name="gt_set_pdl")
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: h
+      integer(c_int32_t), value :: on
+    end function
     integer(c_int) function gt_autotune(h, steps, ms_per_step, best) bind(C, name="gt_autotune")
       import :: c_int, c_ptr, c_int32_t, c_double
       type(c_ptr), value :: h

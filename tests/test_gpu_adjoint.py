@@ -173,6 +173,25 @@ def test_gradient_with_and_without_col_split(n, variant, rko):
     assert (torch.linalg.norm(zT1 - zT0) / torch.linalg.norm(zT0)).item() < 1e-13
 
 
+@pytest.mark.parametrize("n,variant", [(256, 2), (1024, 2)])
+def test_gradient_with_and_without_pdl(n, variant):
+    """Programmatic dependent launch of the forward, tangent and transposed pass kernels leaves
+    the gradient and the tangent-linear run bit for bit the same."""
+    from gturbo_gb300.adjoint import gradient, tlm_run
+    p, sol, z0, ns = _setup(n=n, nsteps=5)
+    sol.variant = variant
+    dz = torch.randn_like(z0) * 1e-3
+    res = {}
+    for pdl in (True, False):
+        sol.pdl = pdl
+        J, gz, gf, zT, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=2)
+        J2, dJ = tlm_run(sol, z0, dz, 0.4, ns, SEED, KMIN, KMAX)
+        res[pdl] = (J, gz.cpu(), gf, zT.cpu(), J2, dJ)
+    a, b = res[True], res[False]
+    assert a[0] == b[0] and a[2] == b[2] and a[4] == b[4] and a[5] == b[5]
+    assert torch.equal(a[1], b[1]) and torch.equal(a[3], b[3])
+
+
 @pytest.mark.parametrize("n,variant", [(128, 0), (128, 2), (256, 1)])
 def test_gradient_driver_matches_step_by_step_adjoint(n, variant):
     """gt_adj_gradient (whose adjoint passes read the physical fields that the recomputed
