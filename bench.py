@@ -456,7 +456,7 @@ def ours_arm(args):
 
             # ---- batched ensemble (64 members of mixed size) vs the plain member loop ----
             try:
-                extras["ensemble"] = ensemble_run(min(K, 100), W, torch)
+                extras["ensemble"] = ensemble_run(min(K, 100), W, torch, pdl=not args.no_pdl)
             except Exception as e:
                 extras["ensemble"] = {"unavailable": str(e)[:300]}
 
@@ -549,7 +549,7 @@ def adjoint_run(torch, rko=2):
             "fd_step": h}
 
 
-def ensemble_run(steps, warm, torch, shard=False):
+def ensemble_run(steps, warm, torch, shard=False, pdl=True):
     """Member-steps/s of the 64-member mixed-size ensemble: batched (one launch per pass, CUDA
     graph) against the plain loop over members through the single-field C-ABI. With
     ``shard`` (every rank of the process group calls it) the members are split over the ranks
@@ -587,6 +587,8 @@ def ensemble_run(steps, warm, torch, shard=False):
     # plain loop on copies of the same initial fields
     zp = [a.clone() for a in z0]
     plain = PlainLoop(members, zp)
+    for ps in plain.solvers:
+        ps.pdl = pdl
     plain.step(min(warm, 2))
     kp = max(5, steps // 4)
     torch.cuda.synchronize()
@@ -667,7 +669,7 @@ def main():
         if args.only == "ensemble":
             if world > 1:  # members sharded over the ranks
                 dist.init_process_group("nccl", device_id=torch.device("cuda", torch.cuda.current_device()))
-            res = ensemble_run(args.steps, max(3, args.warmup), torch, shard=world > 1)
+            res = ensemble_run(args.steps, max(3, args.warmup), torch, shard=world > 1, pdl=not args.no_pdl)
             if world > 1:
                 dist.destroy_process_group()
         elif rank == 0:
