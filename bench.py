@@ -55,6 +55,8 @@ def parse():
                     help="launch variant of the nonlinear-term passes (default: autotuned)")
     ap.add_argument("--row-variant", type=int, default=None,
                     help="with --variant: the row passes' own launch variant (default: the same)")
+    ap.add_argument("--col-split", type=int, choices=[0, 1, 2], default=None,
+                    help="field-split column passes: 0 off, 1 counter epilogue, 2 2-CTA clusters")
     ap.add_argument("--no-pdl", action="store_true",
                     help="launch the pass kernels without programmatic dependent launch")
     ap.add_argument("--adjoint-rk", type=int, choices=[2, 4], default=2,
@@ -322,6 +324,8 @@ def ours_arm(args):
         if args.row_variant is not None:
             sol.variants = (args.variant, args.row_variant)
         tune = {"variant": args.variant, "ms_per_step": None}
+    if args.col_split is not None:
+        sol.col_split = args.col_split
     stream = sol.stream
     work = sol.work()
     z0 = torch.from_numpy(random_phase_ic(p, k0, 0.5, seed=replica_ic_seed(rank))).to(dev)

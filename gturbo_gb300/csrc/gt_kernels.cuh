@@ -20,6 +20,8 @@
 // CTA, the *_field_tile functions), which evens out the SMs' share of the 2/3-rule columns.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "gt_fft.cuh"
 
 namespace gt {
@@ -829,6 +831,63 @@ __device__ __forceinline__ void colfwd_field_tile(const NltArgs& a, int unit) {
   }
 }
 
+// Pass C split by field, the column's two CTAs forming one 2-CTA cluster (unit = 2 i + g, g = 0
+// transforms A = F(u q), g = 1 B = F(v q)). Each CTA leaves the half of its transformed column
+// that the other CTA needs in its own shared memory; after a cluster barrier each CTA runs the
+// epilogue for its half of the rows (g = 0: j < N/2), reading the other field from the partner's
+// shared memory. No global round trip and no per-column counter; the epilogue work is shared.
+// A second cluster barrier keeps each CTA's shared memory alive until the partner has read it.
+// Columns beyond the 2/3 cut: each CTA stores the zero-input epilogue of its half.
+template <int N, int R, bool KICK>
+__device__ __forceinline__ void colfwd_cluster_tile(const NltArgs& a, int unit) {
+  constexpr int T = N / R, NH = N / 2 + 1, H = R / 2;
+  extern __shared__ double2 smem[];
+  const int t = threadIdx.x;
+  const int i = unit >> 1, g = unit & 1;
+  if (unit == 0 && t == 0) *a.flag = 0;  // pass B of this nlt is complete
+  if (i > a.kxlim) {  // both CTAs of the cluster take this branch: no barrier is pending
+#pragma unroll
+    for (int s = 0; s < H; ++s) epilogue<KICK>(a.epi, i, t + (g * H + s) * T, NH, czero());
+    return;
+  }
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const double scale = 0.5 / ((double)N * (double)N);
+  const double2* own = g == 0 ? a.u : a.v;
+  double2 v[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = own[(size_t)(t + s * T) * NH + i];
+  fft_regs<N, R, false, 1>(v, smem, t, a.tw, 0);
+  if (g == 0) {
+    const double kxs = __ldg(&a.fkx[i]) * scale;
+#pragma unroll
+    for (int s = 0; s < R; ++s) v[s] = make_double2(kxs * v[s].x, kxs * v[s].y);
+  }
+  // fft_regs ends with a barrier after its last shared-memory read: the buffer is free
+#pragma unroll
+  for (int s = 0; s < H; ++s) {
+    const int j = t + ((1 - g) * H + s) * T;
+    smem[j] = v[(1 - g) * H + s];
+  }
+  cluster.sync();
+  const double2* peer = cluster.map_shared_rank(smem, (unsigned)(g ^ 1));
+  const int kc = a.truncate ? __ldg(&a.kcut[i]) : N;
+#pragma unroll
+  for (int s = 0; s < H; ++s) {
+    const int j = t + (g * H + s) * T;
+    const double2 o = peer[j];
+    const double2 fa = g == 0 ? v[g * H + s] : o;
+    const double2 fb = g == 0 ? o : v[g * H + s];
+    const double kys = __ldg(&a.fky[j]) * scale;
+    // N = -i (kx A + ky B): re = kx Im A + ky Im B, im = -(kx Re A + ky Re B)
+    double2 nh = make_double2(fma(kys, fb.y, fa.y), -fma(kys, fb.x, fa.x));
+    const int aj = min(j, N - j);
+    if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
+    epilogue<KICK>(a.epi, i, j, NH, nh);
+  }
+  cluster.sync();
+}
+
 // ---- single-field kernels ---------------------------------------------------------------
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS, MinBlocks<N>::COL)
@@ -947,6 +1006,13 @@ template <int N, int V, bool KICK>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_nlt_colfwd_fs(NltArgs a) {
   pdl_enter();
   if constexpr (SplitVar<N, V>::OK) colfwd_field_tile<N, Var<N, V>::R, KICK>(a, blockIdx.x);
+}
+// the same pass with the column's two CTAs as one cluster (grid 2 NH)
+template <int N, int V, bool KICK>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB)
+    k_nlt_colfwd_cl(NltArgs a) {
+  pdl_enter();
+  if constexpr (SplitVar<N, V>::OK) colfwd_cluster_tile<N, Var<N, V>::R, KICK>(a, blockIdx.x);
 }
 
 // ---- ensemble kernels: one launch per pass for every member ------------------------------

@@ -28,7 +28,8 @@ enum OpKind : int {
   OP_ROW_C2R_F32 = 14,     // row C2R of `a` written as floats to `f32` (dumps)
   OP_ROW_R2C_F32 = 15,     // row R2C of the floats `f32` into `a` (restarts)
   OP_NLT_COLINV_FS = 16,   // pass A split by field (q must not alias zin)
-  OP_NLT_COLFWD_FS = 17,   // pass C split by field, epilogue by the column's second CTA
+  OP_NLT_COLFWD_FS = 17,   // pass C split by field, epilogue by the column's second CTA (or,
+                           // with GtOp::cluster, by both CTAs of the column's 2-CTA cluster)
   OP_ADJ_COLINV_FS = 18,   // transposed pass A split by field
   OP_ADJ_COLFWD_FS = 19,   // transposed pass C split by field, update by the column's third CTA
   OP_TLM_COLINV_FS = 20,   // tangent pass A split by field
@@ -49,6 +50,7 @@ struct GtOp {
   const double2* tw;
   double scale;
   bool pdl;           // launch the pass kernels with programmatic dependent launch
+  bool cluster;       // OP_NLT_COLFWD_FS: the column's two CTAs as one cluster
 };
 
 // Launches the pass kernel k on stream s. With `pdl` the launch may begin while the previous

@@ -74,7 +74,7 @@ struct gt_handle {
   // two CTAs per column meet at a per-column counter
   double2* d_qscr = nullptr;
   int* d_colcnt = nullptr;
-  int col_split = 1;  // use them where the column variant allows (gt_set_col_split)
+  int col_split = 2;  // use them where the column variant allows (gt_set_col_split: 0, 1, 2)
   int pdl = 1;        // programmatic dependent launch of the pass kernels (gt_set_pdl)
   // diagnostics scratch
   double *d_part = nullptr, *d_rowsum = nullptr, *d_bins = nullptr, *d_fl = nullptr, *d_glob = nullptr;
@@ -297,6 +297,7 @@ GtOp base_op(const gt_handle* h) {
   op.tw = h->d_tw;
   op.nlt = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, h->d_flag);
   op.pdl = gt::handle_pdl(h);
+  op.cluster = h->col_split == 2;
   return op;
 }
 
@@ -989,7 +990,7 @@ int gt_profile_read(gt_handle* h, double* ms, int64_t* launches) {
 
 int gt_set_col_split(gt_handle* h, int32_t on) {
   if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_col_split: null handle");
-  h->col_split = on ? 1 : 0;
+  h->col_split = on <= 0 ? 0 : on >= 2 ? 2 : 1;
   return GT_OK;
 }
 
@@ -1007,7 +1008,7 @@ int gt_get_pdl(const gt_handle* h, int32_t* on) {
 
 int gt_get_col_split(const gt_handle* h, int32_t* active) {
   if (!h || !active) return fail(nullptr, GT_ERR_ARG, "gt_get_col_split: null argument");
-  *active = split_active(h) ? 1 : 0;
+  *active = split_active(h) ? h->col_split : 0;
   return GT_OK;
 }
 
@@ -1122,9 +1123,10 @@ int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best)
     // stage 3: the best pair with one CTA per column, where the field-split passes ran
     h->variant = best_c;
     if (!rc && h->col_split && split_active(h)) {
+      const int mode = h->col_split;
       h->col_split = 0;
       const double t = time_pair(best_c, best_r);
-      if (rc || !(t < best_ms)) h->col_split = 1;
+      if (rc || !(t < best_ms)) h->col_split = mode;
     }
     if (buf) {
       cudaStreamSynchronize(h->stream);

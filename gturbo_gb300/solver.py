@@ -166,15 +166,16 @@ class Solver:
         self._check(self.lib.gt_set_variants(self.h, int(cr[0]), int(cr[1])))
 
     @property
-    def col_split(self) -> bool:
-        """Whether the field-split column passes run (gt_get_col_split)."""
+    def col_split(self) -> int:
+        """The field-split column passes that run (gt_get_col_split): 0 none, 1 pass C's epilogue
+        by the column's second CTA, 2 pass C as 2-CTA clusters sharing the epilogue."""
         a = ctypes.c_int32()
         self._check(self.lib.gt_get_col_split(self.h, ctypes.byref(a)))
-        return bool(a.value)
+        return a.value
 
     @col_split.setter
-    def col_split(self, on: bool) -> None:
-        self._check(self.lib.gt_set_col_split(self.h, int(bool(on))))
+    def col_split(self, mode: int) -> None:
+        self._check(self.lib.gt_set_col_split(self.h, int(mode)))
 
     @property
     def pdl(self) -> bool:

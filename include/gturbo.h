@@ -311,9 +311,13 @@ int gt_get_variants(const gt_handle* h, int32_t* col_variant, int32_t* row_varia
 /* Field-split column passes (N <= 2048, column variants with one column per CTA and no
  * thread groups: 0 from N = 1024, 1, 2): each CTA transforms one field of one column, so a
  * column pass has 3 (pass A) or 2 (pass C) work units per column and the SMs finish together;
- * q then lives in the handle's scratch field. On by default; gt_set_col_split(h, 0) returns to
- * one CTA per column. gt_get_col_split reports whether the split passes run with the handle's
- * current size and column variant. Results are the same to rounding. */
+ * q then lives in the handle's scratch field. on = 1: pass C's epilogue is run by the column's
+ * CTA that finishes second, which reads the other field back through L2 (a per-column counter);
+ * on = 2: the column's two pass C CTAs form one 2-CTA cluster, exchange halves through
+ * distributed shared memory and each run the epilogue for half of the rows. On (2) by default;
+ * gt_set_col_split(h, 0) returns to one CTA per column. gt_get_col_split reports the mode that
+ * runs with the handle's current size and column variant (0 where the split passes do not
+ * apply). Results are the same to rounding. */
 int gt_set_col_split(gt_handle* h, int32_t on);
 int gt_get_col_split(const gt_handle* h, int32_t* active);
 /* Programmatic dependent launch of the pass kernels (nonlinear term, tangent-linear, adjoint):

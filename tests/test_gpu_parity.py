@@ -245,18 +245,18 @@ def test_forced_step_equals_step_then_forcing(n, rko, kw):
                                                     (1024, 4, 2, 1), (2048, 2, 1, 1), (2048, 2, 0, 1),
                                                     (1024, 2, 2, 0), (512, 4, 1, 0)])
 def test_col_split_equals_one_cta_per_column(n, rko, variant, truncate):
-    """The field-split column passes (one field of one column per CTA, q in the handle's scratch,
-    pass C's epilogue by the column's second CTA) agree with one CTA per column to rounding, for
-    steps, forced steps, the nonlinear term of an untruncated field and the split integrator.
-    The arithmetic is the same, but nvcc may contract a stage update into FMAs differently in
-    the two kernels, so the bits may differ by an ulp."""
+    """The field-split column passes (one field of one column per CTA, q in the handle's scratch;
+    pass C's epilogue by the column's second CTA, or shared by the column's 2-CTA cluster) agree
+    with one CTA per column to rounding, for steps, forced steps, the nonlinear term of an
+    untruncated field and the split integrator. The arithmetic is the same, but nvcc may contract
+    a stage update into FMAs differently in the kernels, so the bits may differ by an ulp."""
     kw = dict(alpnu=1.0, alpmu=0.0, nu=1e-3) if (rko == 2 and n == 512) else {}
     p = _params(n, rko=rko, dt=1e-3, famp=0.5, truncate=truncate, **kw)
     orc, sol = Oracle(p), _solver(p)
     sol.variants = (variant, 1 if variant == 0 and n >= 2048 else variant)
     a = rand_field(orc, 25, truncate=bool(truncate)) * 20.0
     out = {}
-    for split in (True, False):
+    for split in (2, 1, 0):
         sol.col_split = split
         assert sol.col_split == split
         z = _dev(a)
@@ -267,12 +267,13 @@ def test_col_split_equals_one_cta_per_column(n, rko, variant, truncate):
         u, v = sol.field(), sol.field()
         sol.nlt(zu, u, v)
         out[split] = (_host(z), _host(z2), s2, _host(zu))
-    assert out[True][2] == out[False][2]
-    for k in (0, 1, 3):
-        assert rel_l2(out[True][k], out[False][k]) < 1e-14, k
     ref = a.copy()
     orc.rk_step(ref)
-    assert rel_l2(out[True][0], ref) < TOL
+    for split in (2, 1):
+        assert out[split][2] == out[0][2]
+        for k in (0, 1, 3):
+            assert rel_l2(out[split][k], out[0][k]) < 1e-14, (split, k)
+        assert rel_l2(out[split][0], ref) < TOL
 
 
 @pytest.mark.parametrize("n,rko,cr", [(64, 4, (3, 3)), (256, 4, (3, 2)), (512, 2, (2, 1)), (1024, 2, (0, 0)),
@@ -290,7 +291,7 @@ def test_pdl_bit_identical(n, rko, cr):
         sol.pdl = pdl
         assert sol.pdl == pdl
         res = []
-        for split in (True, False):
+        for split in (2, 1, 0):
             sol.col_split = split
             z, w = _dev(a), sol.work()
             seed = 4242
