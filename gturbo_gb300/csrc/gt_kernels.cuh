@@ -257,8 +257,8 @@ struct NltArgs {
   // backward sweep keeps them from the recomputed forward stages instead of transforming again.
   double2* phys_uv;
   double2* phys_q;
-  // Per-column counters (NH ints, zero between launches) of the field-split pass C: the second
-  // of a column's two CTAs runs its epilogue.
+  // Per-column counters (NH ints, zero between launches) of the field-split pass C in its
+  // counter form: the second of a column's two CTAs runs its epilogue.
   int* colcnt;
 };
 

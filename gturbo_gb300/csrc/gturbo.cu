@@ -70,8 +70,9 @@ struct gt_handle {
   uint32_t *d_lcga = nullptr, *d_lcgb = nullptr;
   double2* d_ff = nullptr;
   int* d_flag = nullptr;
-  // field-split column passes (N <= 2048): q goes to the handle's own field, and pass C's
-  // two CTAs per column meet at a per-column counter
+  // field-split column passes (N <= 2048): q goes to the handle's own field; in mode 1 pass C's
+  // two CTAs per column meet at a per-column counter (mode 2 forms 2-CTA clusters instead), as
+  // do the transposed and tangent pass C's CTAs
   double2* d_qscr = nullptr;
   int* d_colcnt = nullptr;
   int col_split = 2;  // use them where the column variant allows (gt_set_col_split: 0, 1, 2)
