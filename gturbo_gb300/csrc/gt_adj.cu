@@ -215,6 +215,7 @@ gt::GtOp op_of(const gt_handle* h, int kind) {
   op.row_variant = gt::handle_row_variant(h);
   op.stream = gt::handle_stream(h);
   op.pdl = gt::handle_pdl(h);
+  op.cluster = gt::handle_col_cluster(h);
   return op;
 }
 

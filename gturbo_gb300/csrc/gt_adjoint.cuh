@@ -721,6 +721,64 @@ __device__ __forceinline__ void adj_colfwd_field_tile(const AdjArgs& a, int unit
   }
 }
 
+// The same pass with the column's three CTAs (q, u, v) as one 3-CTA cluster. Each CTA leaves its
+// transformed field in its own shared memory for the rows the others combine; after a cluster
+// barrier CTA f combines the rows j = t + s T with s = f, f + 3, ..., reading the other two
+// fields from the partners' shared memory, and runs the update there (the same per-value
+// arithmetic as above). A second barrier keeps the shared memory alive until the partners have
+// read it. The transformed u and v are not written back: nothing reads them after this pass.
+template <int N, int R>
+__device__ __forceinline__ void adj_colfwd_cluster_tile(const AdjArgs& a, int unit) {
+  constexpr int T = N / R, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  const int i = unit / 3, f = unit % 3, t = threadIdx.x;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const double2* own = f == 0 ? a.q : f == 1 ? a.u : a.v;
+  double2 v[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = own[(size_t)(t + s * T) * NH + i];
+  fft_regs<N, R, false, 1>(v, smem, t, a.tw, 0);
+  // fft_regs ends with a barrier after its last shared-memory read: the buffer is free
+#pragma unroll
+  for (int s = 0; s < R; ++s)
+    if (s % 3 != f) smem[t + s * T] = v[s];
+  cluster.sync();
+  const double2* pq = cluster.map_shared_rank(smem, 0u);
+  const double2* pu = cluster.map_shared_rank(smem, 1u);
+  const double2* pv = cluster.map_shared_rank(smem, 2u);
+  const double kx = __ldg(&a.fkx[i]);
+  const double cw = (i == 0 || i == NH - 1) ? 0.5 : 1.0;
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    if (s % 3 != f) continue;
+    const int j = t + s * T;
+    const size_t o = (size_t)j * NH + i;
+    const double2 fq = f == 0 ? v[s] : pq[j];
+    const double2 fu = f == 1 ? v[s] : pu[j];
+    const double2 fv = f == 2 ? v[s] : pv[j];
+    double2 g = make_double2(cw * fq.x, cw * fq.y);
+    const double mu = -__ldg(&a.fky[j]) * __ldg(&a.kainv[o]) * cw;
+    g = make_double2(fma(-mu, fu.y, g.x), fma(mu, fu.x, g.y));
+    const double mv = kx * __ldg(&a.kainv[o]) * cw;
+    g = make_double2(fma(-mv, fv.y, g.x), fma(mv, fv.x, g.y));
+    a.q[o] = g;
+    if (a.mode == ADJ_STAGE_B) {
+      const double e = stage_e(a.emk, a.emkx, a.emky, a.split, i, j, NH);
+      const bool origin = (i == 0 && j == 0);
+      const double2 l = a.lin[o];
+      a.lam[o] = origin ? czero() : make_double2(e * (e * l.x + g.x), e * (e * l.y + g.y));
+      a.rho[o] = origin ? czero() : make_double2(a.dt2 * e * g.x, a.dt2 * e * g.y);
+    } else if (a.mode == ADJ_PLAIN) {
+      a.lam[o] = g;
+    } else {
+      const double2 l = a.lam[o];
+      a.lam[o] = make_double2(l.x + g.x, l.y + g.y);
+    }
+  }
+  cluster.sync();
+}
+
 // ---- kernels ------------------------------------------------------------------------------
 template <int N>
 struct AdjShape {
@@ -826,6 +884,12 @@ template <int N, int V>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_adj_colfwd_fs(AdjArgs a) {
   pdl_enter();
   if constexpr (AdjSplitVar<N, V>::OK) adj_colfwd_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
+}
+template <int N, int V>
+__global__ void __cluster_dims__(3, 1, 1) __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB)
+    k_adj_colfwd_cl(AdjArgs a) {
+  pdl_enter();
+  if constexpr (AdjSplitVar<N, V>::OK) adj_colfwd_cluster_tile<N, Var<N, V>::R>(a, blockIdx.x);
 }
 
 }  // namespace gt

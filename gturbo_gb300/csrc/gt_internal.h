@@ -47,6 +47,8 @@ int handle_variant(const gt_handle* h);
 int handle_row_variant(const gt_handle* h);
 // whether the field-split column passes run for this handle (size, column variant, setting)
 bool handle_col_split(const gt_handle* h);
+// whether the split pass C runs as clusters (gt_set_col_split mode 2)
+bool handle_col_cluster(const gt_handle* h);
 // whether the pass kernels launch with programmatic dependent launch (setting, profiling off)
 bool handle_pdl(const gt_handle* h);
 // Records msg as h's last error (h == NULL: the thread's create/no-handle error); returns code.

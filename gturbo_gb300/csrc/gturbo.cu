@@ -390,6 +390,7 @@ gt::EpiArgs make_epi(const gt_handle* h, int mode, double* out, double* znew, co
 
 namespace gt {
 bool handle_col_split(const gt_handle* h) { return split_active(h); }
+bool handle_col_cluster(const gt_handle* h) { return h->col_split == 2; }
 // the per-launch timing events of the profiling mode sit between the kernels: no overlap there
 bool handle_pdl(const gt_handle* h) { return h->pdl && !h->prof; }
 }  // namespace gt

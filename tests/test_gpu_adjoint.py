@@ -152,8 +152,8 @@ def test_adjoint_in_every_launch_variant(n):
 
 @pytest.mark.parametrize("n,variant,rko", [(512, 2, 2), (1024, 1, 2), (1024, 0, 4)])
 def test_gradient_with_and_without_col_split(n, variant, rko):
-    """The field-split column passes (forward, recomputed and transposed) give the gradient of
-    one CTA per column to rounding, for RK2 and RK4."""
+    """The field-split column passes (forward, recomputed and transposed; pass C in its counter
+    form and as clusters) give the gradient of one CTA per column to rounding, for RK2 and RK4."""
     from gturbo_gb300.adjoint import gradient
     p, sol, z0, ns = _setup(n=n, nsteps=4)
     if rko == 4:
@@ -162,15 +162,17 @@ def test_gradient_with_and_without_col_split(n, variant, rko):
         sol = Solver(p)
     sol.variant = variant
     res = {}
-    for split in (True, False):
+    for split in (2, 1, 0):
         sol.col_split = split
         assert sol.col_split == split
         res[split] = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=2)
-    (J1, gz1, gf1, zT1, _), (J0, gz0, gf0, zT0, _) = res[True], res[False]
-    assert J1 == pytest.approx(J0, rel=1e-13)
-    assert gf1 == pytest.approx(gf0, rel=1e-11, abs=1e-20)
-    assert (torch.linalg.norm(gz1 - gz0) / torch.linalg.norm(gz0)).item() < 1e-12
-    assert (torch.linalg.norm(zT1 - zT0) / torch.linalg.norm(zT0)).item() < 1e-13
+    J0, gz0, gf0, zT0, _ = res[0]
+    for split in (2, 1):
+        J1, gz1, gf1, zT1, _ = res[split]
+        assert J1 == pytest.approx(J0, rel=1e-13), split
+        assert gf1 == pytest.approx(gf0, rel=1e-11, abs=1e-20), split
+        assert (torch.linalg.norm(gz1 - gz0) / torch.linalg.norm(gz0)).item() < 1e-12, split
+        assert (torch.linalg.norm(zT1 - zT0) / torch.linalg.norm(zT0)).item() < 1e-13, split
 
 
 @pytest.mark.parametrize("n,variant", [(256, 2), (1024, 2)])
