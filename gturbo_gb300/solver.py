@@ -199,8 +199,9 @@ class Solver:
 
         With a cache file (JSON, keyed by device name, N, integrator order and the library
         file's size and time), a stored choice is reused without timing; None disables it. Returns
-        {"variant": column variant, "row_variant": row variant, "col_split": whether the
-        field-split column passes run, "ms_per_step": per column variant or None, "cached": bool}.
+        {"variant": column variant, "row_variant": row variant, "col_split": the field-split
+        mode that runs (0, 1, 2: ``col_split``), "ms_per_step": per column variant or None,
+        "cached": bool}.
         """
         if cache == "default":
             cache = _tune_cache_default()
