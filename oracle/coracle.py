@@ -1,7 +1,8 @@
 """ctypes wrapper of the C oracle (``oracle/gturbo_oracle.c``).
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, the smoke check and the CPU-baseline leg
-of ``bench.py``, where it is the checker, never the thing measured for the GPU path.
+of ``bench.py``, where results are compared with it; it is never the thing measured for the
+GPU path.
 
 Fields are numpy float64 arrays of shape (N, N+2): the physical view ``real(8) z(N+2,N)``.
 ``spec(a)`` gives the complex (N, N/2+1) view of the same memory (``complex(8) z(N/2+1,N)``).

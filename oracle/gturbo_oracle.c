@@ -1,7 +1,7 @@
 /*
  * gturbo_oracle.c -- CPU FP64 ORACLE for the Gturbo time-stepping hot path.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker that the CUDA path is
+ * TEST INFRASTRUCTURE ONLY. This file is the reference that the CUDA path is
  * compared against (tests, the smoke check and the CPU-baseline leg of the
  * benchmark). It is never linked into, called by or shipped with the product
  * library.
