@@ -666,6 +666,35 @@ __device__ __forceinline__ void adj_colinv_field_tile(const AdjArgs& a, int unit
   for (int s = 0; s < R; ++s) dst[(size_t)(t + s * T) * NH + i] = v[s];
 }
 
+// The transposed pass C's value at (i, j) of the split forms from the transformed fields fq, fu,
+// fv, in the order q, u, v of adj_colfwd_tile: g = c (fq + conj(Mu) fu + conj(Mv) fv) with
+// conj(Mu) = -i ky/|k|^a, conj(Mv) = +i kx/|k|^a and c = cw (the row pass delivered 2 FFT(s);
+// 1/2 on kx = 0 and Nyquist), stored to q, then the stage update of a.mode.
+template <int N>
+__device__ __forceinline__ void adj_colfwd_store(const AdjArgs& a, int i, int j, double kx, double cw, double2 fq,
+                                                 double2 fu, double2 fv) {
+  constexpr int NH = N / 2 + 1;
+  const size_t o = (size_t)j * NH + i;
+  double2 g = make_double2(cw * fq.x, cw * fq.y);
+  const double mu = -__ldg(&a.fky[j]) * __ldg(&a.kainv[o]) * cw;
+  g = make_double2(fma(-mu, fu.y, g.x), fma(mu, fu.x, g.y));
+  const double mv = kx * __ldg(&a.kainv[o]) * cw;
+  g = make_double2(fma(-mv, fv.y, g.x), fma(mv, fv.x, g.y));
+  a.q[o] = g;
+  if (a.mode == ADJ_STAGE_B) {
+    const double e = stage_e(a.emk, a.emkx, a.emky, a.split, i, j, NH);
+    const bool origin = (i == 0 && j == 0);
+    const double2 l = a.lin[o];
+    a.lam[o] = origin ? czero() : make_double2(e * (e * l.x + g.x), e * (e * l.y + g.y));
+    a.rho[o] = origin ? czero() : make_double2(a.dt2 * e * g.x, a.dt2 * e * g.y);
+  } else if (a.mode == ADJ_PLAIN) {
+    a.lam[o] = g;
+  } else {
+    const double2 l = a.lam[o];
+    a.lam[o] = make_double2(l.x + g.x, l.y + g.y);
+  }
+}
+
 // Transposed pass C, field f of column i (unit 3 i + f; f = 0, 1, 2: q, u, v): the forward
 // transform written back in place; the third of the column's CTAs to finish (a per-column
 // counter, no waiting) reads the other two through L2, forms the accumulated gradient in the
@@ -699,25 +728,7 @@ __device__ __forceinline__ void adj_colfwd_field_tile(const AdjArgs& a, int unit
     const double2 fq = f == 0 ? v[s] : __ldcg(&a.q[o]);
     const double2 fu = f == 1 ? v[s] : __ldcg(&a.u[o]);
     const double2 fv = f == 2 ? v[s] : __ldcg(&a.v[o]);
-    // conj(Mu) = -i ky/|k|^a, conj(Mv) = +i kx/|k|^a
-    double2 g = make_double2(cw * fq.x, cw * fq.y);
-    const double mu = -__ldg(&a.fky[j]) * __ldg(&a.kainv[o]) * cw;
-    g = make_double2(fma(-mu, fu.y, g.x), fma(mu, fu.x, g.y));
-    const double mv = kx * __ldg(&a.kainv[o]) * cw;
-    g = make_double2(fma(-mv, fv.y, g.x), fma(mv, fv.x, g.y));
-    a.q[o] = g;
-    if (a.mode == ADJ_STAGE_B) {
-      const double e = stage_e(a.emk, a.emkx, a.emky, a.split, i, j, NH);
-      const bool origin = (i == 0 && j == 0);
-      const double2 l = a.lin[o];
-      a.lam[o] = origin ? czero() : make_double2(e * (e * l.x + g.x), e * (e * l.y + g.y));
-      a.rho[o] = origin ? czero() : make_double2(a.dt2 * e * g.x, a.dt2 * e * g.y);
-    } else if (a.mode == ADJ_PLAIN) {
-      a.lam[o] = g;
-    } else {
-      const double2 l = a.lam[o];
-      a.lam[o] = make_double2(l.x + g.x, l.y + g.y);
-    }
+    adj_colfwd_store<N>(a, i, j, kx, cw, fq, fu, fv);
   }
 }
 
@@ -753,28 +764,7 @@ __device__ __forceinline__ void adj_colfwd_cluster_tile(const AdjArgs& a, int un
   for (int s = 0; s < R; ++s) {
     if (s % 3 != f) continue;
     const int j = t + s * T;
-    const size_t o = (size_t)j * NH + i;
-    const double2 fq = f == 0 ? v[s] : pq[j];
-    const double2 fu = f == 1 ? v[s] : pu[j];
-    const double2 fv = f == 2 ? v[s] : pv[j];
-    double2 g = make_double2(cw * fq.x, cw * fq.y);
-    const double mu = -__ldg(&a.fky[j]) * __ldg(&a.kainv[o]) * cw;
-    g = make_double2(fma(-mu, fu.y, g.x), fma(mu, fu.x, g.y));
-    const double mv = kx * __ldg(&a.kainv[o]) * cw;
-    g = make_double2(fma(-mv, fv.y, g.x), fma(mv, fv.x, g.y));
-    a.q[o] = g;
-    if (a.mode == ADJ_STAGE_B) {
-      const double e = stage_e(a.emk, a.emkx, a.emky, a.split, i, j, NH);
-      const bool origin = (i == 0 && j == 0);
-      const double2 l = a.lin[o];
-      a.lam[o] = origin ? czero() : make_double2(e * (e * l.x + g.x), e * (e * l.y + g.y));
-      a.rho[o] = origin ? czero() : make_double2(a.dt2 * e * g.x, a.dt2 * e * g.y);
-    } else if (a.mode == ADJ_PLAIN) {
-      a.lam[o] = g;
-    } else {
-      const double2 l = a.lam[o];
-      a.lam[o] = make_double2(l.x + g.x, l.y + g.y);
-    }
+    adj_colfwd_store<N>(a, i, j, kx, cw, f == 0 ? v[s] : pq[j], f == 1 ? v[s] : pu[j], f == 2 ? v[s] : pv[j]);
   }
   cluster.sync();
 }

@@ -776,6 +776,20 @@ __device__ __forceinline__ void colinv_field_tile(const NltArgs& a, int unit) {
 // (N = 0 there: the epilogue only).
 __host__ __device__ inline int colfwd_split_units(int nh, int kxlim) { return 2 * (kxlim + 1) + (nh - 1 - kxlim); }
 
+// Pass C's value at (i, j) of the split forms from the column transforms fa = scale kx A (scaled
+// by the caller) and fb = B, A = F(u q), B = F(v q) (ky's factor carries the scale for B):
+// N = -i (kx A + ky B), re = kx Im A + ky Im B, im = -(kx Re A + ky Re B); zero outside the 2/3
+// cut (kc) and at the mean; then the stage epilogue.
+template <int N, bool KICK>
+__device__ __forceinline__ void colfwd_store(const NltArgs& a, int i, int j, int kc, double scale, double2 fa,
+                                             double2 fb) {
+  const double kys = __ldg(&a.fky[j]) * scale;
+  double2 nh = make_double2(fma(kys, fb.y, fa.y), -fma(kys, fb.x, fa.x));
+  const int aj = min(j, N - j);
+  if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
+  epilogue<KICK>(a.epi, i, j, N / 2 + 1, nh);
+}
+
 // Pass C, unit 2 i + g (g = 0: A, 1: B) of column i <= kxlim: the forward transform of the
 // field, written back in place (kx*FA for A). The second of the column's two CTAs to finish
 // (a per-column counter, no waiting) reads the other field and runs the epilogue. Its
@@ -820,14 +834,7 @@ __device__ __forceinline__ void colfwd_field_tile(const NltArgs& a, int unit) {
   for (int s = 0; s < R; ++s) {
     const int j = t + s * T;
     const double2 o = __ldcg(&other[(size_t)j * NH + i]);
-    const double2 fa = g == 0 ? v[s] : o;
-    const double2 fb = g == 0 ? o : v[s];
-    const double kys = __ldg(&a.fky[j]) * scale;
-    // N = -i (kx A + ky B): re = kx Im A + ky Im B, im = -(kx Re A + ky Re B)
-    double2 nh = make_double2(fma(kys, fb.y, fa.y), -fma(kys, fb.x, fa.x));
-    const int aj = min(j, N - j);
-    if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
-    epilogue<KICK>(a.epi, i, j, NH, nh);
+    colfwd_store<N, KICK>(a, i, j, kc, scale, g == 0 ? v[s] : o, g == 0 ? o : v[s]);
   }
 }
 
@@ -876,14 +883,7 @@ __device__ __forceinline__ void colfwd_cluster_tile(const NltArgs& a, int unit) 
   for (int s = 0; s < H; ++s) {
     const int j = t + (g * H + s) * T;
     const double2 o = peer[j];
-    const double2 fa = g == 0 ? v[g * H + s] : o;
-    const double2 fb = g == 0 ? o : v[g * H + s];
-    const double kys = __ldg(&a.fky[j]) * scale;
-    // N = -i (kx A + ky B): re = kx Im A + ky Im B, im = -(kx Re A + ky Re B)
-    double2 nh = make_double2(fma(kys, fb.y, fa.y), -fma(kys, fb.x, fa.x));
-    const int aj = min(j, N - j);
-    if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
-    epilogue<KICK>(a.epi, i, j, NH, nh);
+    colfwd_store<N, KICK>(a, i, j, kc, scale, g == 0 ? v[g * H + s] : o, g == 0 ? o : v[g * H + s]);
   }
   cluster.sync();
 }
