@@ -76,6 +76,17 @@ def workload(name):
     return p, IC_K0[name], desc
 
 
+def run_config(args):
+    """The JSON line's `config`, built the same way by both arms from the workload alone (the
+    GPU arm's launch settings go to its own `settings` object)."""
+    p, _, desc = workload(args.config)
+    return {"workload": desc, "n": p.n, "alpha": p.alpv, "rk": p.rko, "dt": p.dt,
+            "imix": p.imix,
+            "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single",
+            "l2": "no flush: working set ~202 MB > 126 MB L2" if p.n >= 2048 else
+                  "no flush: the working set fits in L2 (small grid)"}
+
+
 # ---------------------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------------------
@@ -193,7 +204,7 @@ def reference_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / res["value"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": desc},
+            "config": run_config(args),
             "cpu_baseline": res,
             "e2e": {"value": res["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -256,19 +267,19 @@ def pass_model(p, kind):
 
 # DRAM bytes (read + write) per launch of a pass, from single-kernel ncu captures
 # (dram__bytes_read.sum + dram__bytes_write.sum) of the same launch variant:
-#   2048^2, variant 0: ncu --set full -k "regex:k_nlt_(row|colfwd_inv|colinv)" -s 4 -c 3
+#   2048^2, variant 0: ncu --set full --clock-control none -k "regex:k_nlt_(row|colfwd_inv|colinv)" -s 4 -c 3
 #                      python bench.py --steps 2 --warmup 3 --no-extras --variant 0
-#   2048^2, variant 1: ncu --set full -k "regex:k_nltv_(row|colfwd_inv|colinv)" -s 4 -c 3
+#   2048^2, variant 1: ncu --set full --clock-control none -k "regex:k_nltv_(row|colfwd_inv|colinv)" -s 4 -c 3
 #                      python bench.py --steps 2 --warmup 3 --no-extras --variant 1
 #   256^2, column variant 3, row variant 2:
-#                      ncu --set full --kernel-name-base demangled -k "regex:k_nltv_(row<\(int\)256,
+#                      ncu --set full --clock-control none --kernel-name-base demangled -k "regex:k_nltv_(row<\(int\)256,
 #                      \(int\)2>|colfwd_inv<\(int\)256, \(int\)3>|colinv<\(int\)256, \(int\)3>)" -s 8 -c 3
 #                      python bench.py --config c1 --steps 2 --warmup 3 --no-extras --variant 3
 # Keyed by (N, the launch variant of that kernel: the row variant for the row pass, the column
 # variant otherwise, pass).
 # FP64 instructions (thread level) per launch of a pass, from ncu's
 # smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum of the same launch variant:
-#   2048^2, variant 1: ncu --metrics <those> -k "regex:k_nltv_(row|colfwd_inv|colinv)" -s 4 -c 3
+#   2048^2, variant 1: ncu --metrics <those> --clock-control none -k "regex:k_nltv_(row|colfwd_inv|colinv)" -s 4 -c 3
 #                      python bench.py --steps 2 --warmup 3 --no-extras --variant 1
 # The FP64 pipe issues 2 such operations per clock per SM (152 SMs).
 NCU_FP64_OPS = {
@@ -367,6 +378,28 @@ def ours_arm(args):
     # the kick after the diagnostics, which add one nonlinear term (3 passes) and 5 kernels
     per_step = 3 * stages if sol.col_split else 2 * stages + 1
     launches = K * (per_step + 1) + ndiag * (3 + 5)
+
+    # ---- diagnostics stated explicitly: the timed region holds ndiag diagnostics steps (one
+    # every imix); here one diagnostics step is timed against a plain step, and the rate with
+    # diagnostics every imix steps is derived from the two ------------------------------------
+    diag = {}
+    if rank == 0:
+        nd = 10
+        t_kind = {}
+        for with_diag in (False, True):
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(nd):
+                seed, _ = sol.main_step(z, seed, work, diag=with_diag)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t_kind[with_diag] = e0.elapsed_time(e1) / nd
+        extra = t_kind[True] - t_kind[False]
+        diag = {"imix": p.imix, "ms_per_plain_step": t_kind[False],
+                "ms_per_diag_step": t_kind[True], "ms_extra_per_diag_step": extra,
+                "steps_per_s_diag_every_imix": 1e3 / (t_kind[False] + extra / p.imix),
+                "note": "a diagnostics step adds one nonlinear term (3 passes) and the spectra, "
+                        "fluxes and budgets of src/diagnostics.f90 to a plain step"}
 
     extras = {}
     if rank == 0:
@@ -493,14 +526,13 @@ def ours_arm(args):
                 "warmup": W, "ms_per_step": 1e3 * t_all / K, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (random-phase IC, reference LCG forcing, seed 481929)",
-                "config": {"workload": desc, "n": p.n, "alpha": p.alpv, "rk": p.rko,
-                           "imix": p.imix, "diag_calls_timed": ndiag,
-                           "launch_variant": tune["variant"],
-                           "row_variant": sol.variants[1], "col_split": sol.col_split, "pdl": sol.pdl,
-                           "autotune_ms_per_step": tune["ms_per_step"],
-                           "parallelism": f"replicas x{world}" if world > 1 else "single",
-                           "l2": "no flush: working set ~202 MB > 126 MB L2"},
+                "config": run_config(args),
+                "settings": {"launch_variant": tune["variant"], "row_variant": sol.variants[1],
+                             "col_split": sol.col_split, "pdl": sol.pdl,
+                             "autotune_ms_per_step": tune["ms_per_step"]},
                 "gpu_launches": launches, "finite": finite, "clocks": clk}
+        diag["calls_timed"] = ndiag
+        line["diagnostics"] = diag
         line.update(extras)
         print(json.dumps(line), flush=True)
     if world > 1:

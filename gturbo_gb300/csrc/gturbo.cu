@@ -1161,8 +1161,10 @@ int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best)
 // The scratch (partial shell sums, per-row budgets, the k^2 tables) is this file-scope device
 // array, present on every GPU that loads the library until the process exits. Host code
 // reaches it only through the address that cudaGetSymbolAddress returns for the current
-// device; the first call on each device looks that address up, so that first call should be
-// made before any stream capture. Every call rewrites all the scratch it reads, so nothing
+// device. Every call made outside a stream capture looks that address up again (a device reset
+// between calls is therefore harmless); a call made while its stream captures reuses the
+// address of the device's last earlier call, so the first call on each device should be made
+// before any stream capture. Every call rewrites all the scratch it reads, so nothing
 // has to start at zero; calls that overlap on the GPU (other streams, other threads) share
 // the array and race.
 // ---------------------------------------------------------------------------------------
@@ -1226,18 +1228,27 @@ extern "C" int gt_diag_static(const gt_params* p, const double* z, const double*
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "gt_diag_static: cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices) return fail(nullptr, GT_ERR_ARG, "gt_diag_static: device index");
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(s, &capturing);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "gt_diag_static: cudaStreamIsCapturing");
   double* base;
   {
+    // Outside a capture the address is looked up on every call, so a device reset or a
+    // re-created primary context between calls leaves no stale address behind. A call on a
+    // capturing stream reuses the address of the device's last earlier call.
     std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_ptr[dev]) {
+    if (capturing == cudaStreamCaptureStatusNone) {
       void* ptr = nullptr;
       e = cudaGetSymbolAddress(&ptr, g_diag_scratch);
       if (e != cudaSuccess) return cuda_fail(nullptr, e, "gt_diag_static: cudaGetSymbolAddress");
       g_static_ptr[dev] = static_cast<double*>(ptr);
+    } else if (!g_static_ptr[dev]) {
+      return fail(nullptr, GT_ERR_STATE,
+                  "gt_diag_static: first call on this device made during a stream capture");
     }
     base = g_static_ptr[dev];
   }
-  cudaStream_t s = (cudaStream_t)cuda_stream;
   const int nh = n / 2 + 1, nb = n / 2;
   gt::DiagArgs D;
   D.z = reinterpret_cast<const double2*>(z);

@@ -253,10 +253,13 @@ int gt_diag(gt_handle* h, const double* z, const double* znl,
  *   z, znl   device fields as for gt_diag
  *   sp..glob DEVICE output arrays (NBIN doubles; glob 6), any may be NULL
  *   stream   CUDA stream of the work (NULL = legacy default stream)
- * Asynchronous: returns after enqueueing. No NaN/Inf check. The first call on
- * a device looks up the scratch address there, so make it before any stream
- * capture. All calls share the scratch: calls that overlap on the GPU race.
- * Errors are reported through gt_last_error(NULL). */
+ * Asynchronous: returns after enqueueing. No NaN/Inf check. Every call made
+ * outside a stream capture looks up the scratch address on the current device
+ * (so a cudaDeviceReset between calls is harmless); a call on a capturing
+ * stream reuses the address of the device's last earlier call and fails with
+ * GT_ERR_STATE if there was none, so make the first call on a device before
+ * any stream capture. All calls share the scratch: calls that overlap on the
+ * GPU race. Errors are reported through gt_last_error(NULL). */
 int gt_diag_static(const gt_params* p, const double* z, const double* znl,
                    double* sp, double* sz, double* fle, double* flz, double* glob,
                    void* cuda_stream);

@@ -63,3 +63,20 @@ def test_reference_arm_line():
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_both_arms_share_one_config(monkeypatch):
+    """Both arms build `config` with the same helper from the workload alone, so the two lines'
+    configs are equal; launch settings of the CUDA arm live in its own `settings` object."""
+    bench = _bench_module()
+    a = _parse(["--config", "c1"], monkeypatch)
+    cfg = bench.run_config(a)
+    assert cfg == bench.run_config(_parse(["--config", "c1", "--impl", "reference"], monkeypatch))
+    for k in ("workload", "n", "alpha", "rk", "dt", "imix", "parallelism", "l2"):
+        assert k in cfg, k
+    assert cfg["n"] == 256 and cfg["rk"] == 4
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--config", "c1", "--steps", "1",
+                          "--warmup", "1", "--cpu-seconds", "1"], cwd=ROOT, capture_output=True, text=True,
+                         timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert json.loads(out.stdout.strip().splitlines()[-1])["config"] == cfg

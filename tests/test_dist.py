@@ -85,29 +85,70 @@ def test_member_sharding_partitions_and_balances():
         shard_members(costs, 0)
 
 
+def _small_ensemble():
+    """Six members of mixed size and alpha (RK4, Philox forcing), small enough for the oracle."""
+    from gturbo_gb300.ensemble import Member
+    from gturbo_gb300.params import Params, famp_for_injection
+
+    out = []
+    for m, (n, a) in enumerate(((32, 0.5), (64, 1.0), (32, 2.0), (64, 3.0), (32, 1.0), (64, 2.0))):
+        p = Params(n=n, alpv=a, rko=4, dt=0.25 / n, nu=1e-12, alpnu=4.0, mu=0.05, alpmu=0.0,
+                   k1f=n / 16.0, k2f=n / 16.0 + 2.0)
+        p = p.replace(famp=famp_for_injection(p, 1.0))
+        out.append(Member(params=p, key=0x6774_0000 + m, k0=n / 16.0, ic_seed=1000 + m))
+    return out
+
+
+def _advance(member, steps):
+    """One member through the oracle: RK4 step, then the Philox kick at the step counter."""
+    from gturbo_gb300.ic import random_phase_ic
+    from oracle.coracle import Oracle
+
+    o = Oracle(member.params)
+    z = random_phase_ic(member.params, member.k0, 0.5, seed=member.ic_seed)
+    for step in range(steps):
+        o.step4(z)
+        o.forcing_philox(z, member.key, step)
+    return z
+
+
 def _shard_worker(rank, world, port, outdir):
     import torch.distributed as dist
 
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
-    from gturbo_gb300.replicas import shard_members, whole_job_rate
-    costs = [4.0, 4.0, 2.0, 1.0, 1.0, 1.0, 1.0]
-    mine = shard_members(costs, world)[rank]
-    # each rank "advances" its own members (no collective on data); only rates combine
-    units, smax, rate = whole_job_rate(len(mine) * 10, 1.0 + 0.5 * rank)
-    np.save(os.path.join(outdir, f"s{rank}.npy"), np.array(mine + [-1] * (7 - len(mine))))
+    from gturbo_gb300.replicas import member_cost, shard_members, whole_job_rate
+
+    members = _small_ensemble()
+    mine = shard_members([member_cost(m.params.n, m.params.rko) for m in members], world)[rank]
+    # each rank advances its own members (no collective on the data path); only rates combine
+    for i in mine:
+        np.save(os.path.join(outdir, f"m{i}_r{rank}.npy"), _advance(members[i], 4))
+    units, smax, rate = whole_job_rate(len(mine) * 4, 1.0 + 0.5 * rank)
     np.save(os.path.join(outdir, f"u{rank}.npy"), np.array([units, smax, rate]))
     dist.barrier()
     dist.destroy_process_group()
 
 
-def test_sharded_ensemble_rates_gloo_world2(tmp_path):
+def test_sharded_ensemble_gloo_world2_equals_one_process(tmp_path):
+    """Two gloo ranks each advance their shard of a mixed-size ensemble (RK4 + Philox kicks)
+    through the oracle: every member is advanced by exactly one rank, and the union of the
+    shards equals a single-process run of all members bit for bit."""
     world = 2
     mp.spawn(_shard_worker, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
-    s0 = [i for i in np.load(tmp_path / "s0.npy") if i >= 0]
-    s1 = [i for i in np.load(tmp_path / "s1.npy") if i >= 0]
-    assert sorted(s0 + s1) == list(range(7)) and not set(s0) & set(s1)
+    members = _small_ensemble()
+    owners = {}
+    for f in tmp_path.glob("m*_r*.npy"):
+        i, r = (int(x) for x in f.stem[1:].split("_r"))
+        assert i not in owners
+        owners[i] = r
+    assert sorted(owners) == list(range(len(members)))
+    assert set(owners.values()) == {0, 1}
+    for i, m in enumerate(members):
+        got = np.load(tmp_path / f"m{i}_r{owners[i]}.npy")
+        assert np.isfinite(got).all()
+        assert np.array_equal(got, _advance(m, 4)), i
     u0, u1 = np.load(tmp_path / "u0.npy"), np.load(tmp_path / "u1.npy")
     assert np.array_equal(u0, u1)
-    assert u0[0] == 70 and u0[1] == 1.5 and u0[2] == pytest.approx(70 / 1.5)
+    assert u0[0] == 4 * len(members) and u0[1] == 1.5

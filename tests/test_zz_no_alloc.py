@@ -8,7 +8,8 @@ its scratch in a static device array and takes only the caller's fields and outp
 This file sorts last so that a run stopping at the first failure has already run every other
 test. It calls the entry point through the C-ABI twice in a row (the second call on a smaller
 grid, so stale scratch from the first call would show) and checks each result against
-gt_diag, with the tolerances of the other diagnostics tests.
+gt_diag and against the oracle, with the tolerances of the other diagnostics tests; a third call
+asks for one output only.
 """
 import ctypes
 
@@ -59,13 +60,44 @@ def test_diag_static_matches_gt_diag_on_two_calls():
         z = torch.from_numpy(a).cuda()
         znl = torch.from_numpy(b).cuda()
         ref = Solver(p).diag(z, znl)
+        direct = orc.diag(a, b)
         got = _static_diag(lib, p, z, znl)
         for k in ("sp", "sz", "glob"):
             assert np.isfinite(got[k]).all(), k
             assert rel_l2(got[k], ref[k]) < 1e-13, k
+            assert rel_l2(got[k], direct[k]) < 1e-12, k
         for k in ("fle", "flz"):
             assert np.isfinite(got[k]).all(), k
             assert np.abs(got[k] - ref[k]).max() <= 1e-12 * np.abs(ref[k]).max(), k
+            assert np.abs(got[k] - direct[k]).max() <= 1e-12 * np.abs(direct[k]).max(), k
+
+
+def test_diag_static_subset_of_outputs_leaves_the_others_untouched():
+    """znl = NULL with only sp requested (no fluxes, no budgets): sp matches the oracle and the
+    output arrays that were not passed keep their NaN contents."""
+    from gturbo_gb300 import _lib
+
+    lib = _lib.load()
+    p = _params(128, 1.0)
+    orc = Oracle(p)
+    a = rand_field(orc, 33)
+    z = torch.from_numpy(a).cuda()
+    nb = p.n // 2
+    sp = torch.full((nb,), float("nan"), dtype=torch.float64, device="cuda")
+    others = [torch.full((nb,), float("nan"), dtype=torch.float64, device="cuda") for _ in range(3)]
+    glob = torch.full((6,), float("nan"), dtype=torch.float64, device="cuda")
+    cp = p.to_ctypes()
+    rc = lib.gt_diag_static(ctypes.byref(cp), z.data_ptr(), None, sp.data_ptr(), None, None, None,
+                            None, None)
+    assert rc == 0, lib.gt_last_error(None)
+    torch.cuda.synchronize()
+    assert rel_l2(sp.cpu().numpy(), orc.diag(a)["sp"]) < 1e-12
+    for t in others + [glob]:
+        assert torch.isnan(t).all()
+    # fluxes without znl are refused
+    rc = lib.gt_diag_static(ctypes.byref(cp), z.data_ptr(), None, None, None, others[0].data_ptr(),
+                            None, None, None)
+    assert rc == 1  # GT_ERR_ARG
 
 
 def test_diag_static_rejects_grid_beyond_its_scratch():
