@@ -31,10 +31,16 @@
  * directly from cos/sin. For Z2D the imaginary parts of the kx=0 and kx=N/2
  * values are ignored (Hermitian input), the convention of numpy's irfft2.
  *
- * PARITY UNPINNED: the reference cannot be built or run (nvfortran + OpenACC +
- * cuFFT; no Fortran compiler exists here or on the GPU host) and ships no test
- * vectors. This oracle is pinned instead to an independent numpy restatement,
- * to analytic known answers and to the closed form of the LCG.
+ * PINNED to the reference's own statements: the reference cannot be compiled
+ * (nvfortran + OpenACC + cuFFT; no Fortran compiler exists here or on the GPU
+ * host) and ships no test vectors, so its Fortran library sources are
+ * transliterated mechanically into C (oracle/f2c_ref.py -> oracle/_ref, the
+ * cuFFT calls answered by a shim following cuFFT's documented definitions).
+ * This oracle matches it bit for bit on every routine without a transform
+ * (tables, mode list, LCG, trunc, produ, forcing, diagnostics) and to rounding
+ * on the rest; the golden vectors of tests/golden/ are computed by it. It is
+ * also checked against an independent numpy restatement, analytic known
+ * answers and the closed form of the LCG.
  *
  * Threads: OpenMP over rows / column blocks (deterministic: every output value
  * is computed by exactly one thread in a fixed order). Reductions

@@ -1,8 +1,12 @@
-"""Generate the golden vectors of tests/golden/ from the numpy restatement (oracle/np_oracle.py).
+"""Generate the golden vectors of tests/golden/ from the reference's own statements.
 
-The reference publishes no test vectors and cannot be run (Fortran + OpenACC + cuFFT, no Fortran
-compiler available), so the fixtures come from the independent numpy restatement of its
-routines. The C oracle and the CUDA path are both checked against them. Run from the repo root:
+The reference ships no test vectors (its Makefile's ``verify`` target is empty) and cannot be
+compiled here (Fortran + OpenACC + cuFFT, no Fortran compiler available). Its library sources are
+transliterated mechanically into C by ``oracle/f2c_ref.py`` (the cuFFT calls answered by a shim
+that follows cuFFT's documented transform definitions), and every vector below is computed by
+those transliterated routines: defk, iniforcing, fft_dir, fft_inv, trunc, nlt, step/step4,
+forcing/rann, spectrum/fluxes/glob and writef2. The C oracle and the CUDA path are both checked
+against the files. Run from the repository root where the reference checkout is present:
 
     python tests/golden/make_golden.py
 """
@@ -10,6 +14,7 @@ from __future__ import annotations
 
 import os
 import sys
+import tempfile
 
 import numpy as np
 
@@ -17,7 +22,6 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 
 from gturbo_gb300.params import Params  # noqa: E402
-from oracle.np_oracle import NpOracle, to_phys_layout  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 
@@ -30,51 +34,93 @@ CASES = {
     "n64_a05_rk2_split": (Params(n=64, alpv=0.5, rko=2, k1f=4.0, k2f=6.0, nu=1e-4, alpnu=1.0,
                                  mu=0.0, alpmu=0.0, dt=1e-3, famp=0.2), 103),
 }
-
-
-def input_field(q: NpOracle, seed: int) -> np.ndarray:
-    rng = np.random.default_rng(seed)
-    x = rng.standard_normal((q.n, q.n))
-    return q.trunc(q.fft_dir(x)) * 20.0, x
+# main-loop horizon: steps of src/main.f90:97-137 with diagnostics every HORIZON_IMIX steps
+HORIZON_STEPS = 20
+HORIZON_IMIX = 10
 
 
 def make_case(name, p, seed):
-    q = NpOracle(p)
-    zk, x = input_field(q, seed)
-    out = {"n": p.n}
-    out["phys_in"] = x
-    out["fft_dir"] = to_phys_layout(q.fft_dir(x))
-    out["spec_in"] = to_phys_layout(zk)
-    out["fft_inv"] = q.fft_inv(zk)
-    out["nlt"] = to_phys_layout(q.nlt(zk))
-    out["step"] = to_phys_layout(q.rk_step(zk))
-    zf, s = zk, 481929
+    from oracle.refcore import Reference
+
+    r = Reference(p)
+    n = p.n
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((n, n))
+    out = {"n": p.n, "phys_in": x}
+    a = r.zeros()
+    a[:, :n] = x
+    r.fft_dir(a)
+    out["fft_dir"] = a.copy()
+    r.trunc(a)
+    a *= 20.0
+    zk = a
+    out["spec_in"] = zk.copy()
+    b = zk.copy()
+    r.fft_inv(b)
+    out["fft_inv"] = b[:, :n].copy()
+    b = zk.copy()
+    r.nlt(b)
+    out["nlt"] = b.copy()
+    znl = b
+    b = zk.copy()
+    r.rk_step(b)
+    out["step"] = b.copy()
+    b, s = zk.copy(), 481929
     for _ in range(3):
-        zf, s = q.forcing(zf, s)
-    out["forcing3"] = to_phys_layout(zf)
+        s = r.forcing(b, s)
+    out["forcing3"] = b
     out["forcing3_seed"] = np.array([s], np.int64)
-    d = q.diag(zk, q.nlt(zk))
-    for k, v in d.items():
-        out["diag_" + k] = v
-    ik = np.array([m[0] for m in q.modes], np.int32)
-    jk = np.array([m[1] for m in q.modes], np.int32)
+    d = r.diag(zk.copy(), znl)
+    for k in ("sp", "sz", "fle", "flz", "glob"):
+        out["diag_" + k] = d[k]
+        out["diag_written_" + k] = d["written"][k].astype(np.float32)
+    ik, jk = r.forcing_modes()
     out["ikxf"], out["ikyf"] = ik, jk
-    out["inpe"] = np.array([q.inpe])
+    info = r.info()
+    out["inpe"] = np.array([info["inpe"]])
+    out["inpz"] = np.array([info["inpz"]])
+    t = r.tables()
+    out["emk"] = t["emk"]
+    # the dump record of fields/w.NNN.MMM (main.f90:119-125: znl = z, fft_inv, writef2)
+    with tempfile.TemporaryDirectory() as wd:
+        b = zk.copy()
+        r.fft_inv(b)
+        path = r.writef2(b, 0, 1, wd)
+        raw = np.fromfile(path, dtype=np.uint8)
+    out["dump_record"] = raw[4:-4].view(np.float32).reshape(n, n).copy()
+    # main-loop horizon from the same field and the reference's seed
+    z, s = zk.copy(), 481929
+    work = [r.zeros() for _ in range(4)]
+    spectra = []
+    for ipas in range(1, HORIZON_STEPS + 1):
+        s, dd = r.main_step(z, s, ipas, HORIZON_IMIX, work)
+        if dd is not None:
+            spectra.append(np.stack([dd["sp"], dd["sz"], dd["fle"], dd["flz"]]))
+    out["horizon_z"] = z
+    out["horizon_seed"] = np.array([s], np.int64)
+    out["horizon_spectra"] = np.stack(spectra)
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
 
 
 def make_lcg():
-    s = 481929
+    from oracle.refcore import Reference
+
+    r = Reference(CASES["n32_a2_rk4"][0])
     draws, states = [], []
+    s = 481929
     for _ in range(1000):
-        r, s = NpOracle.rann(s)
-        draws.append(r)
+        d, s = r.rann(s, 1)
+        draws.append(d[0])
         states.append(s)
     np.savez_compressed(os.path.join(OUT, "lcg_481929.npz"), draws=np.array(draws, np.float32),
                         states=np.array(states, np.int64))
 
 
 if __name__ == "__main__":
+    from oracle import refcore
+
+    if not refcore.available():
+        sys.exit("the reference's sources are needed to generate the golden vectors")
     for name, (p, seed) in CASES.items():
         make_case(name, p, seed)
     make_lcg()

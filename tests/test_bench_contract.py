@@ -59,6 +59,9 @@ def test_reference_arm_line():
     assert line["impl"] == "reference"
     assert line["value"] > 0 and line["unit"] == "steps/s" and line["higher_is_better"] is True
     assert line["cpu_baseline"]["kind"] in ("port", "reference")
+    from oracle import refcore
+    if refcore.available():  # the reference's own statements, transliterated (oracle/_ref)
+        assert line["cpu_baseline"]["kind"] == "reference"
     assert line["cpu_baseline"]["cores"] >= 1 and line["cpu_baseline"]["value"] == line["value"]
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]

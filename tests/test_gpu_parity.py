@@ -455,7 +455,8 @@ def test_spectra_50_step_horizon(cfg):
 
 @pytest.mark.parametrize("name", ["n32_a2_rk4", "n64_a1_rk2", "n64_a05_rk2_split"])
 def test_against_golden_vectors(name):
-    """The CUDA path against the committed vectors of the numpy restatement."""
+    """The CUDA path against the committed vectors of the reference's own statements
+    (tests/golden/make_golden.py: the transliterated Fortran with the cuFFT shim)."""
     import os
     from tests.golden.make_golden import CASES
     p, _ = CASES[name]
@@ -484,6 +485,28 @@ def test_against_golden_vectors(name):
     assert np.abs(_host(z) - g["forcing3"]).max() < 1e-14
     ik, jk = sol.forcing_modes()
     assert np.array_equal(ik, g["ikxf"]) and np.array_equal(jk, g["ikyf"])
+    # diagnostics of the fixture's field and its nonlinear term (FP64 operands of the writes)
+    d = sol.diag(_dev(g["spec_in"]), _dev(g["nlt"]))
+    for k in ("sp", "sz", "fle", "flz", "glob"):
+        ref = g["diag_" + k]
+        assert np.abs(d[k] - ref).max() <= 1e-12 * np.abs(ref).max(), k
+    # the dump record of fields/w.NNN.MMM, within one real(4) rounding
+    rec = sol.dump_real4(_dev(g["spec_in"]))
+    ulp = np.spacing(np.abs(g["dump_record"])).astype(np.float64)
+    assert (np.abs(rec.astype(np.float64) - g["dump_record"]) <= ulp).all()
+    # the main loop (step, diagnostics every HORIZON_IMIX, forcing) over the fixture's horizon
+    from tests.golden.make_golden import HORIZON_IMIX, HORIZON_STEPS
+    z, work, s = _dev(g["spec_in"]), sol.work(), 481929
+    spectra = []
+    for ipas in range(1, HORIZON_STEPS + 1):
+        s, out = sol.main_step(z, s, work, diag=(ipas % HORIZON_IMIX == 0))
+        if out is not None:
+            spectra.append(np.stack([out["sp"], out["sz"], out["fle"], out["flz"]]))
+    assert s == int(g["horizon_seed"][0])
+    assert rel_l2(_host(z), g["horizon_z"]) < TOL
+    got, ref = np.stack(spectra), g["horizon_spectra"]
+    for k in range(4):
+        assert np.abs(got[:, k] - ref[:, k]).max() <= 1e-9 * np.abs(ref[:, k]).max()
 
 
 def test_single_mode_decay_on_gpu():
