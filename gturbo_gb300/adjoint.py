@@ -46,8 +46,15 @@ def tlm_run(sol: Solver, z0, dz0, dfamp: float, nsteps: int, seed: int, kmin: fl
     return J.value, dJ.value
 
 
-def gradient(sol: Solver, z0, nsteps: int, seed: int, kmin: float, kmax: float, checkpoint: int = 20):
-    """(J, dJ/dz0, dJ/dfamp, z_T, (forward ms, backward ms)) by the checkpointed adjoint."""
+def gradient(sol: Solver, z0, nsteps: int, seed: int, kmin: float, kmax: float, checkpoint: int = 20,
+             memory: int | None = None):
+    """(J, dJ/dz0, dJ/dfamp, z_T, (forward ms, backward ms)) by the checkpointed adjoint.
+
+    ``memory`` (bytes), when given, sets the handle's budget for whole kept segments
+    (``Solver.adj_memory``): the forward sweep keeps as many of its last segments as fit, and only
+    the earlier ones are recomputed from their checkpoints."""
+    if memory is not None:
+        sol.adj_memory = memory
     J, gf = ctypes.c_double(), ctypes.c_double()
     gz, zT = sol.field(), sol.field()
     t = (ctypes.c_double * 2)()

@@ -7,6 +7,8 @@
 // forcing amplitude famp; the forcing phases are the reference's LCG sequence from a seed.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -281,6 +283,24 @@ struct Phys {
   double2* q = nullptr;
 };
 
+// Segments the forward sweep of gt_adj_gradient keeps whole: as many of its last segments as
+// the handle's budget (gt_adj_set_memory) holds, at least one (the storage a recomputed segment
+// needs anyway) and at most all of them; never more than 90 % of the free device memory allows.
+// step_bytes: one step's stage states and physical fields.
+int kept_segments(const gt_handle* h, int ncp, int K, size_t step_bytes) {
+  const int64_t seg = (int64_t)K * (int64_t)step_bytes;
+  int64_t budget = gt::handle_adj_memory(h);
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+    const int64_t cap = (int64_t)(0.9 * (double)free_b);
+    if (budget > cap) budget = cap;
+  } else {
+    cudaGetLastError();
+  }
+  const int64_t fit = seg > 0 ? budget / seg : 0;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(ncp, fit));
+}
+
 // w = P0 e (z + dt/2 N(z)): the forward stage A with the fused passes (work: 3 fields)
 int stage_a(gt_handle* h, const double* z, double* w, double* const* work, Phys keep = Phys()) {
   gt::GtOp op = op_of(h, gt::OP_NLT_COLINV);
@@ -528,24 +548,27 @@ int gradient_rk4(gt_handle* h, const double* z0, int nsteps, int32_t seed, int K
   const size_t fb = field_bytes(h);
   const int n = gt::handle_params(h)->n;
   const int ncp = (nsteps + K - 1) / K;
+  const size_t uvb = sizeof(double2) * (size_t)n * n, qb = sizeof(double2) * (size_t)n * (n / 2);
+  // the forward sweep keeps its last m segments whole (slots for m K steps)
+  const int m = kept_segments(h, ncp, K, 4 * fb + 4 * (uvb + qb));
+  const int slots = m * K;
   DevPool pool;
-  std::vector<double*> cp(ncp), zs(K), w1(K), w2(K), w3(K), work(8);
+  std::vector<double*> cp(ncp), zs(slots), w1(slots), w2(slots), w3(slots), work(8);
   for (auto* v : {&cp, &zs, &w1, &w2, &w3, &work})
     for (auto& q : *v) q = pool.field(fb);
   double* z = pool.field(fb);
   double* znew = pool.field(fb);
   double* lam = pool.field(fb);
   double* scal = pool.field(sizeof(double) * ((size_t)nsteps + n + 2));
-  if (pool.ptrs.size() != (size_t)(ncp + 4 * K + 8 + 4))
+  if (pool.ptrs.size() != (size_t)(ncp + 4 * slots + 8 + 4))
     return afail(h, GT_ERR_NOMEM, "gt_adj_gradient: cudaMalloc of the checkpoint storage failed");
   double* dots = scal;
   double* rows = scal + nsteps;
-  // the physical u+iv and q of the 4K stage evaluations of a segment (24 N^2 bytes each), read
-  // by the transposed terms; without the memory for them those terms transform x themselves
+  // the physical u+iv and q of the 4 stage evaluations of every slot's step (24 N^2 bytes each),
+  // read by the transposed terms; without the memory for them those terms transform x themselves
   DevPool phys_pool;
-  std::vector<Phys> keep(4 * (size_t)K);
+  std::vector<Phys> keep(4 * (size_t)slots);
   {
-    const size_t uvb = sizeof(double2) * (size_t)n * n, qb = sizeof(double2) * (size_t)n * (n / 2);
     bool ok = true;
     for (auto& k : keep) {
       if (!ok) break;
@@ -565,15 +588,15 @@ int gradient_rk4(gt_handle* h, const double* z0, int nsteps, int32_t seed, int K
   std::vector<int32_t> seeds(nsteps);
   GA_CUDA(h, cudaEventRecord(e0, s));
   GA_CUDA(h, cudaMemcpyAsync(z, z0, fb, cudaMemcpyDeviceToDevice, s));
-  const int last0 = (ncp - 1) * K;
+  const int keep0 = (ncp - m) * K;  // first step of the kept segments
   int32_t sd = seed;
   int rc = GT_OK;
   for (int st = 0; st < nsteps; ++st) {
     if (st % K == 0) GA_CUDA(h, cudaMemcpyAsync(cp[st / K], z, fb, cudaMemcpyDeviceToDevice, s));
     seeds[st] = sd;
-    const int r = st >= last0 ? st - last0 : 0;  // earlier steps use slot 0 as scratch
-    if (st >= last0) GA_CUDA(h, cudaMemcpyAsync(zs[r], z, fb, cudaMemcpyDeviceToDevice, s));
-    rc = rk4_step_keep(h, z, w1[r], w2[r], w3[r], znew, work.data(), st >= last0 ? &keep[4 * r] : nullptr);
+    const int r = st >= keep0 ? st - keep0 : 0;  // earlier steps use slot 0 as scratch
+    if (st >= keep0) GA_CUDA(h, cudaMemcpyAsync(zs[r], z, fb, cudaMemcpyDeviceToDevice, s));
+    rc = rk4_step_keep(h, z, w1[r], w2[r], w3[r], znew, work.data(), st >= keep0 ? &keep[4 * (size_t)r] : nullptr);
     if (!rc) rc = gt_forcing(h, z, &sd);
     if (rc) return rc;
   }
@@ -583,7 +606,9 @@ int gradient_rk4(gt_handle* h, const double* z0, int nsteps, int32_t seed, int K
   GA_CUDA(h, cudaEventRecord(e1, s));
   for (int c = ncp - 1; c >= 0; --c) {
     const int s0 = c * K, s1 = (s0 + K < nsteps) ? s0 + K : nsteps;
-    if (c != ncp - 1) {  // recompute the segment's stage states from its checkpoint
+    const bool kept = c >= ncp - m;        // stored by the forward sweep
+    const int base = kept ? s0 - keep0 : 0;  // its first slot (recomputed segments: slot 0)
+    if (!kept) {  // recompute the segment's stage states from its checkpoint
       GA_CUDA(h, cudaMemcpyAsync(zs[0], cp[c], fb, cudaMemcpyDeviceToDevice, s));
       for (int st = s0; st < s1; ++st) {
         const int r = st - s0;
@@ -600,11 +625,11 @@ int gradient_rk4(gt_handle* h, const double* z0, int nsteps, int32_t seed, int K
       }
     }
     for (int st = s1 - 1; st >= s0; --st) {
-      const int r = st - s0;
+      const int r = base + st - s0;
       rc = forcing_dot_dev(h, lam, (uint32_t)seeds[st], dots + st);
       // a recomputed segment's last stage D was not evaluated: its term transforms w3 itself
       Phys kr[4] = {keep[4 * (size_t)r], keep[4 * (size_t)r + 1], keep[4 * (size_t)r + 2], keep[4 * (size_t)r + 3]};
-      if (c != ncp - 1 && st + 1 == s1) kr[3] = Phys();
+      if (!kept && st + 1 == s1) kr[3] = Phys();
       if (!rc) rc = adj_step_rk4(h, zs[r], w1[r], w2[r], w3[r], lam, work.data(), kr);
       if (rc) return rc;
     }
@@ -728,8 +753,12 @@ int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed
   const size_t fb = field_bytes(h);
   const int n = gt::handle_params(h)->n;
   const int ncp = (nsteps + K - 1) / K;
+  const size_t uvb = sizeof(double2) * (size_t)n * n, qb = sizeof(double2) * (size_t)n * (n / 2);
+  // the forward sweep keeps its last m segments whole (slots for m K steps)
+  const int m = kept_segments(h, ncp, K, 2 * fb + 2 * (uvb + qb));
+  const int slots = m * K;
   DevPool pool;
-  std::vector<double*> cp(ncp), zs(K), ws(K), work(6);
+  std::vector<double*> cp(ncp), zs(slots), ws(slots), work(6);
   for (auto& p : cp) p = pool.field(fb);
   for (auto& p : zs) p = pool.field(fb);
   for (auto& p : ws) p = pool.field(fb);
@@ -737,19 +766,18 @@ int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed
   double* z = pool.field(fb);
   double* lam = pool.field(fb);
   double* scal = pool.field(sizeof(double) * ((size_t)nsteps + n + 2));
-  if (pool.ptrs.size() != (size_t)(ncp + 2 * K + 6 + 3))
+  if (pool.ptrs.size() != (size_t)(ncp + 2 * slots + 6 + 3))
     return afail(h, GT_ERR_NOMEM, "gt_adj_gradient: cudaMalloc of the checkpoint storage failed");
   double* dots = scal;           // [nsteps]
   double* rows = scal + nsteps;  // [n + 1], objective scratch + result
-  // The physical u+iv and q of every recomputed stage of a segment (2K evaluations, 24 N^2 bytes
-  // each), so that the adjoint passes do not transform the linearisation points again. Without
-  // the memory for them the adjoint recomputes those transforms itself.
+  // The physical u+iv and q of both stages of every slot's step (24 N^2 bytes each), so that the
+  // adjoint passes do not transform the linearisation points again. Without the memory for them
+  // the adjoint recomputes those transforms itself.
   DevPool phys_pool;
-  std::vector<Phys> pz(K), pw(K);
+  std::vector<Phys> pz(slots), pw(slots);
   {
-    const size_t uvb = sizeof(double2) * (size_t)n * n, qb = sizeof(double2) * (size_t)n * (n / 2);
     bool ok = true;
-    for (int r = 0; r < K && ok; ++r) {
+    for (int r = 0; r < slots && ok; ++r) {
       pz[r].uv = reinterpret_cast<double2*>(phys_pool.field(uvb));
       pz[r].q = reinterpret_cast<double2*>(phys_pool.field(qb));
       pw[r].uv = reinterpret_cast<double2*>(phys_pool.field(uvb));
@@ -758,7 +786,7 @@ int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed
     }
     if (!ok) {
       cudaGetLastError();  // clear the failed allocation
-      for (int r = 0; r < K; ++r) pz[r] = pw[r] = Phys();
+      for (int r = 0; r < slots; ++r) pz[r] = pw[r] = Phys();
     }
   }
   cudaEvent_t e0, e1, e2;
@@ -769,15 +797,15 @@ int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed
   GA_CUDA(h, cudaEventRecord(e0, s));
   // forward sweep, checkpoint every K steps
   GA_CUDA(h, cudaMemcpyAsync(z, z0, fb, cudaMemcpyDeviceToDevice, s));
-  // The last segment keeps its states (z_s, w_s) and physical fields as it goes: the backward
-  // sweep starts on it without recomputing it.
-  const int last0 = (ncp - 1) * K;
+  // The last m segments keep their states (z_s, w_s) and physical fields as they go: the
+  // backward sweep runs over them without recomputing them.
+  const int keep0 = (ncp - m) * K;
   int32_t sd = seed;
   for (int st = 0; st < nsteps; ++st) {
     if (st % K == 0) GA_CUDA(h, cudaMemcpyAsync(cp[st / K], z, fb, cudaMemcpyDeviceToDevice, s));
     seeds[st] = sd;
-    if (st >= last0) {
-      const int r = st - last0;
+    if (st >= keep0) {
+      const int r = st - keep0;
       GA_CUDA(h, cudaMemcpyAsync(zs[r], z, fb, cudaMemcpyDeviceToDevice, s));
       rc = stage_a(h, z, ws[r], work.data(), pz[r]);
       if (!rc) rc = stage_b(h, ws[r], z, work.data(), pw[r]);
@@ -795,7 +823,8 @@ int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed
   // backward sweep: per segment, recompute and store (z_s, w_s), then run the adjoint back
   for (int c = ncp - 1; c >= 0; --c) {
     const int s0 = c * K, s1 = (s0 + K < nsteps) ? s0 + K : nsteps;
-    const bool kept = (c == ncp - 1);  // stored by the forward sweep
+    const bool kept = c >= ncp - m;          // stored by the forward sweep
+    const int base = kept ? s0 - keep0 : 0;  // its first slot (recomputed segments: slot 0)
     if (!kept) GA_CUDA(h, cudaMemcpyAsync(zs[0], cp[c], fb, cudaMemcpyDeviceToDevice, s));
     for (int st = s0; st < s1 && !kept; ++st) {
       const int r = st - s0;
@@ -810,7 +839,7 @@ int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed
       }
     }
     for (int st = s1 - 1; st >= s0; --st) {
-      const int r = st - s0;
+      const int r = base + st - s0;
       rc = forcing_dot_dev(h, lam, (uint32_t)seeds[st], dots + st);
       // a recomputed segment's last stage B was not evaluated: its adjoint transforms w itself
       if (!rc) rc = adj_step(h, zs[r], ws[r], lam, work.data(), pz[r], (kept || st + 1 < s1) ? pw[r] : Phys());

@@ -51,6 +51,8 @@ bool handle_col_split(const gt_handle* h);
 bool handle_col_cluster(const gt_handle* h);
 // whether the pass kernels launch with programmatic dependent launch (setting, profiling off)
 bool handle_pdl(const gt_handle* h);
+// device memory gt_adj_gradient may hold for whole kept segments (gt_adj_set_memory)
+int64_t handle_adj_memory(const gt_handle* h);
 // Records msg as h's last error (h == NULL: the thread's create/no-handle error); returns code.
 int set_error(gt_handle* h, int code, const char* msg);
 

@@ -77,6 +77,7 @@ struct gt_handle {
   int* d_colcnt = nullptr;
   int col_split = 2;  // use them where the column variant allows (gt_set_col_split: 0, 1, 2)
   int pdl = 1;        // programmatic dependent launch of the pass kernels (gt_set_pdl)
+  int64_t adj_mem = 0;  // device memory for whole kept segments of gt_adj_gradient (gt_adj_set_memory)
   // diagnostics scratch
   double *d_part = nullptr, *d_rowsum = nullptr, *d_bins = nullptr, *d_fl = nullptr, *d_glob = nullptr;
   double* h_diag = nullptr;  // pinned: bins [nbin*4] + fl [nbin*2] + glob [6]
@@ -393,6 +394,7 @@ bool handle_col_split(const gt_handle* h) { return split_active(h); }
 bool handle_col_cluster(const gt_handle* h) { return h->col_split == 2; }
 // the per-launch timing events of the profiling mode sit between the kernels: no overlap there
 bool handle_pdl(const gt_handle* h) { return h->pdl && !h->prof; }
+int64_t handle_adj_memory(const gt_handle* h) { return h->adj_mem; }
 }  // namespace gt
 
 extern "C" {
@@ -1005,6 +1007,19 @@ int gt_set_pdl(gt_handle* h, int32_t on) {
 int gt_get_pdl(const gt_handle* h, int32_t* on) {
   if (!h || !on) return fail(nullptr, GT_ERR_ARG, "gt_get_pdl: null argument");
   *on = h->pdl;
+  return GT_OK;
+}
+
+int gt_adj_set_memory(gt_handle* h, int64_t bytes) {
+  if (!h) return fail(nullptr, GT_ERR_ARG, "gt_adj_set_memory: null handle");
+  if (bytes < 0) return fail(h, GT_ERR_ARG, "gt_adj_set_memory: negative budget");
+  h->adj_mem = bytes;
+  return GT_OK;
+}
+
+int gt_adj_get_memory(const gt_handle* h, int64_t* bytes) {
+  if (!h || !bytes) return fail(nullptr, GT_ERR_ARG, "gt_adj_get_memory: null argument");
+  *bytes = h->adj_mem;
   return GT_OK;
 }
 

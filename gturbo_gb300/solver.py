@@ -188,6 +188,18 @@ class Solver:
     def pdl(self, on: bool) -> None:
         self._check(self.lib.gt_set_pdl(self.h, int(bool(on))))
 
+    @property
+    def adj_memory(self) -> int:
+        """Device memory (bytes) the adjoint gradient may hold for whole kept segments
+        (gt_adj_get_memory; 0 = only its last segment)."""
+        a = ctypes.c_int64()
+        self._check(self.lib.gt_adj_get_memory(self.h, ctypes.byref(a)))
+        return int(a.value)
+
+    @adj_memory.setter
+    def adj_memory(self, nbytes: int) -> None:
+        self._check(self.lib.gt_adj_set_memory(self.h, int(nbytes)))
+
     def supported_variants(self) -> list[int]:
         return [v for v in range(self.NVARIANTS) if self.lib.gt_variant_supported(self.n, v)]
 

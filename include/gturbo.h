@@ -222,6 +222,16 @@ int gt_adj_step_rk2(gt_handle* h, const double* z, const double* w, double* lam,
 int gt_adj_gradient(gt_handle* h, const double* z0, int32_t nsteps, int32_t seed, int32_t K,
                     double kmin, double kmax, double* J, double* grad_z0, double* grad_famp,
                     double* zT, double* times_ms);
+/* Memory of gt_adj_gradient's kept segments. The forward sweep always keeps its
+ * last segment whole (the stage states and the physical u+iv and q of every
+ * stage evaluation: RK2 2 fields + 48 N^2 bytes per step, RK4 4 fields +
+ * 96 N^2 bytes), which is the storage the backward sweep needs to recompute a
+ * segment anyway. With `bytes` > 0 it keeps as many of its last segments whole
+ * as fit in `bytes` (at least one), and the backward sweep recomputes only the
+ * earlier ones from their checkpoints: memory against recomputation. Default 0
+ * (one segment). No counterpart in the reference. */
+int gt_adj_set_memory(gt_handle* h, int64_t bytes);
+int gt_adj_get_memory(const gt_handle* h, int64_t* bytes);
 /* Tangent-linear run: J and its derivative dJ along (dz0, dfamp) after nsteps
  * of the handle's integrator (RK2 or RK4) + kick. */
 int gt_tlm_run(gt_handle* h, const double* z0, const double* dz0, double dfamp, int32_t nsteps,

@@ -292,3 +292,57 @@ def test_rk4_dot_product_adjoint_vs_tlm(k):
         adj = float((gz * dz).sum().item()) + gf * dfamp
         assert J2 == pytest.approx(J, rel=1e-14)
         assert adj == pytest.approx(dJ, rel=1e-11, abs=1e-14 * abs(J))
+
+
+@pytest.mark.parametrize("rko", [2, 4])
+def test_gradient_with_kept_segments_matches_recomputation(rko):
+    """gt_adj_set_memory: keeping more whole segments (less recomputation) changes only where the
+    adjoint reads the stage states and physical fields from, not the gradient."""
+    from gturbo_gb300.adjoint import gradient
+    p, sol, z0, ns = _setup(n=128, nsteps=12)
+    if rko == 4:
+        from gturbo_gb300.solver import Solver
+        sol = Solver(p.replace(rko=4))
+    J0, g0, f0, _, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=4, memory=0)
+    for mem in (1, 10 ** 7, 1 << 40):  # one segment, two of three, everything (capped by free memory)
+        J, g, f, _, _ = gradient(sol, z0, ns, SEED, KMIN, KMAX, checkpoint=4, memory=mem)
+        assert J == J0
+        assert float((g - g0).norm() / g0.norm()) < 1e-13
+        assert f == pytest.approx(f0, rel=1e-12)
+    sol.adj_memory = 0
+    assert sol.adj_memory == 0
+
+
+def test_c5_configuration_fd_tlm_and_dot_product():
+    """The gradient workload at its own configuration: 1024^2, alpha=1, Lawson RK2, 200 steps with
+    the LCG kick, checkpoint every 20, J = energy in 4 <= |k| <= 8. Along 8 random directions of
+    the initial field and along the forcing amplitude, FP64 central differences (h = 1e-6) agree
+    with the tangent-linear run to 1e-6, and the adjoint gradient's directional derivatives equal
+    the tangent's (dot-product test)."""
+    from gturbo_gb300.adjoint import forward_objective, gradient, tlm_run
+    from gturbo_gb300.ic import random_phase_ic
+    from gturbo_gb300.params import IC_K0, config
+    from gturbo_gb300.solver import Solver
+
+    p = config("c5")
+    nsteps, K, h = 200, 20, 1e-6
+    sol = Solver(p)
+    z0 = torch.from_numpy(random_phase_ic(p, IC_K0["c5"], 0.5, seed=1)).cuda()
+    J, gz, gf, _, _ = gradient(sol, z0, nsteps, SEED, KMIN, KMAX, checkpoint=K)
+    assert J == pytest.approx(forward_objective(sol, z0, nsteps, SEED, KMIN, KMAX), rel=1e-14)
+    for d in range(8):
+        dz = _direction(z0, 500 + d, truncated_only=(d % 2 == 1))
+        J2, dJ = tlm_run(sol, z0, dz, 0.0, nsteps, SEED, KMIN, KMAX)
+        assert J2 == pytest.approx(J, rel=1e-14)
+        adj = float((gz * dz).sum().item())
+        assert adj == pytest.approx(dJ, rel=1e-11, abs=1e-14 * abs(J)), d
+        fd = (forward_objective(sol, z0 + h * dz, nsteps, SEED, KMIN, KMAX)
+              - forward_objective(sol, z0 - h * dz, nsteps, SEED, KMIN, KMAX)) / (2 * h)
+        assert fd == pytest.approx(dJ, rel=1e-6), d
+    # the forcing-amplitude direction
+    _, dJf = tlm_run(sol, z0, torch.zeros_like(z0), 1.0, nsteps, SEED, KMIN, KMAX)
+    assert gf == pytest.approx(dJf, rel=1e-11)
+    hf = h * p.famp
+    fd = (forward_objective(Solver(p.replace(famp=p.famp + hf)), z0, nsteps, SEED, KMIN, KMAX)
+          - forward_objective(Solver(p.replace(famp=p.famp - hf)), z0, nsteps, SEED, KMIN, KMAX)) / (2 * hf)
+    assert fd == pytest.approx(dJf, rel=1e-6)
