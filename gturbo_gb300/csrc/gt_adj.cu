@@ -198,6 +198,7 @@ int check_adj_size(gt_handle* h) {
   if (!h) return afail(nullptr, GT_ERR_ARG, "null handle");
   const gt_params* p = gt::handle_params(h);
   if (p->n > GT_ADJ_MAX_N) return afail(h, GT_ERR_ARG, "adjoint / tangent-linear: n must be <= GT_ADJ_MAX_N (4096)");
+  if (p->ny != p->n) return afail(h, GT_ERR_ARG, "adjoint / tangent-linear: square grids only");
   return GT_OK;
 }
 
@@ -218,6 +219,11 @@ gt::GtOp op_of(const gt_handle* h, int kind) {
   op.stream = gt::handle_stream(h);
   op.pdl = gt::handle_pdl(h);
   op.cluster = gt::handle_col_cluster(h);
+  const gt::NltArgs base = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, nullptr);
+  op.tw = base.tw;
+  op.twr = base.twr;
+  op.nh = base.nh;
+  op.nrows = gt::handle_params(h)->ny;
   return op;
 }
 
@@ -665,6 +671,8 @@ extern "C" {
 
 int gt_objective(gt_handle* h, const double* z, double kmin, double kmax, double* J, double* grad) {
   if (!h || !z || !J) return afail(h, GT_ERR_ARG, "gt_objective: null argument");
+  if (gt::handle_params(h)->ny != gt::handle_params(h)->n)
+    return afail(h, GT_ERR_ARG, "gt_objective: square grids only");
   DevPool pool;
   const int n = gt::handle_params(h)->n;
   double* rows = pool.field(sizeof(double) * (n + 1));

@@ -244,9 +244,10 @@ int gt_ens_create(const gt_params* members, int32_t nmembers, const uint64_t* ke
   e->keys.assign(keys, keys + nmembers);
   const int rko0 = members[0].rko == 4 ? 4 : 2;
   for (int m = 0; m < nmembers; ++m) {
-    if (!valid_ens_n(members[m].n)) {
+    if (!valid_ens_n(members[m].n) || (members[m].ny != 0 && members[m].ny != members[m].n)) {
       delete e;
-      return efail(nullptr, GT_ERR_ARG, "gt_ens_create: member grid sizes must be powers of two in [128, 2048]");
+      return efail(nullptr, GT_ERR_ARG,
+                   "gt_ens_create: member grids must be square, sizes powers of two in [128, 2048]");
     }
     if ((members[m].rko == 4 ? 4 : 2) != rko0) {
       delete e;

@@ -54,6 +54,7 @@ struct EpiArgs {
   const int* fmap;
   int fwi, fwj, fh;
   const double2* kick;   // this step's per-mode increments (forcing_increment)
+  int ny;                // rows of the field (NY): the row index wrap of the forced window
 };
 
 // The kick of forced mode k: phase te = 2 pi rann of the (k+1)-th LCG draw from seed0
@@ -76,10 +77,10 @@ __device__ __forceinline__ double2 add_kick(double2 a, double2 inc, bool conj) {
   return make_double2(a.x + inc.x, conj ? a.y - inc.y : a.y + inc.y);
 }
 
-// The fused kick at (i, j) of an N x NH field, if (i, j) is forced.
+// The fused kick at (i, j) of an NY x NH field, if (i, j) is forced.
 __device__ __forceinline__ double2 fused_kick(const EpiArgs& E, int i, int j, int NH, double2 r) {
   if (i >= E.fwi) return r;
-  const int N = 2 * (NH - 1);
+  const int N = E.ny;
   int jj;
   if (j < E.fwj) jj = j;
   else if (j >= N - (E.fh - E.fwj)) jj = j - (N - E.fh);
@@ -248,7 +249,10 @@ struct NltArgs {
   const double* fkx;
   const double* fky;
   const int* kcut;       // largest kept |ky| per column
-  const double2* tw;     // exp(-2 pi i k / N)
+  const double2* tw;     // twiddle buffer of the column transforms (length NY)
+  const double2* twr;    // twiddle buffer of the row transforms (length NX; = tw when square)
+  int nh;                // columns NX/2+1 (the row stride of every field)
+  double cscale;         // 0.5 / (NX NY): pass C's normalisation of the packed product transforms
   int kxlim, kin, kout, truncate;
   int* flag;             // untruncated-input flag of this field
   EpiArgs epi;
@@ -262,11 +266,23 @@ struct NltArgs {
   int* colcnt;
 };
 
+// Columns of the field (NX/2+1) and pass C's normalisation 0.5/(NX NY): compile-time constants of
+// a square grid (RT = false), the values in the arguments for a non-square one (RT = true), whose
+// column kernels are separate instantiations so that the square grids' kernels keep their
+// constant strides (and their register counts).
+template <int N, bool RT>
+__device__ __forceinline__ int col_count(const NltArgs& a) { return RT ? a.nh : N / 2 + 1; }
+template <int N, bool RT>
+__device__ __forceinline__ double col_scale(const NltArgs& a) {
+  return RT ? a.cscale : 0.5 / ((double)N * (double)N);
+}
+
 // Pass A: inverse y-transforms of u, v and q (in that order: zin may alias q, as the
 // reference destroys z, so q is re-read from zin before the q column is overwritten).
-template <int N, int C, int R = 16>
+template <int N, int C, int R = 16, bool RT = false>
 __device__ __forceinline__ void colinv_tile(const NltArgs& a, int tile) {
-  constexpr int T = N / R, NH = N / 2 + 1;
+  constexpr int T = N / R;
+  const int NH = col_count<N, RT>(a);
   extern __shared__ double2 smem[];
   const int c = threadIdx.x % C, t = threadIdx.x / C;
   const int i = tile * C + c;
@@ -397,7 +413,7 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
       sm_ = make_double2(b.x, -b.y);
       d = make_double2(-b.x, b.y);
     }
-    zs[padix(k)] = pack_c2r(sm_, d, __ldg(&a.tw[k]));
+    zs[padix(k)] = pack_c2r(sm_, d, __ldg(&a.twr[k]));
   }
   __syncthreads();
   // q: inverse length-M transform, R/2 values per thread; result back to zs
@@ -406,7 +422,7 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
 #pragma unroll
     for (int s = 0; s < R / 2; ++s) h[s] = zs[padix(t + s * T)];
     __syncthreads();
-    fft_regs<M, R / 2, true, 1>(h, zs, t, a.tw, 1);
+    fft_regs<M, R / 2, true, 1>(h, zs, t, a.twr, 1);
     __syncthreads();
 #pragma unroll
     for (int s = 0; s < R / 2; ++s) zs[padix(t + s * T)] = h[s];
@@ -420,7 +436,7 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
 #pragma unroll
   for (int s = 0; s < R; ++s) v[s] = cs[padix(t + s * T)];
   __syncthreads();
-  fft_regs<N, R, true, 1>(v, cs, t, a.tw, 0, 8 * kl < 3 * N);
+  fft_regs<N, R, true, 1>(v, cs, t, a.twr, 0, 8 * kl < 3 * N);
   __syncthreads();
   if (a.phys_uv) {
 #pragma unroll
@@ -434,7 +450,7 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
     const double q = (x & 1) ? zq.y : zq.x;
     v[s] = make_double2(v[s].x * q, v[s].y * q);
   }
-  fft_regs<N, R, false, 1>(v, cs, t, a.tw, 0);
+  fft_regs<N, R, false, 1>(v, cs, t, a.twr, 0);
   __syncthreads();
 #pragma unroll
   for (int s = 0; s < R; ++s) cs[padix(t + s * T)] = v[s];
@@ -455,9 +471,10 @@ __device__ __forceinline__ void row_tile(const NltArgs& a, int tile) {
 
 // Pass C: forward y-transforms of A and B, N = -i (kx A + ky B) / (2 N^2), the 2/3 mask
 // (row j of column i is kept iff min(j, N-j) <= kcut[i]) and the stage epilogue.
-template <int N, int C, int R = 16, bool KICK = false>
+template <int N, int C, int R = 16, bool KICK = false, bool RT = false>
 __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
-  constexpr int T = N / R, NH = N / 2 + 1;
+  constexpr int T = N / R;
+  const int NH = col_count<N, RT>(a);
   extern __shared__ double2 smem[];
   if (tile == 0 && threadIdx.x == 0) *a.flag = 0;  // pass B of this nlt is complete
   const int c = threadIdx.x % C, t = threadIdx.x / C;
@@ -474,7 +491,7 @@ __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
     double2* sm = smem + c;
     double2* af = a.u;
     const double2* bf = a.v;
-    const double scale = 0.5 / ((double)N * (double)N);
+    const double scale = col_scale<N, RT>(a);
     const double kxs = __ldg(&a.fkx[ic]) * scale;
     double2 v[R];
 #pragma unroll
@@ -511,11 +528,11 @@ __device__ __forceinline__ void colfwd_tile(const NltArgs& a, int tile) {
 // stage value written by the epilogue is re-read by the thread that wrote it. The two
 // evaluations use different untruncated-input flags (next.flag != cur.flag): pass C clears
 // cur.flag while pass A may raise next.flag.
-template <int N, int C, int R = 16>
+template <int N, int C, int R = 16, bool RT = false>
 __device__ __forceinline__ void colfwd_colinv_tile(const NltArgs& cur, const NltArgs& next, int tile) {
-  colfwd_tile<N, C, R>(cur, tile);
+  colfwd_tile<N, C, R, false, RT>(cur, tile);
   __syncthreads();
-  colinv_tile<N, C, R>(next, tile);
+  colinv_tile<N, C, R, RT>(next, tile);
 }
 
 // ---- grouped column tiles ------------------------------------------------------------------
@@ -667,7 +684,7 @@ __device__ __forceinline__ void row_grp_tile(const NltArgs& a, int tile) {
 #pragma unroll
   for (int s = 0; s < R; ++s) v[s] = buf[padix(t + s * T)];
   __syncthreads();
-  fft_regs<N, R, true, 1>(v, buf, t, a.tw, 0, 8 * kl < 3 * N);  // both groups
+  fft_regs<N, R, true, 1>(v, buf, t, a.twr, 0, 8 * kl < 3 * N);  // both groups
   // group 0 holds u + i v, group 1 holds q (real part) at x = t + s*T
   __syncthreads();
   if (g == 1) {
@@ -694,7 +711,7 @@ __device__ __forceinline__ void row_grp_tile(const NltArgs& a, int tile) {
     }
   }
   __syncthreads();  // every read of qs is done before group 1 reuses it as exchange buffer
-  fft_regs<N, R, false, 1>(v, buf, t, a.tw, 0);  // both groups; group 1's result is unused
+  fft_regs<N, R, false, 1>(v, buf, t, a.twr, 0);  // both groups; group 1's result is unused
   __syncthreads();
   if (g == 0) {
 #pragma unroll
@@ -727,9 +744,10 @@ __device__ __forceinline__ void colfwd_colinv_grp_tile(const NltArgs& cur, const
 
 // Pass A, field g of column i: unit = 3 i + g (g = 0: u, 1: v, 2: q). q must not alias zin: the
 // caller passes a q buffer of its own (the three units of a column run in different CTAs).
-template <int N, int R>
+template <int N, int R, bool RT = false>
 __device__ __forceinline__ void colinv_field_tile(const NltArgs& a, int unit) {
-  constexpr int T = N / R, NH = N / 2 + 1;
+  constexpr int T = N / R;
+  const int NH = col_count<N, RT>(a);
   extern __shared__ double2 smem[];
   const int i = unit / 3, g = unit % 3, t = threadIdx.x;
   double2 v[R];
@@ -780,23 +798,24 @@ __host__ __device__ inline int colfwd_split_units(int nh, int kxlim) { return 2 
 // by the caller) and fb = B, A = F(u q), B = F(v q) (ky's factor carries the scale for B):
 // N = -i (kx A + ky B), re = kx Im A + ky Im B, im = -(kx Re A + ky Re B); zero outside the 2/3
 // cut (kc) and at the mean; then the stage epilogue.
-template <int N, bool KICK>
+template <int N, bool KICK, bool RT = false>
 __device__ __forceinline__ void colfwd_store(const NltArgs& a, int i, int j, int kc, double scale, double2 fa,
                                              double2 fb) {
   const double kys = __ldg(&a.fky[j]) * scale;
   double2 nh = make_double2(fma(kys, fb.y, fa.y), -fma(kys, fb.x, fa.x));
   const int aj = min(j, N - j);
   if (aj > kc || (i == 0 && j == 0 && a.truncate)) nh = czero();
-  epilogue<KICK>(a.epi, i, j, N / 2 + 1, nh);
+  epilogue<KICK>(a.epi, i, j, col_count<N, RT>(a), nh);
 }
 
 // Pass C, unit 2 i + g (g = 0: A, 1: B) of column i <= kxlim: the forward transform of the
 // field, written back in place (kx*FA for A). The second of the column's two CTAs to finish
 // (a per-column counter, no waiting) reads the other field and runs the epilogue. Its
 // loads of the other CTA's column go through L2 (__ldcg) after that CTA's __threadfence.
-template <int N, int R, bool KICK>
+template <int N, int R, bool KICK, bool RT = false>
 __device__ __forceinline__ void colfwd_field_tile(const NltArgs& a, int unit) {
-  constexpr int T = N / R, NH = N / 2 + 1;
+  constexpr int T = N / R;
+  const int NH = col_count<N, RT>(a);
   extern __shared__ double2 smem[];
   __shared__ int last;
   const int t = threadIdx.x;
@@ -809,7 +828,7 @@ __device__ __forceinline__ void colfwd_field_tile(const NltArgs& a, int unit) {
     return;
   }
   const int i = unit >> 1, g = unit & 1;
-  const double scale = 0.5 / ((double)N * (double)N);
+  const double scale = col_scale<N, RT>(a);
   double2* own = g == 0 ? a.u : a.v;
   double2 v[R];
 #pragma unroll
@@ -834,7 +853,7 @@ __device__ __forceinline__ void colfwd_field_tile(const NltArgs& a, int unit) {
   for (int s = 0; s < R; ++s) {
     const int j = t + s * T;
     const double2 o = __ldcg(&other[(size_t)j * NH + i]);
-    colfwd_store<N, KICK>(a, i, j, kc, scale, g == 0 ? v[s] : o, g == 0 ? o : v[s]);
+    colfwd_store<N, KICK, RT>(a, i, j, kc, scale, g == 0 ? v[s] : o, g == 0 ? o : v[s]);
   }
 }
 
@@ -845,9 +864,10 @@ __device__ __forceinline__ void colfwd_field_tile(const NltArgs& a, int unit) {
 // shared memory. No global round trip and no per-column counter; the epilogue work is shared.
 // A second cluster barrier keeps each CTA's shared memory alive until the partner has read it.
 // Columns beyond the 2/3 cut: each CTA stores the zero-input epilogue of its half.
-template <int N, int R, bool KICK>
+template <int N, int R, bool KICK, bool RT = false>
 __device__ __forceinline__ void colfwd_cluster_tile(const NltArgs& a, int unit) {
-  constexpr int T = N / R, NH = N / 2 + 1, H = R / 2;
+  constexpr int T = N / R, H = R / 2;
+  const int NH = col_count<N, RT>(a);
   extern __shared__ double2 smem[];
   const int t = threadIdx.x;
   const int i = unit >> 1, g = unit & 1;
@@ -859,7 +879,7 @@ __device__ __forceinline__ void colfwd_cluster_tile(const NltArgs& a, int unit) 
   }
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
-  const double scale = 0.5 / ((double)N * (double)N);
+  const double scale = col_scale<N, RT>(a);
   const double2* own = g == 0 ? a.u : a.v;
   double2 v[R];
 #pragma unroll
@@ -883,7 +903,7 @@ __device__ __forceinline__ void colfwd_cluster_tile(const NltArgs& a, int unit) 
   for (int s = 0; s < H; ++s) {
     const int j = t + (g * H + s) * T;
     const double2 o = peer[j];
-    colfwd_store<N, KICK>(a, i, j, kc, scale, g == 0 ? v[g * H + s] : o, g == 0 ? o : v[g * H + s]);
+    colfwd_store<N, KICK, RT>(a, i, j, kc, scale, g == 0 ? v[g * H + s] : o, g == 0 ? o : v[g * H + s]);
   }
   cluster.sync();
 }
@@ -945,11 +965,12 @@ struct Var {
   static constexpr bool OK = V == 0 || (V == 1 && N <= 4096) || (V >= 2 && V <= 4 && N <= 1024);
 };
 
-template <int N, int V>
+// RT = true: the column count at run time (non-square grids; ungrouped variants only)
+template <int N, int V, bool RT = false>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colinv(NltArgs a) {
   pdl_enter();
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colinv_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
-  else if constexpr (Var<N, V>::OK) colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(a, blockIdx.x);
+  else if constexpr (Var<N, V>::OK) colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R, RT>(a, blockIdx.x);
 }
 // Without a CTA count ptxas keeps the 8-value row kernels at 76-80 registers (3 CTAs per SM);
 // an explicit count of 1 lets them grow to 164. GT_VROW_MINB sets a count for the 8-value rows
@@ -965,19 +986,19 @@ __global__ void GT_VROW_BOUNDS(N, V) k_nltv_row(NltArgs a) {
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) row_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
   else if constexpr (Var<N, V>::OK) row_tile<N, Var<N, V>::ROWS, Var<N, V>::R>(a, blockIdx.x);
 }
-template <int N, int V>
+template <int N, int V, bool RT = false>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd(NltArgs a) {
   pdl_enter();
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colfwd_grp_tile<N, Var<N, V>::R, true>(a, blockIdx.x);
-  else if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R, true>(a, blockIdx.x);
+  else if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R, true, RT>(a, blockIdx.x);
 }
-template <int N, int V>
+template <int N, int V, bool RT = false>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltArgs cur, NltArgs next) {
   pdl_enter();
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED)
     colfwd_colinv_grp_tile<N, Var<N, V>::R>(cur, next, blockIdx.x);
   else if constexpr (Var<N, V>::OK)
-    colfwd_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R>(cur, next, blockIdx.x);
+    colfwd_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R, RT>(cur, next, blockIdx.x);
 }
 
 // Field-split column kernels (variants with one column per CTA and no thread groups).
@@ -996,23 +1017,23 @@ struct SplitVar {
   static constexpr int MINB = V == 0 ? MinBlocks<N>::COL : min_blocks(GT_SPLIT_MINB, THREADS, GT_SPLIT_REGS);
   static constexpr size_t SMEM = (size_t)padded(N) * sizeof(double2);
 };
-template <int N, int V>
+template <int N, int V, bool RT = false>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_nlt_colinv_fs(NltArgs a) {
   pdl_enter();
-  if constexpr (SplitVar<N, V>::OK) colinv_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
+  if constexpr (SplitVar<N, V>::OK) colinv_field_tile<N, Var<N, V>::R, RT>(a, blockIdx.x);
 }
 // KICK: the final stage with the fused forcing kick
-template <int N, int V, bool KICK>
+template <int N, int V, bool KICK, bool RT = false>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_nlt_colfwd_fs(NltArgs a) {
   pdl_enter();
-  if constexpr (SplitVar<N, V>::OK) colfwd_field_tile<N, Var<N, V>::R, KICK>(a, blockIdx.x);
+  if constexpr (SplitVar<N, V>::OK) colfwd_field_tile<N, Var<N, V>::R, KICK, RT>(a, blockIdx.x);
 }
 // the same pass with the column's two CTAs as one cluster (grid 2 NH)
-template <int N, int V, bool KICK>
+template <int N, int V, bool KICK, bool RT = false>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB)
     k_nlt_colfwd_cl(NltArgs a) {
   pdl_enter();
-  if constexpr (SplitVar<N, V>::OK) colfwd_cluster_tile<N, Var<N, V>::R, KICK>(a, blockIdx.x);
+  if constexpr (SplitVar<N, V>::OK) colfwd_cluster_tile<N, Var<N, V>::R, KICK, RT>(a, blockIdx.x);
 }
 
 // ---- ensemble kernels: one launch per pass for every member ------------------------------
@@ -1040,11 +1061,12 @@ __host__ __device__ constexpr int ens_row_tiles(int n) { return n / (2048 / n); 
 // ---------------------------------------------------------------------------------------
 
 // y-transform of every column; forward results are multiplied by `scale`.
-template <int N, bool INV>
+template <int N, bool INV, bool RT = false>
 __global__ void __launch_bounds__(Shape<N>::COL_THREADS)
-k_col_fft(double2* z, const double2* __restrict__ tw, double scale) {
+k_col_fft(double2* z, const double2* __restrict__ tw, double scale, int nh) {
   using S = Shape<N>;
-  constexpr int T = S::T, C = S::COLS, NH = S::NH;
+  constexpr int T = S::T, C = S::COLS;
+  const int NH = RT ? nh : S::NH;
   extern __shared__ double2 smem[];
   const int c = threadIdx.x % C, t = threadIdx.x / C;
   const int i = blockIdx.x * C + c;

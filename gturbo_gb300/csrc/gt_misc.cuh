@@ -16,10 +16,10 @@ __global__ void k_trunc(double2* z, int n, int nh, const int* __restrict__ kcut)
   }
 }
 
-// produ (produ.f90:11-23)
-__global__ void k_produ(const double* __restrict__ z, double* u, double* v, int n) {
+// produ (produ.f90:11-23) on an n x ny field (rows of n + 2 doubles)
+__global__ void k_produ(const double* __restrict__ z, double* u, double* v, int n, int ny) {
   const int ns = n + 2;
-  const size_t total = (size_t)ns * n;
+  const size_t total = (size_t)ns * ny;
   for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < total;
        o += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(o % ns);
@@ -80,7 +80,7 @@ struct DiagArgs {
   const double* fkxs;
   const double* fkys;
   const double* kainv;  // 1/|k|^alpha table [n][nh] or null (then pow per mode)
-  int n, nh, nbin;
+  int n, nh, nbin;       // n: rows (NY); nh = NX/2+1 columns; nbin = NX/2
   int unit_k;           // 1: dkx = dky = 1 (box 2 pi), integer wavenumbers -> integer bins
   double dk, alpv;
   double nu, mu, alpnu, alpmu;
@@ -193,9 +193,9 @@ inline int diag_int_exponent(double a) {
   return (a >= 0.0 && a <= 64.0 && a == (double)(int)a) ? (int)a : -1;
 }
 
-// Dynamic shared memory of k_diag_bins and k_diag_suffix for grid size n.
-inline size_t diag_bins_smem(int n) { return (size_t)(n / 2 + 1) * sizeof(double4); }
-inline size_t diag_suffix_smem(int n) { return (size_t)(n / 2) * sizeof(double2); }
+// Dynamic shared memory of k_diag_bins (nh columns) and k_diag_suffix (nbin bins).
+inline size_t diag_bins_smem(int nh) { return (size_t)nh * sizeof(double4); }
+inline size_t diag_suffix_smem(int nbin) { return (size_t)nbin * sizeof(double2); }
 
 // out[b*4 + q] = sum over groups (in order); then spectra / dk and flux suffix sums.
 __global__ void k_diag_bins_final(DiagArgs D, double* out /* [nbin][4] */) {
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_suffix(const double* bins
 // The shell-sum kernel for D.n (bins per thread from nbin = n/2).
 inline void diag_launch_bins(const DiagArgs& D, cudaStream_t s) {
   const int ng = diag_groups(D.n);
-  const size_t smem = diag_bins_smem(D.n);
+  const size_t smem = diag_bins_smem(D.nh);
   const int mb = (D.nbin + kDiagThreads - 1) / kDiagThreads;
   if (mb <= 1) k_diag_bins<1><<<ng, kDiagThreads, smem, s>>>(D);
   else if (mb <= 2) k_diag_bins<2><<<ng, kDiagThreads, smem, s>>>(D);
@@ -245,9 +245,9 @@ inline void diag_launch_bins(const DiagArgs& D, cudaStream_t s) {
 inline cudaError_t diag_prepare() {
   cudaError_t e = cudaSuccess;
   const cudaFuncAttribute attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  if ((e = cudaFuncSetAttribute(k_diag_bins<8>, attr, (int)diag_bins_smem(4096)))) return e;
-  if ((e = cudaFuncSetAttribute(k_diag_bins<16>, attr, (int)diag_bins_smem(8192)))) return e;
-  return cudaFuncSetAttribute(k_diag_suffix, attr, (int)diag_suffix_smem(8192));
+  if ((e = cudaFuncSetAttribute(k_diag_bins<8>, attr, (int)diag_bins_smem(4096 / 2 + 1)))) return e;
+  if ((e = cudaFuncSetAttribute(k_diag_bins<16>, attr, (int)diag_bins_smem(8192 / 2 + 1)))) return e;
+  return cudaFuncSetAttribute(k_diag_suffix, attr, (int)diag_suffix_smem(8192 / 2));
 }
 
 // x^n for a small non-negative integer n by repeated squaring

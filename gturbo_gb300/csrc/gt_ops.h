@@ -47,8 +47,12 @@ struct GtOp {
   AdjArgs adj;
   double2* a;         // field of the standalone transforms
   float* f32;         // real(4) output of OP_ROW_C2R_F32
-  const double2* tw;
+  const double2* tw;  // twiddle buffer of the column transforms (length NY)
+  const double2* twr; // twiddle buffer of the row transforms (length NX)
   double scale;
+  int nh;             // columns of the field, NX/2+1: the grid of the column passes
+  int nrows;          // rows of the field, NY: the grid of the row passes
+  bool rt;            // non-square grid: the column kernels with the column count at run time
   bool pdl;           // launch the pass kernels with programmatic dependent launch
   bool cluster;       // OP_NLT_COLFWD_FS: the column's two CTAs as one cluster
 };
@@ -70,6 +74,17 @@ inline void launch_pass(bool pdl, cudaStream_t s, void (*k)(KArgs...), unsigned 
   cfg.attrs = &at;
   cfg.numAttrs = pdl ? 1 : 0;
   cudaLaunchKernelEx(&cfg, k, args...);
+}
+
+// CTAs of a column pass over nh columns, C per CTA, and of a row pass over nrows rows, ROWS per
+// CTA (the handle keeps nrows a multiple of ROWS).
+inline unsigned col_ctas(int nh, int cols) { return (unsigned)((nh + cols - 1) / cols); }
+inline unsigned row_ctas(int nrows, int rows) { return (unsigned)(nrows / rows); }
+// Row passes run in the instantiation of the row length NX, column passes in that of the column
+// length NY.
+inline bool is_row_op(int kind) {
+  return kind == OP_NLT_ROW || kind == OP_ROW_C2R || kind == OP_ROW_R2C || kind == OP_ROW_C2R_F32 ||
+         kind == OP_ROW_R2C_F32 || kind == OP_TLM_ROW || kind == OP_ADJ_ROW;
 }
 
 // Per-N entry points (defined in gt_inst_<N>.cu).

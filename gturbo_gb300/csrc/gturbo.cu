@@ -37,7 +37,9 @@ struct DevBuf {
 
 struct gt_handle {
   gt_params p;
-  int N = 0, NH = 0, NBIN = 0, split = 0, rko = 2, truncate = 1;
+  // N = NX (row length, x fastest), NY rows, NH = NX/2+1 columns of the spectral field
+  int N = 0, NY = 0, NH = 0, NBIN = 0, split = 0, rko = 2, truncate = 1;
+  bool rt = false;  // non-square: column kernels with the column count at run time (variants 1, 2)
   int kxlim = 0;
   double dkx = 0, dky = 0, dt2 = 0, dt3 = 0, dt6 = 0, sdt = 0;
   double fkxsmax = 0, fkysmax = 0, rtrunc2 = 0;
@@ -61,7 +63,8 @@ struct gt_handle {
   cudaStream_t stream = nullptr;
   std::string err;
   // device tables
-  double2* d_tw = nullptr;
+  double2* d_tw = nullptr;   // column transforms (length NY)
+  double2* d_twr = nullptr;  // row transforms (length NX); null for a square grid (d_tw serves)
   double* d_emk = nullptr;
   double* d_kainv = nullptr;
   double *d_fkx = nullptr, *d_fky = nullptr, *d_fkxs = nullptr, *d_fkys = nullptr;
@@ -81,7 +84,8 @@ struct gt_handle {
   // diagnostics scratch
   double *d_part = nullptr, *d_rowsum = nullptr, *d_bins = nullptr, *d_fl = nullptr, *d_glob = nullptr;
   double* h_diag = nullptr;  // pinned: bins [nbin*4] + fl [nbin*2] + glob [6]
-  cudaError_t (*dispatch)(const GtOp&) = nullptr;
+  cudaError_t (*dispatch)(const GtOp&) = nullptr;      // column passes: the NY instantiation
+  cudaError_t (*dispatch_row)(const GtOp&) = nullptr;  // row passes: the NX instantiation
   // launch timing (gt_profile)
   bool prof = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -104,6 +108,9 @@ NltArgs handle_nlt_args(const gt_handle* h, const double* zin, double* q, double
   a.fky = h->d_fky;
   a.kcut = h->d_kcut;
   a.tw = h->d_tw;
+  a.twr = h->d_twr ? h->d_twr : h->d_tw;
+  a.nh = h->NH;
+  a.cscale = 0.5 / ((double)h->N * (double)h->NY);
   a.truncate = h->truncate;
   a.kxlim = h->truncate ? h->kxlim : h->N / 2;
   a.kin = a.kxlim;
@@ -118,6 +125,7 @@ NltArgs handle_nlt_args(const gt_handle* h, const double* zin, double* q, double
   a.epi.dt2 = h->dt2;
   a.epi.dt3 = h->dt3;
   a.epi.dt6 = h->dt6;
+  a.epi.ny = h->NY;
   return a;
 }
 
@@ -137,7 +145,9 @@ ForcingView handle_forcing(const gt_handle* h) {
   return f;
 }
 
-cudaError_t handle_dispatch(const gt_handle* h, const GtOp& op) { return h->dispatch(op); }
+cudaError_t handle_dispatch(const gt_handle* h, const GtOp& op) {
+  return is_row_op(op.kind) ? h->dispatch_row(op) : h->dispatch(op);
+}
 
 cudaError_t forcing_amp(gt_handle* h, double* z, uint32_t seed0, double famp) {
   if (h->nf == 0) return cudaSuccess;
@@ -187,6 +197,19 @@ int cuda_fail(gt_handle* h, cudaError_t e, const char* what) {
   } while (0)
 
 bool pow2_in_range(int n) { return n >= 16 && n <= 8192 && (n & (n - 1)) == 0; }
+
+// A grid NX x NY: both powers of two in [16, 8192]; a non-square grid has both sides >= 32, so
+// that its row count is a multiple of every row pass's rows per CTA (at most 32).
+// Its columns (length NY) run the column variants 1 or 2, so NY <= 4096.
+bool grid_ok(int nx, int ny) {
+  return pow2_in_range(nx) && pow2_in_range(ny) && (nx == ny || (nx >= 32 && ny >= 32 && ny <= 4096));
+}
+
+// Column variant v exists for the handle's grid: for its column length, and, on a non-square grid,
+// among the variants whose column kernels take the column count at run time (1 and 2).
+bool col_variant_ok(const gt_handle* h, int v) {
+  return gt_variant_supported(h->NY, v) && (!h->rt || v == 1 || v == 2);
+}
 
 // The row variant that goes with column variant v in gt_set_variant: the same launch variant.
 int natural_row_variant(int v) { return v; }
@@ -281,7 +304,7 @@ cudaError_t prepare_for(int n) {
 }
 
 void free_device(gt_handle* h) {
-  void* ptrs[] = {h->d_tw, h->d_emk, h->d_kainv, h->d_fkx, h->d_fky, h->d_fkxs, h->d_fkys,
+  void* ptrs[] = {h->d_tw, h->d_twr, h->d_emk, h->d_kainv, h->d_fkx, h->d_fky, h->d_fkxs, h->d_fkys,
                   h->d_emkx, h->d_emky, h->d_kcut, h->d_jc, h->d_ikxf, h->d_ikyf, h->d_lcga,
                   h->d_lcgb, h->d_ff, h->d_flag, h->d_part, h->d_rowsum, h->d_bins, h->d_fl,
                   h->d_glob, h->d_fmap, h->d_qscr, h->d_colcnt, h->d_kick};
@@ -297,6 +320,10 @@ GtOp base_op(const gt_handle* h) {
   op.variant = h->variant;
   op.row_variant = h->row_variant;
   op.tw = h->d_tw;
+  op.twr = h->d_twr ? h->d_twr : h->d_tw;
+  op.nh = h->NH;
+  op.nrows = h->NY;
+  op.rt = h->rt;
   op.nlt = gt::handle_nlt_args(h, nullptr, nullptr, nullptr, nullptr, h->d_flag);
   op.pdl = gt::handle_pdl(h);
   op.cluster = h->col_split == 2;
@@ -335,7 +362,7 @@ int op_class(int kind) {
 
 int run(gt_handle* h, const GtOp& op) {
   const int pair = prof_begin(h, op_class(op.kind));
-  cudaError_t e = h->dispatch(op);
+  cudaError_t e = gt::handle_dispatch(h, op);
   prof_end(h, pair);
   if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
   return GT_OK;
@@ -344,7 +371,7 @@ int run(gt_handle* h, const GtOp& op) {
 // The field-split column passes run when the handle has their scratch (N <= 2048), the user
 // has not turned them off, and the column variant has one column per CTA without thread groups.
 bool split_active(const gt_handle* h) {
-  const bool one_col = (h->variant == 0 && h->N >= 1024) || h->variant == 1 || h->variant == 2;
+  const bool one_col = (h->variant == 0 && h->NY >= 1024) || h->variant == 1 || h->variant == 2;
   return h->col_split && h->d_qscr && one_col;
 }
 
@@ -402,23 +429,32 @@ extern "C" {
 int gt_create(const gt_params* p, gt_handle** out) {
   if (!p || !out) return fail(nullptr, GT_ERR_ARG, "gt_create: null argument");
   *out = nullptr;
-  if (!pow2_in_range(p->n))
-    return fail(nullptr, GT_ERR_ARG, "gt_create: n must be a power of two in [16, 8192]");
+  const int ny_in = p->ny > 0 ? p->ny : p->n;
+  if (p->ny < 0 || !grid_ok(p->n, ny_in))
+    return fail(nullptr, GT_ERR_ARG,
+                "gt_create: n (NX) and ny (NY) must each be a power of two in [16, 8192]; a non-square grid "
+                "has both >= 32 and ny <= 4096");
   if (!(p->xlx > 0.0) || !(p->xly > 0.0) || !(p->dt > 0.0))
     return fail(nullptr, GT_ERR_ARG, "gt_create: xlx, xly and dt must be positive");
   gt_handle* h = new (std::nothrow) gt_handle();
   if (!h) return fail(nullptr, GT_ERR_NOMEM, "gt_create: out of host memory");
   h->p = *p;
-  const int N = h->N = p->n;
+  h->p.ny = ny_in;
+  const int N = h->N = p->n;  // NX
+  const int NY = h->NY = ny_in;
   const int NH = h->NH = N / 2 + 1;
   h->NBIN = N / 2;
-  h->dispatch = dispatch_for(N);
+  h->rt = N != NY;
+  h->dispatch = dispatch_for(NY);
+  h->dispatch_row = dispatch_for(N);
   // The launch variants that timed fastest on GB300 for this grid size (RK2 and RK4 alike).
   // Columns: grouped with 4 values per thread up to 256^2, 4 values per thread at 512^2 and
   // 1024^2, 8 at 2048^2, 16 from 4096^2 up. Rows: grouped with 4 values per thread up to
   // 128^2, 4 values per thread at 256^2 and 512^2, 8 at 1024^2 and 2048^2, 16 from 4096^2 up.
   // gt_autotune re-times.
-  h->variant = N <= 256 ? 3 : N <= 1024 ? 2 : N == 2048 ? 1 : 0;
+  // (Columns follow the column length NY, rows the row length NX.)
+  h->variant = NY <= 256 ? 3 : NY <= 1024 ? 2 : NY == 2048 ? 1 : 0;
+  if (h->rt) h->variant = NY <= 1024 ? 2 : 1;
   h->row_variant = N <= 128 ? 3 : N <= 512 ? 2 : N <= 2048 ? 1 : 0;
   // inieuler.f90:22-36, 237-244
   int split = 0;
@@ -437,36 +473,36 @@ int gt_create(const gt_params* p, gt_handle** out) {
   h->dt2 = p->dt / 2.0;
   h->dt3 = p->dt / 3.0;
   h->dt6 = p->dt / 6.0;
-  // defk.f90:12-73
-  h->jc.resize(N);
+  // defk.f90:12-73 (x over NX/2+1 columns, y over NY rows)
+  h->jc.resize(NY);
   h->jc[0] = 0;
-  for (int j = 1; j < N; ++j) h->jc[j] = N - j;
+  for (int j = 1; j < NY; ++j) h->jc[j] = NY - j;
   h->dkx = 2.0 * 3.14159265358979323846 / p->xlx;
   h->dky = 2.0 * 3.14159265358979323846 / p->xly;
   h->fkx.resize(NH);
   h->fkxs.resize(NH);
-  h->fky.resize(N);
-  h->fkys.resize(N);
+  h->fky.resize(NY);
+  h->fkys.resize(NY);
   for (int i = 0; i < NH; ++i) h->fkx[i] = (double)i * h->dkx;
-  for (int j = 0; j <= N / 2; ++j) h->fky[j] = (double)j * h->dky;
-  for (int j = N / 2 + 1; j < N; ++j) h->fky[j] = (double)(j - N) * h->dky;
+  for (int j = 0; j <= NY / 2; ++j) h->fky[j] = (double)j * h->dky;
+  for (int j = NY / 2 + 1; j < NY; ++j) h->fky[j] = (double)(j - NY) * h->dky;
   for (int i = 0; i < NH; ++i) h->fkxs[i] = h->fkx[i] * h->fkx[i];
-  for (int j = 0; j < N; ++j) h->fkys[j] = h->fky[j] * h->fky[j];
-  h->emky.resize(N);
+  for (int j = 0; j < NY; ++j) h->fkys[j] = h->fky[j] * h->fky[j];
+  h->emky.resize(NY);
   h->emkx.resize(NH);
-  for (int j = 0; j < N; ++j)
+  for (int j = 0; j < NY; ++j)
     h->emky[j] = std::exp(-0.5 * p->dt * (p->nu * std::pow(h->fkys[j], p->alpnu) + p->mu));
   for (int i = 0; i < NH; ++i)
     h->emkx[i] = std::exp(-0.5 * p->dt * (p->nu * std::pow(h->fkxs[i], p->alpnu)));
   h->fkxsmax = h->fkxs[N / 2];
-  h->fkysmax = h->fkys[N / 2];
+  h->fkysmax = h->fkys[NY / 2];
   h->rtrunc2 = p->rtrunc * p->rtrunc;
   // truncation cut-off per column: largest |ky| row kept by trunc.f90:12-16 (monotone in |ky|)
   h->kcut.resize(NH);
   h->kxlim = -1;
   for (int i = 0; i < NH; ++i) {
     int a = 0;
-    while (a <= N / 2) {
+    while (a <= NY / 2) {
       const double k1 = h->fkys[a] / h->fkysmax;
       const double k2 = k1 + h->fkxs[i] / h->fkxsmax;
       if (k2 > h->rtrunc2) break;
@@ -482,7 +518,7 @@ int gt_create(const gt_params* p, gt_handle** out) {
     const int ihi = pass == 0 ? 0 : pass == 1 ? N / 2 - 1 : N / 2;
     for (int i = ilo; i <= ihi; ++i) {
       const int jlo = pass == 0 ? 1 : 0;
-      const int jhi = pass == 1 ? N - 1 : N / 2;
+      const int jhi = pass == 1 ? NY - 1 : NY / 2;
       for (int j = jlo; j <= jhi; ++j) {
         const double k2 = h->fkxs[i] + h->fkys[j];
         const double k2n = h->fkxs[i] / h->fkxsmax + h->fkys[j] / h->fkysmax;
@@ -513,16 +549,16 @@ int gt_create(const gt_params* p, gt_handle** out) {
   // map of the forced values for the fused kick: mode k at (ikx, iky), and its conjugate partner
   // (ikx, jc[iky]) on the kx = 0 and Nyquist columns (forcing.f90:21-31)
   if (h->nf > 0) {
-    auto aky = [&](int j) { return j <= N / 2 ? j : N - j; };
+    auto aky = [&](int j) { return j <= NY / 2 ? j : NY - j; };
     for (int k = 0; k < h->nf; ++k) {
       h->fwi = std::max(h->fwi, h->ikxf[k] + 1);
       h->fwj = std::max(h->fwj, aky(h->ikyf[k]) + 1);
     }
-    h->fh = std::min(N, 2 * h->fwj - 1);
+    h->fh = std::min(NY, 2 * h->fwj - 1);
     h->fmap.assign((size_t)h->fwi * h->fh, -1);
     h->fuse_ok = 1;
     auto put = [&](int i, int j, int e) {
-      const int jj = j < h->fwj ? j : j - (N - h->fh);
+      const int jj = j < h->fwj ? j : j - (NY - h->fh);
       int& slot = h->fmap[(size_t)i * h->fh + jj];
       if (slot >= 0) h->fuse_ok = 0;
       slot = e;
@@ -539,25 +575,28 @@ int gt_create(const gt_params* p, gt_handle** out) {
   cudaError_t e = cudaGetDevice(&h->device);
   if (e != cudaSuccess) rc = cuda_fail(h, e, "cudaGetDevice");
   if (!rc) {
-    e = prepare_for(N);
-    if (e == cudaSuccess && N >= 4096) e = gt::diag_prepare();
+    e = prepare_for(NY);
+    if (e == cudaSuccess && NY != N) e = prepare_for(N);
+    if (e == cudaSuccess && std::max(N, NY) >= 4096) e = gt::diag_prepare();
     if (e != cudaSuccess) rc = cuda_fail(h, e, "cudaFuncSetAttribute");
   }
-  std::vector<double2> tw;
-  make_twiddles(N, tw);
+  std::vector<double2> tw, twr;
+  make_twiddles(NY, tw);
+  if (NY != N) make_twiddles(N, twr);
   std::vector<double2> ff(h->nf > 0 ? h->nf : 1, make_double2(1.0, 1.0));
-  const size_t nc = (size_t)N * NH;
+  const size_t nc = (size_t)NY * NH;
   if (!rc) rc = upload(h, &h->d_tw, tw.data(), tw.size());
+  if (!rc && NY != N) rc = upload(h, &h->d_twr, twr.data(), twr.size());
   if (!rc) rc = upload<double>(h, &h->d_emk, nullptr, nc);
   if (!rc) rc = upload<double>(h, &h->d_kainv, nullptr, nc);
   if (!rc) rc = upload(h, &h->d_fkx, h->fkx.data(), NH);
-  if (!rc) rc = upload(h, &h->d_fky, h->fky.data(), N);
+  if (!rc) rc = upload(h, &h->d_fky, h->fky.data(), NY);
   if (!rc) rc = upload(h, &h->d_fkxs, h->fkxs.data(), NH);
-  if (!rc) rc = upload(h, &h->d_fkys, h->fkys.data(), N);
+  if (!rc) rc = upload(h, &h->d_fkys, h->fkys.data(), NY);
   if (!rc) rc = upload(h, &h->d_emkx, h->emkx.data(), NH);
-  if (!rc) rc = upload(h, &h->d_emky, h->emky.data(), N);
+  if (!rc) rc = upload(h, &h->d_emky, h->emky.data(), NY);
   if (!rc) rc = upload(h, &h->d_kcut, h->kcut.data(), NH);
-  if (!rc) rc = upload(h, &h->d_jc, h->jc.data(), N);
+  if (!rc) rc = upload(h, &h->d_jc, h->jc.data(), NY);
   if (!rc) rc = upload(h, &h->d_ikxf, h->ikxf.data(), h->nf);
   if (!rc) rc = upload(h, &h->d_ikyf, h->ikyf.data(), h->nf);
   if (!rc) rc = upload(h, &h->d_lcga, h->lcga.data(), h->nf);
@@ -565,16 +604,16 @@ int gt_create(const gt_params* p, gt_handle** out) {
   if (!rc) rc = upload(h, &h->d_ff, ff.data(), ff.size());
   if (!rc && h->nf > 0) rc = upload(h, &h->d_fmap, h->fmap.data(), h->fmap.size());
   if (!rc && h->nf > 0) rc = upload<double2>(h, &h->d_kick, nullptr, (size_t)h->nf);
-  if (!rc && N <= 2048) {
+  if (!rc && NY <= 2048) {  // the field-split column passes (column length up to 2048)
     const std::vector<int> zeros(NH, 0);
-    rc = upload<double2>(h, &h->d_qscr, nullptr, (size_t)N * NH);
+    rc = upload<double2>(h, &h->d_qscr, nullptr, (size_t)NY * NH);
     if (!rc) rc = upload(h, &h->d_colcnt, zeros.data(), NH);
   }
   const int zeros2[2] = {0, 0};  // untruncated-input flags of even / odd stages
   if (!rc) rc = upload(h, &h->d_flag, zeros2, 2);
-  const int ngroups = gt::diag_groups(N);
+  const int ngroups = gt::diag_groups(NY);
   if (!rc) rc = upload<double>(h, &h->d_part, nullptr, (size_t)ngroups * h->NBIN * 4);
-  if (!rc) rc = upload<double>(h, &h->d_rowsum, nullptr, (size_t)N * 6);
+  if (!rc) rc = upload<double>(h, &h->d_rowsum, nullptr, (size_t)NY * 6);
   if (!rc) rc = upload<double>(h, &h->d_bins, nullptr, (size_t)h->NBIN * 4);
   if (!rc) rc = upload<double>(h, &h->d_fl, nullptr, (size_t)h->NBIN * 2);
   if (!rc) rc = upload<double>(h, &h->d_glob, nullptr, 6);
@@ -583,7 +622,7 @@ int gt_create(const gt_params* p, gt_handle** out) {
     if (e != cudaSuccess) rc = cuda_fail(h, e, "cudaMallocHost");
   }
   if (!rc) {
-    gt::k_init_tables<<<1024, 256>>>(h->d_emk, h->d_kainv, h->d_fkxs, h->d_fkys, N, NH, p->nu,
+    gt::k_init_tables<<<1024, 256>>>(h->d_emk, h->d_kainv, h->d_fkxs, h->d_fkys, NY, NH, p->nu,
                                       p->alpnu, p->mu, p->alpmu, p->alpv, p->dt);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -621,13 +660,14 @@ int gt_get_info(const gt_handle* h, gt_info* info) {
   if (!h || !info) return GT_ERR_ARG;
   std::memset(info, 0, sizeof(*info));
   info->n = h->N;
+  info->ny = h->NY;
   info->nh = h->NH;
   info->nbin = h->NBIN;
   info->rko = h->rko;
   info->split = h->split;
   info->truncate = h->truncate;
   info->nf = h->nf;
-  info->field_doubles = (int64_t)(h->N + 2) * h->N;
+  info->field_doubles = (int64_t)(h->N + 2) * h->NY;
   info->dkx = h->dkx;
   info->dky = h->dky;
   info->inpz = h->inpz;
@@ -667,7 +707,7 @@ int gt_fft_dir(gt_handle* h, double* z) {
   int rc = run(h, op);
   if (rc) return rc;
   op.kind = gt::OP_COL_FWD;
-  op.scale = 1.0 / ((double)h->N * (double)h->N);
+  op.scale = 1.0 / ((double)h->N * (double)h->NY);
   return run(h, op);
 }
 
@@ -703,7 +743,7 @@ int gt_load_real4(gt_handle* h, const float* in, double* z) {
   int rc = run(h, op);
   if (rc) return rc;
   op.kind = gt::OP_COL_FWD;
-  op.scale = 1.0 / ((double)h->N * (double)h->N);
+  op.scale = 1.0 / ((double)h->N * (double)h->NY);
   rc = run(h, op);
   if (rc || !h->truncate) return rc;
   return gt_trunc(h, z);
@@ -711,14 +751,14 @@ int gt_load_real4(gt_handle* h, const float* in, double* z) {
 
 int gt_trunc(gt_handle* h, double* z) {
   if (!h || !z) return fail(h, GT_ERR_ARG, "gt_trunc: null argument");
-  gt::k_trunc<<<4 * 152, 256, 0, h->stream>>>(reinterpret_cast<double2*>(z), h->N, h->NH, h->d_kcut);
+  gt::k_trunc<<<4 * 152, 256, 0, h->stream>>>(reinterpret_cast<double2*>(z), h->NY, h->NH, h->d_kcut);
   GT_CUDA(h, cudaGetLastError());
   return GT_OK;
 }
 
 int gt_produ(gt_handle* h, const double* z, double* u, double* v) {
   if (!h || !z || !u || !v) return fail(h, GT_ERR_ARG, "gt_produ: null argument");
-  gt::k_produ<<<4 * 152, 256, 0, h->stream>>>(z, u, v, h->N);
+  gt::k_produ<<<4 * 152, 256, 0, h->stream>>>(z, u, v, h->N, h->NY);
   GT_CUDA(h, cudaGetLastError());
   return GT_OK;
 }
@@ -913,7 +953,7 @@ int gt_diag(gt_handle* h, const double* z, const double* znl, double* sp, double
   D.fkxs = h->d_fkxs;
   D.fkys = h->d_fkys;
   D.kainv = h->d_kainv;
-  D.n = h->N;
+  D.n = h->NY;  // rows
   D.nh = h->NH;
   D.nbin = h->NBIN;
   D.dk = h->dkx;
@@ -939,13 +979,13 @@ int gt_diag(gt_handle* h, const double* z, const double* znl, double* sp, double
     GT_CUDA(h, cudaGetLastError());
     GT_CUDA(h, cudaMemcpyAsync(hb, h->d_bins, sizeof(double) * nb * 4, cudaMemcpyDeviceToHost, h->stream));
     if (znl) {
-      gt::k_diag_suffix<<<1, gt::kDiagThreads, gt::diag_suffix_smem(h->N), h->stream>>>(h->d_bins, h->d_fl, nb);
+      gt::k_diag_suffix<<<1, gt::kDiagThreads, gt::diag_suffix_smem(nb), h->stream>>>(h->d_bins, h->d_fl, nb);
       GT_CUDA(h, cudaGetLastError());
       GT_CUDA(h, cudaMemcpyAsync(hf, h->d_fl, sizeof(double) * nb * 2, cudaMemcpyDeviceToHost, h->stream));
     }
   }
   if (glob) {
-    gt::k_diag_glob_rows<<<h->N, 256, 0, h->stream>>>(D);
+    gt::k_diag_glob_rows<<<h->NY, 256, 0, h->stream>>>(D);
     gt::k_diag_glob_final<<<1, 192, 0, h->stream>>>(D, h->d_glob);
     GT_CUDA(h, cudaGetLastError());
     GT_CUDA(h, cudaMemcpyAsync(hg, h->d_glob, sizeof(double) * 6, cudaMemcpyDeviceToHost, h->stream));
@@ -1048,9 +1088,10 @@ static_assert(GT_NROW_VARIANTS == GT_NVARIANTS, "row and column variants share t
 
 int gt_set_variants(gt_handle* h, int32_t col_variant, int32_t row_variant) {
   if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_variants: null handle");
-  if (!gt_variant_supported(h->N, col_variant) || !gt_row_variant_supported(h->N, row_variant))
+  if (!col_variant_ok(h, col_variant) || !gt_row_variant_supported(h->N, row_variant))
     return fail(h, GT_ERR_ARG, "gt_set_variants: variants (" + std::to_string(col_variant) + ", " +
-                                   std::to_string(row_variant) + ") do not exist for n=" + std::to_string(h->N));
+                                   std::to_string(row_variant) + ") do not exist for the " + std::to_string(h->N) +
+                                   " x " + std::to_string(h->NY) + " grid (columns of length NY, rows of NX)");
   h->variant = col_variant;
   h->row_variant = row_variant;
   return GT_OK;
@@ -1058,9 +1099,9 @@ int gt_set_variants(gt_handle* h, int32_t col_variant, int32_t row_variant) {
 
 int gt_set_variant(gt_handle* h, int32_t variant) {
   if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_variant: null handle");
-  if (!gt_variant_supported(h->N, variant))
-    return fail(h, GT_ERR_ARG, "gt_set_variant: variant " + std::to_string(variant) +
-                                   " does not exist for n=" + std::to_string(h->N));
+  if (!col_variant_ok(h, variant) || !gt_row_variant_supported(h->N, natural_row_variant(variant)))
+    return fail(h, GT_ERR_ARG, "gt_set_variant: variant " + std::to_string(variant) + " does not exist for the " +
+                                   std::to_string(h->N) + " x " + std::to_string(h->NY) + " grid");
   return gt_set_variants(h, variant, natural_row_variant(variant));
 }
 
@@ -1084,10 +1125,10 @@ int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best)
   int navail = 0;
   for (int v = 0; v < GT_NVARIANTS; ++v) {
     ms[v] = -1.0;
-    navail += gt_variant_supported(h->N, v);
+    navail += col_variant_ok(h, v) + gt_row_variant_supported(h->N, v);
   }
-  if (navail > 1) {
-    const size_t nd = (size_t)h->N * (size_t)(h->N + 2);
+  if (navail > 2) {
+    const size_t nd = (size_t)h->NY * (size_t)(h->N + 2);
     double* buf = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     const int saved_col = h->variant, saved_row = h->row_variant;
@@ -1119,18 +1160,21 @@ int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best)
       if (!rc && e != cudaSuccess) rc = cuda_fail(h, e, "gt_autotune: timing");
       return rc ? -1.0 : (double)t / steps;
     };
-    // stage 1: every column variant with the row tiles of its own register radix
+    // stage 1: every column variant with the row tiles of its own register radix (the handle's
+    // row variant where the row length has no such variant)
     int best_c = 0;
+    auto row_for = [&](int v) { return gt_row_variant_supported(h->N, natural_row_variant(v)) ? natural_row_variant(v)
+                                                                                             : saved_row; };
     for (int v = 0; v < GT_NVARIANTS && !rc; ++v) {
-      if (!gt_variant_supported(h->N, v)) continue;
-      ms[v] = time_pair(v, natural_row_variant(v));
+      if (!col_variant_ok(h, v)) continue;
+      ms[v] = time_pair(v, row_for(v));
       if (!rc && (ms[best_c] < 0.0 || ms[v] < ms[best_c])) best_c = v;
     }
     // stage 2: the row variants under the best column variant
-    int best_r = natural_row_variant(best_c);
+    int best_r = row_for(best_c);
     double best_ms = ms[best_c];
     for (int r = 0; r < GT_NROW_VARIANTS && !rc; ++r) {
-      if (r == natural_row_variant(best_c) || !gt_row_variant_supported(h->N, r)) continue;
+      if (r == best_r || !gt_row_variant_supported(h->N, r)) continue;
       const double t = time_pair(best_c, r);
       if (!rc && t < best_ms) {
         best_ms = t;
@@ -1237,6 +1281,7 @@ extern "C" int gt_diag_static(const gt_params* p, const double* z, const double*
     return fail(nullptr, GT_ERR_ARG,
                 "gt_diag_static: n must be a power of two in [16, GT_DIAG_STATIC_MAX_N=2048]");
   if ((fle || flz) && !znl) return fail(nullptr, GT_ERR_ARG, "gt_diag_static: fluxes need znl");
+  if (p->ny != 0 && p->ny != n) return fail(nullptr, GT_ERR_ARG, "gt_diag_static: square grids only (ny = 0 or n)");
   if (!(p->xlx > 0.0) || !(p->xly > 0.0))
     return fail(nullptr, GT_ERR_ARG, "gt_diag_static: xlx and xly must be positive");
   int dev = 0;
@@ -1290,7 +1335,7 @@ extern "C" int gt_diag_static(const gt_params* p, const double* z, const double*
   if (sp || sz || fle || flz) {
     gt::diag_launch_bins(D, s);
     gt::k_diag_bins_final<<<(nb + 127) / 128, 128, 0, s>>>(D, base + kOffBins);
-    if (znl) gt::k_diag_suffix<<<1, gt::kDiagThreads, gt::diag_suffix_smem(n), s>>>(base + kOffBins, base + kOffFl, nb);
+    if (znl) gt::k_diag_suffix<<<1, gt::kDiagThreads, gt::diag_suffix_smem(nb), s>>>(base + kOffBins, base + kOffFl, nb);
     k_static_scatter<<<(nb + 127) / 128, 128, 0, s>>>(base + kOffBins, base + kOffFl, sp, sz,
                                                        znl ? fle : nullptr, znl ? flz : nullptr, nb);
   }

@@ -5,7 +5,8 @@ The reference reads the same quantities in ``src/inieuler.f90:13-20``::
 
     xlx xly / nu alpnu mu alpmu alpv / dt rko / npas iout imix / rtrunc truncate / famp k1f k2f
 
-and takes the grid size NX=NY from the compile-time constant in ``src/modules.f90:4``.
+and takes the grid size NX, NY from the compile-time constants in ``src/modules.f90:4``
+(``n`` = NX; ``ny`` = NY, 0 for a square grid).
 """
 from __future__ import annotations
 
@@ -37,6 +38,8 @@ class GtParams(ctypes.Structure):
         ("famp", ctypes.c_double),
         ("k1f", ctypes.c_double),
         ("k2f", ctypes.c_double),
+        ("ny", ctypes.c_int32),
+        ("ny_pad_", ctypes.c_int32),
     ]
 
 
@@ -51,7 +54,7 @@ class GtInfo(ctypes.Structure):
         ("split", ctypes.c_int32),
         ("truncate", ctypes.c_int32),
         ("nf", ctypes.c_int32),
-        ("pad_", ctypes.c_int32),
+        ("ny", ctypes.c_int32),
         ("field_doubles", ctypes.c_int64),
         ("dkx", ctypes.c_double),
         ("dky", ctypes.c_double),
@@ -83,6 +86,7 @@ class Params:
     k1f: float = 10.0
     k2f: float = 12.0
     split: int = -1  # -1: derived as src/inieuler.f90:22-36
+    ny: int = 0  # NY (rows); 0: NY = NX = n
     # run control (src/inieuler.f90:17); not part of gt_params
     npas: int = 1000
     iout: int = 1000000
@@ -94,10 +98,24 @@ class Params:
             xlx=float(self.xlx), xly=float(self.xly), nu=float(self.nu), alpnu=float(self.alpnu),
             mu=float(self.mu), alpmu=float(self.alpmu), alpv=float(self.alpv), dt=float(self.dt),
             rtrunc=float(self.rtrunc), famp=float(self.famp), k1f=float(self.k1f), k2f=float(self.k2f),
+            ny=int(self.ny),
         )
 
     def replace(self, **kw) -> "Params":
         return dataclasses.replace(self, **kw)
+
+    @property
+    def nx(self) -> int:
+        return self.n
+
+    @property
+    def rows(self) -> int:
+        """NY, the number of rows of a field."""
+        return self.ny if self.ny else self.n
+
+    @property
+    def square(self) -> bool:
+        return self.rows == self.n
 
     @property
     def nh(self) -> int:
@@ -105,12 +123,17 @@ class Params:
 
     @property
     def field_doubles(self) -> int:
-        return (self.n + 2) * self.n
+        return (self.n + 2) * self.rows
+
+    @property
+    def field_shape(self) -> tuple[int, int]:
+        """(NY, NX + 2): the physical view real(8) z(NX+2, NY) of a field."""
+        return (self.rows, self.n + 2)
 
     @property
     def spectral_bytes(self) -> int:
-        """S = 16 * N * (N/2+1): one complex128 spectral field."""
-        return 16 * self.n * self.nh
+        """S = 16 * NY * (NX/2+1): one complex128 spectral field."""
+        return 16 * self.rows * self.nh
 
 
 _FORTRAN_REAL = re.compile(r"([0-9.+-]+)[dD]([+-]?[0-9]+)")

@@ -59,9 +59,8 @@ def _write_cache(path: str, table: dict) -> None:
 
 
 def spec(z: torch.Tensor) -> torch.Tensor:
-    """Complex (N, N/2+1) view of an (N, N+2) float64 field."""
-    n = z.shape[0]
-    return z.view(torch.complex128).view(n, n // 2 + 1)
+    """Complex (NY, NX/2+1) view of an (NY, NX+2) float64 field."""
+    return z.view(torch.complex128).view(z.shape[0], z.shape[1] // 2)
 
 
 class Solver:
@@ -71,7 +70,8 @@ class Solver:
                  stream: torch.cuda.Stream | None = None):
         self.lib = _lib.load()
         self.p = p
-        self.n = p.n
+        self.n = p.n  # NX
+        self.ny = p.rows  # NY
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else
                                    torch.device(device).index or 0)
         self._cp = p.to_ctypes()
@@ -105,7 +105,7 @@ class Solver:
             pass
 
     def field(self) -> torch.Tensor:
-        return torch.zeros((self.n, self.n + 2), dtype=torch.float64, device=self.device)
+        return torch.zeros((self.ny, self.n + 2), dtype=torch.float64, device=self.device)
 
     def work(self, count: int = 4) -> list[torch.Tensor]:
         return [self.field() for _ in range(count)]
@@ -113,8 +113,8 @@ class Solver:
     def _ptr(self, t: torch.Tensor) -> int:
         if t.dtype != torch.float64 or not t.is_cuda or not t.is_contiguous():
             raise ValueError("fields must be contiguous float64 CUDA tensors")
-        if t.numel() != (self.n + 2) * self.n:
-            raise ValueError(f"field has {t.numel()} values, expected (N+2)*N = {(self.n + 2) * self.n}")
+        if t.numel() != (self.n + 2) * self.ny:
+            raise ValueError(f"field has {t.numel()} values, expected (NX+2)*NY = {(self.n + 2) * self.ny}")
         return t.data_ptr()
 
     def forcing_modes(self):
@@ -201,7 +201,8 @@ class Solver:
         self._check(self.lib.gt_adj_set_memory(self.h, int(nbytes)))
 
     def supported_variants(self) -> list[int]:
-        return [v for v in range(self.NVARIANTS) if self.lib.gt_variant_supported(self.n, v)]
+        ok = [v for v in range(self.NVARIANTS) if self.lib.gt_variant_supported(self.ny, v)]
+        return ok if self.ny == self.n else [v for v in ok if v in (1, 2)]
 
     def supported_row_variants(self) -> list[int]:
         return [r for r in range(self.NVARIANTS) if self.lib.gt_row_variant_supported(self.n, r)]
@@ -219,7 +220,8 @@ class Solver:
             cache = _tune_cache_default()
         # the library's identity (size, mtime) is part of the key: a rebuilt library re-times
         st = os.stat(getattr(self.lib, "_gt_path", _lib.LIB_PATH))
-        key = (f"{torch.cuda.get_device_name(self.device)}|n={self.n}|rko={self.info.rko}"
+        key = (f"{torch.cuda.get_device_name(self.device)}|n={self.n}"
+               f"{'' if self.ny == self.n else 'x' + str(self.ny)}|rko={self.info.rko}"
                f"|lib={st.st_size}-{int(st.st_mtime)}")
         table = _read_cache(cache)
         hit = table.get(key)
@@ -254,7 +256,7 @@ class Solver:
         N x N float32 array (x fastest), inverse-transformed and converted on the device."""
         with torch.cuda.stream(self.stream):
             work = z.clone()
-            out = torch.empty((self.n, self.n), dtype=torch.float32, device=self.device)
+            out = torch.empty((self.ny, self.n), dtype=torch.float32, device=self.device)
         self._check(self.lib.gt_dump_real4(self.h, self._ptr(work), out.data_ptr()))
         with torch.cuda.stream(self.stream):
             host = out.cpu()
@@ -267,8 +269,8 @@ class Solver:
         with torch.cuda.stream(self.stream):
             wd = torch.as_tensor(np.ascontiguousarray(w, np.float32) if isinstance(w, np.ndarray) else w)
             wd = wd.to(self.device, torch.float32).contiguous()
-            if wd.shape != (self.n, self.n):
-                raise ValueError(f"dump must be {self.n} x {self.n} float32")
+            if wd.shape != (self.ny, self.n):
+                raise ValueError(f"dump must be {self.ny} x {self.n} float32 (NY rows of NX)")
             if z is None:
                 z = self.field()
         # wd was allocated on the solver's stream: its memory is not reused before the

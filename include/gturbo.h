@@ -9,11 +9,11 @@
  * (wavenumbers, integrating factor, forcing list, twiddles) and, up to N = 2048,
  * one spectral scratch field for the field-split column passes.
  *
- * Memory layout of a field (identical to the reference):
- *   spectral  complex(8) z(N/2+1, N)  -> C: double z[N][N/2+1][2], kx fastest
- *   physical  real(8)    z(N+2, N)    -> C: double z[N][N+2], x fastest,
- *                                        2 padding doubles per row
- * Both views are the same NS = (N+2)*N doubles (src/modules.f90:4-9).
+ * Memory layout of a field (identical to the reference), NX = n, NY = ny:
+ *   spectral  complex(8) z(NX/2+1, NY) -> C: double z[NY][NX/2+1][2], kx fastest
+ *   physical  real(8)    z(NX+2, NY)   -> C: double z[NY][NX+2], x fastest,
+ *                                         2 padding doubles per row
+ * Both views are the same NS = (NX+2)*NY doubles (src/modules.f90:4-9).
  *
  * Every function returns GT_OK (0) or a GT_ERR_* code; the message of the last
  * failure is returned by gt_last_error(h) (or gt_last_error(NULL) for a failed
@@ -43,9 +43,9 @@ extern "C" {
 #define GT_NFORC 2048
 
 /* Runtime parameters: the contents of params.dat (src/inieuler.f90:13-20)
- * plus the compile-time grid size NX=NY (src/modules.f90:4). */
+ * plus the compile-time grid size NX, NY (src/modules.f90:4). */
 typedef struct gt_params {
-  int32_t n;        /* NX = NY, a power of two in [16, 8192]                */
+  int32_t n;        /* NX (row length, x fastest), a power of two in [16, 8192] */
   int32_t rko;      /* Runge-Kutta order, 2 or 4 (anything else -> 2, as inieuler.f90:241-243) */
   int32_t truncate; /* 1 = 2/3-rule dealiasing (trunc), 0 = none           */
   int32_t split;    /* -1 = derive as inieuler.f90:22-36; 0/1 = force     */
@@ -56,16 +56,23 @@ typedef struct gt_params {
   double dt;        /* time step                                            */
   double rtrunc;    /* truncation radius as written in params.dat (unsquared) */
   double famp, k1f, k2f; /* forcing amplitude and shell k1f < |k| <= k2f     */
+  int32_t ny;       /* NY (rows), a power of two in [16, 8192]; 0 = NX (square).
+                     * A non-square grid has NX, NY >= 32. The reference declares NX
+                     * and NY separately (modules.f90:4) but plans its transforms as
+                     * NY x NY (main.f90:27,32); here every routine follows NX x NY.
+                     * The ensemble, the tangent-linear model, the adjoint and
+                     * gt_diag_static take square grids only.                     */
+  int32_t ny_pad_;
 } gt_params;
 
 /* Derived quantities of a handle (read-only). */
 typedef struct gt_info {
-  int32_t n, nh;        /* N and N/2+1                                       */
-  int32_t nbin;         /* NBIN = N/2 (src/modules.f90:9)                    */
+  int32_t n, nh;        /* NX and NX/2+1                                     */
+  int32_t nbin;         /* NBIN = NX/2 (src/modules.f90:9)                   */
   int32_t rko, split, truncate;
   int32_t nf;           /* number of forced modes (iniforcing)              */
-  int32_t pad_;
-  int64_t field_doubles;/* NS = (N+2)*N                                      */
+  int32_t ny;           /* NY                                                */
+  int64_t field_doubles;/* NS = (NX+2)*NY                                    */
   double dkx, dky;
   double inpz, inpe;    /* mean enstrophy / energy input (iniforcing.f90:28-29) */
   double fkxsmax, fkysmax, rtrunc2;

@@ -18,6 +18,7 @@ module gturbo_c
   type, bind(C) :: gt_params
     integer(c_int32_t) :: n, rko, truncate, split
     real(c_double) :: xlx, xly, nu, alpnu, mu, alpmu, alpv, dt, rtrunc, famp, k1f, k2f
+    integer(c_int32_t) :: ny, ny_pad_
   end type
 
   interface

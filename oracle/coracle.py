@@ -4,8 +4,8 @@ TEST INFRASTRUCTURE ONLY: imported by ``tests/``, the smoke check and the CPU-ba
 of ``bench.py``, where results are compared with it; it is never the thing measured for the
 GPU path.
 
-Fields are numpy float64 arrays of shape (N, N+2): the physical view ``real(8) z(N+2,N)``.
-``spec(a)`` gives the complex (N, N/2+1) view of the same memory (``complex(8) z(N/2+1,N)``).
+Fields are numpy float64 arrays of shape (NY, NX+2): the physical view ``real(8) z(NX+2,NY)``.
+``spec(a)`` gives the complex (NY, NX/2+1) view of the same memory (``complex(8) z(NX/2+1,NY)``).
 """
 from __future__ import annotations
 
@@ -73,9 +73,8 @@ def _dp(a):
 
 
 def spec(a: np.ndarray) -> np.ndarray:
-    """Complex (N, N/2+1) view of an (N, N+2) float64 field."""
-    n = a.shape[0]
-    return a.view(np.complex128).reshape(n, n // 2 + 1)
+    """Complex (NY, NX/2+1) view of an (NY, NX+2) float64 field."""
+    return a.view(np.complex128).reshape(a.shape[0], a.shape[1] // 2)
 
 
 def philox4x64_10(counter, key):
@@ -115,7 +114,8 @@ class Oracle:
         self.h = self.lib.or_create(ctypes.byref(self._cp), ctypes.byref(err))
         if not self.h:
             raise ValueError(f"or_create failed with status {err.value}")
-        self.n = p.n
+        self.n = p.n  # NX
+        self.ny = p.rows  # NY
         info = GtInfo()
         self.lib.or_info(self.h, ctypes.byref(info))
         self.info = info
@@ -132,7 +132,7 @@ class Oracle:
             pass
 
     def zeros(self) -> np.ndarray:
-        return np.zeros((self.n, self.n + 2), dtype=np.float64)
+        return np.zeros((self.ny, self.n + 2), dtype=np.float64)
 
     def forcing_modes(self):
         ik = np.zeros(2048, np.int32)
@@ -142,7 +142,7 @@ class Oracle:
         return ik[:nf].copy(), jk[:nf].copy()
 
     def emk(self) -> np.ndarray:
-        e = np.zeros((self.n, self.n // 2 + 1), np.float64)
+        e = np.zeros((self.ny, self.n // 2 + 1), np.float64)
         self.lib.or_tables(self.h, _dp(e), None, None)
         return e
 

@@ -64,7 +64,7 @@ typedef struct {
 
 typedef struct or_ctx {
   gt_params p;
-  int N, NH, NBIN, split, rko, truncate;
+  int N, NY, NH, NBIN, split, rko, truncate;  /* N = NX (row length), NY rows */
   double dkx, dky, dt2, dt3, dt6, sdt, fkxsmax, fkysmax, rtrunc2;
   double *fkx, *fky, *fkxs, *fkys;
   int* jc;
@@ -200,7 +200,7 @@ static void irfft_row(const or_ctx* c, double* r) {
 
 /* Complex FFT along y of every column kx of the spectral field, in place. */
 static void col_fft(const or_ctx* c, double* z, int sign) {
-  const int N = c->N, NH = c->NH;
+  const int N = c->NY, NH = c->NH;  /* column length NY */
   const int nblk = (NH + COLB - 1) / COLB;
 #pragma omp parallel
   {
@@ -238,11 +238,13 @@ void or_destroy(or_ctx* c);
 or_ctx* or_create(const gt_params* p, int* err) {
   *err = GT_ERR_ARG;
   int N = p->n;
+  const int NY = p->ny > 0 ? p->ny : N;
   if (N < 16 || N > 16384 || (N & (N - 1))) return NULL;
+  if (NY < 16 || NY > 16384 || (NY & (NY - 1))) return NULL;
   or_ctx* c = (or_ctx*)calloc(1, sizeof(or_ctx));
   if (!c) { *err = GT_ERR_NOMEM; return NULL; }
   c->p = *p;
-  c->N = N; c->NH = N / 2 + 1; c->NBIN = N / 2;
+  c->N = N; c->NY = NY; c->NH = N / 2 + 1; c->NBIN = N / 2;
   const int NH = c->NH;
 #ifdef _OPENMP
   c->nthreads = omp_get_max_threads();
@@ -265,32 +267,32 @@ or_ctx* or_create(const gt_params* p, int* err) {
 
   c->fkx = (double*)malloc(sizeof(double) * NH);
   c->fkxs = (double*)malloc(sizeof(double) * NH);
-  c->fky = (double*)malloc(sizeof(double) * N);
-  c->fkys = (double*)malloc(sizeof(double) * N);
-  c->jc = (int*)malloc(sizeof(int) * N);
-  c->emk = (double*)malloc(sizeof(double) * (size_t)NH * N);
+  c->fky = (double*)malloc(sizeof(double) * NY);
+  c->fkys = (double*)malloc(sizeof(double) * NY);
+  c->jc = (int*)malloc(sizeof(int) * NY);
+  c->emk = (double*)malloc(sizeof(double) * (size_t)NH * NY);
   c->emkx = (double*)malloc(sizeof(double) * NH);
-  c->emky = (double*)malloc(sizeof(double) * N);
+  c->emky = (double*)malloc(sizeof(double) * NY);
   c->wrow = (double*)malloc(sizeof(double) * 2 * (N / 2 + 1));
   if (!c->fkx || !c->fkxs || !c->fky || !c->fkys || !c->jc || !c->emk || !c->emkx ||
-      !c->emky || !c->wrow || plan_init(&c->col, N) || plan_init(&c->half, N / 2)) {
+      !c->emky || !c->wrow || plan_init(&c->col, NY) || plan_init(&c->half, N / 2)) {
     or_destroy(c);
     *err = GT_ERR_NOMEM;
     return NULL;
   }
   /* defk.f90:12-15 conjugate index (0-based) */
   c->jc[0] = 0;
-  for (int j = 1; j < N; j++) c->jc[j] = N - j;
+  for (int j = 1; j < NY; j++) c->jc[j] = NY - j;
   /* defk.f90:18-36 */
   c->dkx = 2.0 * 3.14159265358979323846 / p->xlx;
   c->dky = 2.0 * 3.14159265358979323846 / p->xly;
   for (int i = 0; i < NH; i++) c->fkx[i] = (double)i * c->dkx;
-  for (int j = 0; j <= N / 2; j++) c->fky[j] = (double)j * c->dky;
-  for (int j = N / 2 + 1; j < N; j++) c->fky[j] = (double)(j - N) * c->dky;
+  for (int j = 0; j <= NY / 2; j++) c->fky[j] = (double)j * c->dky;
+  for (int j = NY / 2 + 1; j < NY; j++) c->fky[j] = (double)(j - NY) * c->dky;
   for (int i = 0; i < NH; i++) c->fkxs[i] = c->fkx[i] * c->fkx[i];
-  for (int j = 0; j < N; j++) c->fkys[j] = c->fky[j] * c->fky[j];
+  for (int j = 0; j < NY; j++) c->fkys[j] = c->fky[j] * c->fky[j];
   /* defk.f90:43-50 */
-  for (int j = 0; j < N; j++)
+  for (int j = 0; j < NY; j++)
     for (int i = 0; i < NH; i++) {
       if (i == 0 && j == 0) { c->emk[0] = 0.0; continue; }
       double fk2 = c->fkxs[i] + c->fkys[j];
@@ -298,7 +300,7 @@ or_ctx* or_create(const gt_params* p, int* err) {
       c->emk[(size_t)j * NH + i] = exp(-0.5 * p->dt * scra);
     }
   /* defk.f90:58-68 */
-  for (int j = 0; j < N; j++) {
+  for (int j = 0; j < NY; j++) {
     double fk2 = c->fkys[j];
     double scra = p->nu * pow(fk2, p->alpnu) + p->mu;
     c->emky[j] = exp(-0.5 * p->dt * scra);
@@ -310,7 +312,7 @@ or_ctx* or_create(const gt_params* p, int* err) {
   }
   /* defk.f90:71-73 */
   c->fkxsmax = c->fkxs[N / 2];
-  c->fkysmax = c->fkys[N / 2];
+  c->fkysmax = c->fkys[NY / 2];
   c->rtrunc2 = p->rtrunc * p->rtrunc;
   /* twiddles of the row post-processing */
   for (int k = 0; k <= N / 2; k++) {
@@ -329,7 +331,7 @@ or_ctx* or_create(const gt_params* p, int* err) {
     else { ilo = N / 2; ihi = N / 2; }
     for (int i = ilo; i <= ihi; i++) {
       int jlo = (pass == 0) ? 1 : 0;
-      int jhi = (pass == 1) ? N - 1 : N / 2;
+      int jhi = (pass == 1) ? NY - 1 : NY / 2;
       for (int j = jlo; j <= jhi; j++) {
         double k2 = c->fkxs[i] + c->fkys[j];
         double k2n = c->fkxs[i] / c->fkxsmax + c->fkys[j] / c->fkysmax;
@@ -363,7 +365,8 @@ void or_info(const or_ctx* c, gt_info* info) {
   info->n = c->N; info->nh = c->NH; info->nbin = c->NBIN;
   info->rko = c->rko; info->split = c->split; info->truncate = c->truncate;
   info->nf = c->nf;
-  info->field_doubles = (int64_t)(c->N + 2) * c->N;
+  info->ny = c->NY;
+  info->field_doubles = (int64_t)(c->N + 2) * c->NY;
   info->dkx = c->dkx; info->dky = c->dky;
   info->inpz = c->inpz; info->inpe = c->inpe;
   info->fkxsmax = c->fkxsmax; info->fkysmax = c->fkysmax; info->rtrunc2 = c->rtrunc2;
@@ -375,37 +378,37 @@ int or_forcing_modes(const or_ctx* c, int32_t* ikxf, int32_t* ikyf) {
 }
 
 void or_tables(const or_ctx* c, double* emk, double* fkx, double* fky) {
-  if (emk) memcpy(emk, c->emk, sizeof(double) * (size_t)c->NH * c->N);
+  if (emk) memcpy(emk, c->emk, sizeof(double) * (size_t)c->NH * c->NY);
   if (fkx) memcpy(fkx, c->fkx, sizeof(double) * c->NH);
-  if (fky) memcpy(fky, c->fky, sizeof(double) * c->N);
+  if (fky) memcpy(fky, c->fky, sizeof(double) * c->NY);
 }
 
 /* fft_dir (src/fft_dir.f90:11-21): D2Z in place, then z(:,j)=z(:,j)/NY/NX. */
 void or_fft_dir(const or_ctx* c, double* z) {
-  const int N = c->N, NS = N + 2;
+  const int N = c->N, NY = c->NY, NS = N + 2;
 #pragma omp parallel for schedule(static)
-  for (int j = 0; j < N; j++) rfft_row(c, z + (size_t)j * NS);
+  for (int j = 0; j < NY; j++) rfft_row(c, z + (size_t)j * NS);
   col_fft(c, z, -1);
 #pragma omp parallel for schedule(static)
-  for (int j = 0; j < N; j++) {
+  for (int j = 0; j < NY; j++) {
     double* r = z + (size_t)j * NS;
-    for (int i = 0; i < NS; i++) r[i] = r[i] / (double)N / (double)N;
+    for (int i = 0; i < NS; i++) r[i] = r[i] / (double)NY / (double)N;
   }
 }
 
 /* fft_inv (src/fft_inv.f90:11-13): Z2D in place, unnormalised. */
 void or_fft_inv(const or_ctx* c, double* z) {
-  const int N = c->N, NS = N + 2;
+  const int N = c->N, NY = c->NY, NS = N + 2;
   col_fft(c, z, +1);
 #pragma omp parallel for schedule(static)
-  for (int j = 0; j < N; j++) irfft_row(c, z + (size_t)j * NS);
+  for (int j = 0; j < NY; j++) irfft_row(c, z + (size_t)j * NS);
 }
 
 /* trunc (src/trunc.f90:10-25) */
 void or_trunc(const or_ctx* c, double* z) {
-  const int N = c->N, NH = c->NH;
+  const int NY = c->NY, NH = c->NH;
 #pragma omp parallel for schedule(static)
-  for (int j = 0; j < N; j++) {
+  for (int j = 0; j < NY; j++) {
     double k1 = c->fkys[j] / c->fkysmax;
     for (int i = 0; i < NH; i++) {
       double k2 = k1 + c->fkxs[i] / c->fkxsmax;
@@ -420,9 +423,9 @@ void or_trunc(const or_ctx* c, double* z) {
 
 /* produ (src/produ.f90:11-23) */
 void or_produ(const or_ctx* c, const double* z, double* u, double* v) {
-  const int N = c->N, NS = N + 2;
+  const int N = c->N, NY = c->NY, NS = N + 2;
 #pragma omp parallel for schedule(static)
-  for (int j = 0; j < N; j++) {
+  for (int j = 0; j < NY; j++) {
     for (int i = 0; i < NS; i++) {
       size_t o = (size_t)j * NS + i;
       if (i < N) {
@@ -438,13 +441,13 @@ void or_produ(const or_ctx* c, const double* z, double* u, double* v) {
 
 /* nlt (src/nlt.f90:17-63) */
 void or_nlt(const or_ctx* c, double* z, double* u, double* v) {
-  const int N = c->N, NH = c->NH;
-  const size_t ns = (size_t)(N + 2) * N;
+  const int N = c->N, NY = c->NY, NH = c->NH;
+  const size_t ns = (size_t)(N + 2) * NY;
   memset(u, 0, sizeof(double) * ns);
   memset(v, 0, sizeof(double) * ns);
   const double ea = c->p.alpv / 2.0;
 #pragma omp parallel for schedule(static)
-  for (int j = 0; j < N; j++) {
+  for (int j = 0; j < NY; j++) {
     for (int i = 0; i < NH; i++) {
       if (i == 0 && j == 0) continue;
       double k2 = c->fkxs[i] + c->fkys[j];
@@ -465,7 +468,7 @@ void or_nlt(const or_ctx* c, double* z, double* u, double* v) {
   or_fft_dir(c, u);
   or_fft_dir(c, v);
 #pragma omp parallel for schedule(static)
-  for (int j = 0; j < N; j++) {
+  for (int j = 0; j < NY; j++) {
     for (int i = 0; i < NH; i++) {
       size_t o = 2 * ((size_t)j * NH + i);
       z[o] = +c->fkx[i] * u[o + 1] + c->fky[j] * v[o + 1];
@@ -481,12 +484,12 @@ static inline double emk_at(const or_ctx* c, int i, int j) {
 
 /* step (src/rkstep.f90:2-76) */
 void or_step(const or_ctx* c, double* z, double* znl, double* u, double* v) {
-  const int N = c->N, NH = c->NH;
-  const size_t ns = (size_t)(N + 2) * N;
+  const int N = c->N, NY = c->NY, NH = c->NH;
+  const size_t ns = (size_t)(N + 2) * NY;
   memcpy(znl, z, sizeof(double) * ns);
   or_nlt(c, znl, u, v);
 #pragma omp parallel for schedule(static)
-  for (int j = 0; j < N; j++)
+  for (int j = 0; j < NY; j++)
     for (int i = 0; i < NH; i++) {
       size_t o = 2 * ((size_t)j * NH + i);
       double e = emk_at(c, i, j);
@@ -497,7 +500,7 @@ void or_step(const or_ctx* c, double* z, double* znl, double* u, double* v) {
   or_nlt(c, znl, u, v);
   const double dt = c->p.dt;
 #pragma omp parallel for schedule(static)
-  for (int j = 0; j < N; j++)
+  for (int j = 0; j < NY; j++)
     for (int i = 0; i < NH; i++) {
       size_t o = 2 * ((size_t)j * NH + i);
       double e = emk_at(c, i, j);
@@ -509,9 +512,9 @@ void or_step(const or_ctx* c, double* z, double* znl, double* u, double* v) {
 
 /* step4 (src/rkstep.f90:82-131) */
 void or_step4(const or_ctx* c, double* z, double* znl, double* znew, double* u, double* v) {
-  const int N = c->N, NH = c->NH;
-  const size_t ns = (size_t)(N + 2) * N;
-  const size_t nc = (size_t)N * NH;
+  const int N = c->N, NY = c->NY, NH = c->NH;
+  const size_t ns = (size_t)(N + 2) * NY;
+  const size_t nc = (size_t)NY * NH;
   const double dt = c->p.dt, dt2 = c->dt2, dt3 = c->dt3, dt6 = c->dt6;
   memcpy(znl, z, sizeof(double) * ns);
   or_nlt(c, znl, u, v);
@@ -585,7 +588,7 @@ void or_forcing(const or_ctx* c, double* z, int32_t* seed) {
  * sp, sz, fle, flz: NBIN doubles; glob: {ee, zz, disz_nu, disz_mu, dise_nu, dise_mu}. */
 void or_diag(const or_ctx* c, const double* z, const double* znl, double* sp, double* sz,
              double* fle, double* flz, double* glob) {
-  const int N = c->N, NH = c->NH, NBIN = c->NBIN;
+  const int NY = c->NY, NH = c->NH, NBIN = c->NBIN;
   const double dk = c->dkx, alpv = c->p.alpv;
   const double nu = c->p.nu, mu = c->p.mu, alpnu = c->p.alpnu, alpmu = c->p.alpmu;
   double* spb = (double*)calloc(NBIN, sizeof(double));
@@ -593,7 +596,7 @@ void or_diag(const or_ctx* c, const double* z, const double* znl, double* sp, do
   double* flem = (double*)calloc(NBIN, sizeof(double));
   double* flzm = (double*)calloc(NBIN, sizeof(double));
   double ee = 0, zz = 0, dnu = 0, dmu = 0, enu = 0, emu = 0;
-  for (int j = 0; j < N; j++) {
+  for (int j = 0; j < NY; j++) {
     for (int i = 0; i < NH; i++) {
       if (i == 0 && j == 0) continue;
       size_t o = 2 * ((size_t)j * NH + i);
@@ -654,7 +657,7 @@ void or_main_step(const or_ctx* c, double* z, double* znl, double* znew, double*
   if (c->rko == 4) or_step4(c, z, znl, znew, u, v);
   else or_step(c, z, znl, u, v);
   if (diag) {
-    memcpy(znl, z, sizeof(double) * (size_t)(c->N + 2) * c->N);
+    memcpy(znl, z, sizeof(double) * (size_t)(c->N + 2) * c->NY);
     or_nlt(c, znl, u, v);
     or_diag(c, z, znl, sp, sz, fle, flz, glob);
   }

@@ -20,6 +20,8 @@ PI_FORC = 3.14159265358979        # src/forcing.f90:10 (truncated in the referen
 
 class NpOracle:
     def __init__(self, p: Params):
+        if p.rows != p.n:
+            raise ValueError("the numpy restatement takes square grids only")
         self.p = p
         n = self.n = p.n
         nh = self.nh = n // 2 + 1

@@ -145,7 +145,7 @@ class Reference:
     def __init__(self, p, nx: int | None = None, ny: int | None = None, threads: int | None = None):
         self.p = p
         self.nx = nx or p.n
-        self.ny = ny or p.n
+        self.ny = ny or getattr(p, "rows", p.n)
         self.lib = _load(self.nx, self.ny)
         if threads:
             self.lib.f2c_set_threads(int(threads))

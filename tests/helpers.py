@@ -8,12 +8,12 @@ def rand_field(orc: Oracle, seed: int, truncate: bool = True, hermitian: bool = 
     """A random spectral field in the (N, N+2) layout, from the oracle's fft_dir of a real field."""
     n = orc.n
     rng = np.random.default_rng(seed)
-    a = np.zeros((n, n + 2))
-    a[:, :n] = rng.standard_normal((n, n))
+    a = orc.zeros()
+    a[:, :n] = rng.standard_normal((a.shape[0], n))
     orc.fft_dir(a)
     if not hermitian:
         s = spec(a)
-        s[:, 0] += 1e-3 * (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+        s[:, 0] += 1e-3 * (rng.standard_normal(a.shape[0]) + 1j * rng.standard_normal(a.shape[0]))
     if truncate:
         orc.trunc(a)
     return a
@@ -31,5 +31,5 @@ def rel_l2(a, b) -> float:
 
 
 def phys(a: np.ndarray) -> np.ndarray:
-    """The N x N physical values of an (N, N+2) field (padding dropped)."""
-    return a[:, : a.shape[0]]
+    """The NY x NX physical values of an (NY, NX+2) field (padding dropped)."""
+    return a[:, : a.shape[1] - 2]

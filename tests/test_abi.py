@@ -97,6 +97,22 @@ def test_create_rejects_bad_grid_size(lib):
     assert b"power of two" in lib.gt_last_error(None)
 
 
+def test_create_rejects_bad_non_square_grids(lib):
+    """A non-square grid has NX, NY >= 32 and NY <= 4096 (the column variants with the column
+    count at run time stop at 4096); every side a power of two."""
+    h = ctypes.c_void_p()
+    for n, ny in ((64, 16), (16, 64), (64, 8192), (64, 48), (64, -2)):
+        cp = Params(n=n, ny=ny).to_ctypes()
+        assert lib.gt_create(ctypes.byref(cp), ctypes.byref(h)) == 1, (n, ny)
+        assert b"power of two" in lib.gt_last_error(None)
+
+
+def test_params_struct_carries_ny():
+    assert Params(n=64, ny=32).field_shape == (32, 66)
+    assert Params(n=64).field_shape == (66 - 2, 66) and Params(n=64).rows == 64
+    assert Params(n=256, ny=1024).to_ctypes().ny == 1024
+
+
 def test_create_reports_nforc_overflow(lib):
     """More than NFORC=2048 forced modes: the reference stops with 'NFORC too small !'
     (src/iniforcing.f90:22); the C-ABI returns GT_ERR_NFORC before touching the device."""

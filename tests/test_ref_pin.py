@@ -40,6 +40,14 @@ CASES = [
     _p(256, alpv=2.0, rko=4, k1f=10.0, k2f=12.0, nu=1e-30, alpnu=8.0),
 ]
 IDS = ["n16a2rk4", "n32a1rk2", "n64a05rk4", "n64a3rk2_notrunc", "n128a1rk2_split", "n256a2rk4"]
+# non-square grids NX x NY (the reference declares NX and NY separately, modules.f90:4)
+CASES += [
+    _p(64, ny=32, alpv=1.0, rko=2),
+    _p(32, ny=64, alpv=2.0, rko=4),
+    _p(128, ny=64, alpv=0.5, rko=4, k1f=6.0, k2f=8.0),
+    _p(64, ny=256, alpv=2.0, rko=2, nu=1e-4, alpnu=1.0, mu=0.0, alpmu=0.0),  # split integrator
+]
+IDS += ["n64x32a1rk2", "n32x64a2rk4", "n128x64a05rk4", "n64x256a2rk2_split"]
 
 
 @needs_ref
@@ -81,7 +89,7 @@ def test_routines_against_reference(p):
     o.trunc(b)
     assert np.array_equal(a, b)
     rng = np.random.default_rng(3)
-    q, u, v = (rng.standard_normal((n, n + 2)) for _ in range(3))
+    q, u, v = (rng.standard_normal((p.rows, n + 2)) for _ in range(3))
     u1, v1, u2, v2 = u.copy(), v.copy(), u.copy(), v.copy()
     r.produ(q, u1, v1)
     o.produ(q, u2, v2)
@@ -94,7 +102,7 @@ def test_routines_against_reference(p):
         s2 = o.forcing(b, s2)
     assert s1 == s2 and np.array_equal(a, b)
     # the transforms and everything built on them: to rounding
-    x = rng.standard_normal((n, n))
+    x = rng.standard_normal((p.rows, n))
     a, b = r.zeros(), o.zeros()
     a[:, :n] = x
     b[:, :n] = x
@@ -128,7 +136,8 @@ def test_diagnostics_against_reference(p):
 
 
 @needs_ref
-@pytest.mark.parametrize("p", [CASES[1], CASES[2], CASES[4]], ids=[IDS[1], IDS[2], IDS[4]])
+@pytest.mark.parametrize("p", [CASES[1], CASES[2], CASES[4], CASES[6], CASES[9]],
+                         ids=[IDS[1], IDS[2], IDS[4], IDS[6], IDS[9]])
 def test_main_loop_horizon_against_reference(p):
     """30 iterations of src/main.f90:97-137 (step, diagnostics every 10, forcing) from the same
     field and seed: the state to 1e-12 and the spectra to 1e-9 (the specification's gates)."""
