@@ -97,6 +97,9 @@ def load(path: str | None = None):
         "gt_ens_get_step": ([P, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
         "gt_ens_use_graph": ([P, ctypes.c_int], ctypes.c_int),
         "gt_ens_step": ([P, ctypes.c_int32], ctypes.c_int),
+        "gt_ens_set_tile": ([P, ctypes.c_int32], ctypes.c_int),
+        "gt_ens_get_tile": ([P, I32P], ctypes.c_int),
+        "gt_ens_autotune": ([P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), I32P], ctypes.c_int),
         "gt_ens_last_error": ([P], ctypes.c_char_p),
         "gt_profile": ([P, ctypes.c_int], ctypes.c_int),
         "gt_profile_read": ([P, H, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),

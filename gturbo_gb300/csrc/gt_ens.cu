@@ -22,61 +22,76 @@
 
 namespace gt {
 
-__global__ void __launch_bounds__(kEnsThreads, kEnsMinBlocks)
+// Tile families of the ensemble passes: R complex values per thread and 2048 / R threads per CTA.
+// Every CTA holds 2048 values (C = 2048/N columns or rows of a size-N member) in every family, so
+// the work lists and the shared memory do not depend on the family; gt_ens_autotune times the
+// families on the ensemble's own members and keeps the fastest. MINB: CTAs per SM requested from
+// ptxas (3 for 256 threads caps a thread at 85 registers, as the 8-value tiles need).
+template <int R>
+struct EnsFam {
+  static constexpr int THREADS = 2048 / R;
+  static constexpr int MINB = R == 8 ? kEnsMinBlocks : R == 16 ? 3 : 2;
+};
+
+template <int R>
+__global__ void __launch_bounds__(EnsFam<R>::THREADS, EnsFam<R>::MINB)
 k_ens_colinv(const NltArgs* __restrict__ args, const EnsTile* __restrict__ tiles) {
   const EnsTile w = tiles[blockIdx.x];
   const NltArgs a = args[w.member];
   switch (a.n) {
-    case 128: colinv_tile<128, 16, 8>(a, w.tile); break;
-    case 256: colinv_tile<256, 8, 8>(a, w.tile); break;
-    case 512: colinv_tile<512, 4, 8>(a, w.tile); break;
-    case 1024: colinv_tile<1024, 2, 8>(a, w.tile); break;
-    case 2048: colinv_tile<2048, 1, 8>(a, w.tile); break;
+    case 128: colinv_tile<128, 16, R>(a, w.tile); break;
+    case 256: colinv_tile<256, 8, R>(a, w.tile); break;
+    case 512: colinv_tile<512, 4, R>(a, w.tile); break;
+    case 1024: colinv_tile<1024, 2, R>(a, w.tile); break;
+    case 2048: colinv_tile<2048, 1, R>(a, w.tile); break;
     default: break;
   }
 }
 
-__global__ void __launch_bounds__(kEnsThreads, kEnsMinBlocks)
+template <int R>
+__global__ void __launch_bounds__(EnsFam<R>::THREADS, EnsFam<R>::MINB)
 k_ens_row(const NltArgs* __restrict__ args, const EnsTile* __restrict__ tiles) {
   const EnsTile w = tiles[blockIdx.x];
   const NltArgs a = args[w.member];
   switch (a.n) {
-    case 128: row_tile<128, 16, 8>(a, w.tile); break;
-    case 256: row_tile<256, 8, 8>(a, w.tile); break;
-    case 512: row_tile<512, 4, 8>(a, w.tile); break;
-    case 1024: row_tile<1024, 2, 8>(a, w.tile); break;
-    case 2048: row_tile<2048, 1, 8>(a, w.tile); break;
+    case 128: row_tile<128, 16, R>(a, w.tile); break;
+    case 256: row_tile<256, 8, R>(a, w.tile); break;
+    case 512: row_tile<512, 4, R>(a, w.tile); break;
+    case 1024: row_tile<1024, 2, R>(a, w.tile); break;
+    case 2048: row_tile<2048, 1, R>(a, w.tile); break;
     default: break;
   }
 }
 
-__global__ void __launch_bounds__(kEnsThreads, kEnsMinBlocks)
+template <int R>
+__global__ void __launch_bounds__(EnsFam<R>::THREADS, EnsFam<R>::MINB)
 k_ens_colfwd(const NltArgs* __restrict__ args, const EnsTile* __restrict__ tiles) {
   const EnsTile w = tiles[blockIdx.x];
   const NltArgs a = args[w.member];
   switch (a.n) {
-    case 128: colfwd_tile<128, 16, 8>(a, w.tile); break;
-    case 256: colfwd_tile<256, 8, 8>(a, w.tile); break;
-    case 512: colfwd_tile<512, 4, 8>(a, w.tile); break;
-    case 1024: colfwd_tile<1024, 2, 8>(a, w.tile); break;
-    case 2048: colfwd_tile<2048, 1, 8>(a, w.tile); break;
+    case 128: colfwd_tile<128, 16, R>(a, w.tile); break;
+    case 256: colfwd_tile<256, 8, R>(a, w.tile); break;
+    case 512: colfwd_tile<512, 4, R>(a, w.tile); break;
+    case 1024: colfwd_tile<1024, 2, R>(a, w.tile); break;
+    case 2048: colfwd_tile<2048, 1, R>(a, w.tile); break;
     default: break;
   }
 }
 
 // pass C of stage cur[m] fused with pass A of stage next[m] (same tiles)
-__global__ void __launch_bounds__(kEnsThreads, kEnsMinBlocks)
+template <int R>
+__global__ void __launch_bounds__(EnsFam<R>::THREADS, EnsFam<R>::MINB)
 k_ens_colfwd_inv(const NltArgs* __restrict__ cur, const NltArgs* __restrict__ next,
                  const EnsTile* __restrict__ tiles) {
   const EnsTile w = tiles[blockIdx.x];
   const NltArgs a = cur[w.member];
   const NltArgs b = next[w.member];
   switch (a.n) {
-    case 128: colfwd_colinv_tile<128, 16, 8>(a, b, w.tile); break;
-    case 256: colfwd_colinv_tile<256, 8, 8>(a, b, w.tile); break;
-    case 512: colfwd_colinv_tile<512, 4, 8>(a, b, w.tile); break;
-    case 1024: colfwd_colinv_tile<1024, 2, 8>(a, b, w.tile); break;
-    case 2048: colfwd_colinv_tile<2048, 1, 8>(a, b, w.tile); break;
+    case 128: colfwd_colinv_tile<128, 16, R>(a, b, w.tile); break;
+    case 256: colfwd_colinv_tile<256, 8, R>(a, b, w.tile); break;
+    case 512: colfwd_colinv_tile<512, 4, R>(a, b, w.tile); break;
+    case 1024: colfwd_colinv_tile<1024, 2, R>(a, b, w.tile); break;
+    case 2048: colfwd_colinv_tile<2048, 1, R>(a, b, w.tile); break;
     default: break;
   }
 }
@@ -170,6 +185,7 @@ struct gt_ens {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   bool use_graph = true;
+  int tile_r = 8;  // values per thread of the pass kernels (tile family 16, 8 or 4)
   std::string err;
 };
 
@@ -211,17 +227,36 @@ void free_ens(gt_ens* e) {
 
 bool valid_ens_n(int n) { return n >= 128 && n <= 2048 && (n & (n - 1)) == 0; }
 
-int enqueue_step(gt_ens* e, cudaStream_t s) {
+// the passes of one step in tile family R
+template <int R>
+void enqueue_passes(gt_ens* e, cudaStream_t s) {
+  constexpr int TH = gt::EnsFam<R>::THREADS;
   // pass A of stage 0, then per stage: pass B, and pass C fused with the next stage's pass A
-  gt::k_ens_colinv<<<e->ncol, gt::kEnsThreads, gt::kEnsColSmem, s>>>(e->d_args, e->d_col);
+  gt::k_ens_colinv<R><<<e->ncol, TH, gt::kEnsColSmem, s>>>(e->d_args, e->d_col);
   for (int st = 0; st < e->stages; ++st) {
     const NltArgs* a = e->d_args + (size_t)st * e->nm;
-    gt::k_ens_row<<<e->nrow, gt::kEnsThreads, gt::kEnsRowSmem, s>>>(a, e->d_row);
+    gt::k_ens_row<R><<<e->nrow, TH, gt::kEnsRowSmem, s>>>(a, e->d_row);
     if (st + 1 < e->stages)
-      gt::k_ens_colfwd_inv<<<e->ncol, gt::kEnsThreads, gt::kEnsColSmem, s>>>(a, a + e->nm, e->d_col);
+      gt::k_ens_colfwd_inv<R><<<e->ncol, TH, gt::kEnsColSmem, s>>>(a, a + e->nm, e->d_col);
     else
-      gt::k_ens_colfwd<<<e->ncol, gt::kEnsThreads, gt::kEnsColSmem, s>>>(a, e->d_col);
+      gt::k_ens_colfwd<R><<<e->ncol, TH, gt::kEnsColSmem, s>>>(a, e->d_col);
   }
+}
+
+template <int R>
+cudaError_t prepare_family() {
+  const cudaFuncAttribute attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t c = cudaFuncSetAttribute(gt::k_ens_colinv<R>, attr, (int)gt::kEnsColSmem);
+  if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_colfwd<R>, attr, (int)gt::kEnsColSmem);
+  if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_colfwd_inv<R>, attr, (int)gt::kEnsColSmem);
+  if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_row<R>, attr, (int)gt::kEnsRowSmem);
+  return c;
+}
+
+int enqueue_step(gt_ens* e, cudaStream_t s) {
+  if (e->tile_r == 16) enqueue_passes<16>(e, s);
+  else if (e->tile_r == 4) enqueue_passes<4>(e, s);
+  else enqueue_passes<8>(e, s);
   if (e->nmodes > 0)
     gt::k_forcing_philox_ens<<<(e->nmodes + 127) / 128, 128, 0, s>>>(e->d_fm, e->d_modes, e->nmodes,
                                                                     e->d_step, e->d_done);
@@ -307,10 +342,9 @@ int gt_ens_create(const gt_params* members, int32_t nmembers, const uint64_t* ke
   up((void**)&e->d_fm, nullptr, sizeof(ForceMember) * nmembers);
   up((void**)&e->d_step, nullptr, sizeof(uint64_t));
   up((void**)&e->d_done, nullptr, sizeof(unsigned));
-  if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_colinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gt::kEnsColSmem);
-  if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_colfwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gt::kEnsColSmem);
-  if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_colfwd_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gt::kEnsColSmem);
-  if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_row, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gt::kEnsRowSmem);
+  if (c == cudaSuccess) c = prepare_family<16>();
+  if (c == cudaSuccess) c = prepare_family<8>();
+  if (c == cudaSuccess) c = prepare_family<4>();
   if (c == cudaSuccess) c = cudaStreamCreateWithFlags(&e->own, cudaStreamNonBlocking);
   if (c == cudaSuccess) c = cudaEventCreateWithFlags(&e->ev_in, cudaEventDisableTiming);
   if (c == cudaSuccess) c = cudaEventCreateWithFlags(&e->ev_out, cudaEventDisableTiming);
@@ -433,6 +467,83 @@ int gt_ens_step(gt_ens* e, int32_t nsteps) {
   }
   GE_CUDA(e, cudaEventRecord(e->ev_out, e->own));
   GE_CUDA(e, cudaStreamWaitEvent(e->user, e->ev_out, 0));
+  return GT_OK;
+}
+
+int gt_ens_set_tile(gt_ens* e, int32_t values_per_thread) {
+  if (!e) return efail(nullptr, GT_ERR_ARG, "gt_ens_set_tile: null ensemble");
+  if (values_per_thread != 16 && values_per_thread != 8 && values_per_thread != 4)
+    return efail(e, GT_ERR_ARG, "gt_ens_set_tile: values per thread must be 16, 8 or 4");
+  if (values_per_thread != e->tile_r) {
+    GE_CUDA(e, cudaStreamSynchronize(e->own));
+    drop_graph(e);  // the next step captures the new family
+    e->tile_r = values_per_thread;
+  }
+  return GT_OK;
+}
+
+int gt_ens_get_tile(const gt_ens* e, int32_t* values_per_thread) {
+  if (!e || !values_per_thread) return efail(nullptr, GT_ERR_ARG, "gt_ens_get_tile: null argument");
+  *values_per_thread = e->tile_r;
+  return GT_OK;
+}
+
+int gt_ens_autotune(gt_ens* e, int32_t steps, double* ms_per_step, int32_t* best) {
+  if (!e) return efail(nullptr, GT_ERR_ARG, "gt_ens_autotune: null ensemble");
+  if (!e->fields_set) return efail(e, GT_ERR_STATE, "gt_ens_autotune: call gt_ens_set_fields first");
+  if (steps < 1) return efail(e, GT_ERR_ARG, "gt_ens_autotune: steps must be >= 1");
+  static const int fam[3] = {16, 8, 4};
+  // the members' fields and the step counter are put back afterwards
+  std::vector<size_t> off(e->nm + 1, 0);
+  for (int m = 0; m < e->nm; ++m) {
+    const int n = e->params[m].n;
+    off[m + 1] = off[m] + sizeof(double) * (size_t)(n + 2) * n;
+  }
+  char* backup = nullptr;
+  GE_CUDA(e, cudaStreamSynchronize(e->user));
+  GE_CUDA(e, cudaMalloc((void**)&backup, off[e->nm]));
+  uint64_t step0 = 0;
+  int rc = GT_OK;
+  cudaError_t c = cudaMemcpy(&step0, e->d_step, sizeof(step0), cudaMemcpyDeviceToHost);
+  for (int m = 0; m < e->nm && c == cudaSuccess; ++m)
+    c = cudaMemcpy(backup + off[m], e->z[m], off[m + 1] - off[m], cudaMemcpyDeviceToDevice);
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  if (c == cudaSuccess) c = cudaEventCreate(&ev[0]);
+  if (c == cudaSuccess) c = cudaEventCreate(&ev[1]);
+  if (c != cudaSuccess) rc = ecuda(e, c, "gt_ens_autotune: set-up");
+  const int saved = e->tile_r;
+  double ms[3] = {-1.0, -1.0, -1.0};
+  int bi = -1;
+  for (int q = 0; q < 3 && !rc; ++q) {
+    rc = gt_ens_set_tile(e, fam[q]);
+    if (!rc) rc = gt_ens_step(e, 2);  // capture + warm-up
+    if (!rc) c = cudaEventRecord(ev[0], e->user);
+    if (!rc && c == cudaSuccess) rc = gt_ens_step(e, steps);
+    if (!rc && c == cudaSuccess) c = cudaEventRecord(ev[1], e->user);
+    if (!rc && c == cudaSuccess) c = cudaEventSynchronize(ev[1]);
+    float t = 0.0f;
+    if (!rc && c == cudaSuccess) c = cudaEventElapsedTime(&t, ev[0], ev[1]);
+    if (!rc && c != cudaSuccess) rc = ecuda(e, c, "gt_ens_autotune: timing");
+    if (!rc) {
+      ms[q] = (double)t / steps;
+      if (bi < 0 || ms[q] < ms[bi]) bi = q;
+    }
+  }
+  // restore the fields and the step counter whatever happened
+  cudaStreamSynchronize(e->own);
+  for (int m = 0; m < e->nm; ++m)
+    cudaMemcpy(e->z[m], backup + off[m], off[m + 1] - off[m], cudaMemcpyDeviceToDevice);
+  cudaMemcpy(e->d_step, &step0, sizeof(step0), cudaMemcpyHostToDevice);
+  cudaFree(backup);
+  for (cudaEvent_t x : ev)
+    if (x) cudaEventDestroy(x);
+  const int keep = rc ? saved : fam[bi];
+  const int rc2 = gt_ens_set_tile(e, keep);
+  if (rc) return rc;
+  if (rc2) return rc2;
+  if (ms_per_step)
+    for (int q = 0; q < 3; ++q) ms_per_step[q] = ms[q];
+  if (best) *best = keep;
   return GT_OK;
 }
 

@@ -1038,10 +1038,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(SplitVar<N, V>::THRE
 
 // ---- ensemble kernels: one launch per pass for every member ------------------------------
 // CTA b works on tile tiles[b] = (member, tile) of the member's field; members may differ in
-// size (N = 128 ... 2048), alpha, dt and tables. Every size uses 256-thread CTAs with 8 complex
-// values per thread (T = N/8 threads per column or row) and the same shared memory (C * N = 2048
-// column values, ROWS * N = 2048 row values), with at least 3 CTAs per SM (at most 85 registers
-// per thread).
+// size (N = 128 ... 2048), alpha, dt and tables. Every CTA holds 2048 values of one member (C * N =
+// 2048 column values, ROWS * N = 2048 row values) with the same shared memory; the tile family
+// (gt_ens.cu: R = 16, 8 or 4 values per thread, 2048 / R threads) is picked per ensemble. The
+// default family is 256-thread CTAs with 8 values per thread and at least 3 CTAs per SM (at most
+// 85 registers per thread).
 constexpr int kEnsThreads = 256;
 constexpr int kEnsMinBlocks = 3;
 constexpr size_t kEnsColSmem = (size_t)padded(2048) * sizeof(double2);

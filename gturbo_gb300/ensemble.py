@@ -96,6 +96,51 @@ class Ensemble:
     def step(self, nsteps: int = 1) -> None:
         self._check(self.lib.gt_ens_step(self.h, int(nsteps)))
 
+    TILES = (16, 8, 4)
+
+    @property
+    def tile(self) -> int:
+        """Values per thread of the pass kernels' tile family (16, 8 or 4; gt_ens_get_tile)."""
+        r = ctypes.c_int32()
+        self._check(self.lib.gt_ens_get_tile(self.h, ctypes.byref(r)))
+        return r.value
+
+    @tile.setter
+    def tile(self, values_per_thread: int) -> None:
+        self._check(self.lib.gt_ens_set_tile(self.h, int(values_per_thread)))
+
+    def autotune(self, steps: int = 10, cache: str | None = "default") -> dict:
+        """Pick the fastest tile family for these members (gt_ens_autotune: each family timed on
+        the members' own fields, which are restored afterwards) and cache the choice in the JSON
+        file of Solver.autotune, keyed by device, member sizes, RK order and library build.
+        Returns {"tile": R, "ms_per_step": {R: ms} or None, "cached": bool}."""
+        import collections
+        import os
+
+        from .solver import _read_cache, _tune_cache_default, _write_cache
+
+        if cache == "default":
+            cache = _tune_cache_default()
+        st = os.stat(getattr(self.lib, "_gt_path", _lib.LIB_PATH))
+        sizes = collections.Counter(m.params.n for m in self.members)
+        key = (f"{torch.cuda.get_device_name(self.device)}|ensemble|"
+               + ",".join(f"{c}x{n}" for n, c in sorted(sizes.items()))
+               + f"|rko={self.members[0].params.rko}|lib={st.st_size}-{int(st.st_mtime)}")
+        table = _read_cache(cache)
+        hit = table.get(key)
+        if hit and hit.get("tile") in self.TILES:
+            self.tile = hit["tile"]
+            return {"tile": hit["tile"], "ms_per_step": hit.get("ms_per_step"), "cached": True}
+        ms = (ctypes.c_double * 3)()
+        best = ctypes.c_int32()
+        self._check(self.lib.gt_ens_autotune(self.h, int(steps), ms, ctypes.byref(best)))
+        res = {"tile": best.value, "ms_per_step": {str(r): ms[q] for q, r in enumerate(self.TILES)}}
+        if cache:
+            table[key] = res
+            _write_cache(cache, table)
+        res["cached"] = False
+        return res
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.gt_ens_destroy(self.h)

@@ -188,6 +188,17 @@ int gt_ens_get_step(gt_ens* e, uint64_t* step);
 int gt_ens_use_graph(gt_ens* e, int enable);
 /* Advance every member by nsteps steps (asynchronous on the ensemble's stream). */
 int gt_ens_step(gt_ens* e, int32_t nsteps);
+/* Tile family of the ensemble's pass kernels: 16, 8 (default) or 4 complex values per thread,
+ * 128, 256 or 512 threads per CTA; every CTA holds 2048 values of one member, so the families
+ * differ only in the radix decomposition of the transforms (results agree to rounding). */
+int gt_ens_set_tile(gt_ens* e, int32_t values_per_thread);
+int gt_ens_get_tile(const gt_ens* e, int32_t* values_per_thread);
+/* Time `steps` steps of the ensemble in each tile family (16, 8, 4) on its own members and keep
+ * the fastest; the members' fields and the Philox step counter are restored afterwards.
+ * ms_per_step[3] (may be NULL): ms per step of the families 16, 8, 4; *best (may be NULL): the
+ * family kept. Needs gt_ens_set_fields; allocates a copy of the members' fields for the call.
+ * Synchronous. */
+int gt_ens_autotune(gt_ens* e, int32_t steps, double* ms_per_step, int32_t* best);
 const char* gt_ens_last_error(const gt_ens* e);
 
 /* ---- tangent-linear model and discrete adjoint (no counterpart in the reference) ----

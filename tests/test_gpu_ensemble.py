@@ -91,3 +91,53 @@ def test_ensemble_rejects_mixed_orders_and_sizes():
     bad = [Member(params=Params(n=64, rko=4), key=1, k0=2.0, ic_seed=1)]
     with pytest.raises(_lib.GturboError):
         Ensemble(bad)
+
+
+@pytest.mark.parametrize("tile", [16, 8, 4])
+def test_every_tile_family_matches_oracle(tile):
+    """The three tile families (16, 8, 4 values per thread; 128, 256, 512 threads per CTA) differ
+    only in the radix decomposition of the transforms: each matches the oracle."""
+    from gturbo_gb300.ensemble import Ensemble
+    members = _members(4)
+    ens = Ensemble(members)
+    ens.tile = tile
+    assert ens.tile == tile
+    ens.load_ic()
+    host = [z.cpu().numpy().copy() for z in ens.z]
+    ens.set_step(0)
+    ens.step(2)
+    torch.cuda.synchronize()
+    for m, z0, z in zip(members, host, ens.z):
+        orc = Oracle(m.params)
+        ref = z0.copy()
+        for s in range(2):
+            orc.rk_step(ref)
+            orc.forcing_philox(ref, m.key, s)
+        assert rel_l2(z.cpu().numpy(), ref) < 1e-12, (tile, m.params.n)
+    with pytest.raises(Exception):
+        ens.tile = 32
+
+
+def test_autotune_restores_members_and_caches(tmp_path):
+    """gt_ens_autotune times every family on the members' own fields and puts them back (with the
+    Philox step counter): stepping after the autotuner equals stepping without it."""
+    from gturbo_gb300.ensemble import Ensemble
+    members = _members(2)
+    a = Ensemble(members)
+    b = Ensemble(members)
+    for e in (a, b):
+        e.load_ic()
+        e.set_step(3)
+    cache = str(tmp_path / "tune.json")
+    res = a.autotune(steps=2, cache=cache)
+    assert res["tile"] in (16, 8, 4) and not res["cached"]
+    assert all(v > 0 for v in res["ms_per_step"].values())
+    assert a.tile == res["tile"] and a.get_step() == 3
+    b.tile = res["tile"]
+    a.step(2)
+    b.step(2)
+    torch.cuda.synchronize()
+    for x, y in zip(a.z, b.z):
+        assert torch.equal(x, y)
+    again = Ensemble(members).autotune(steps=2, cache=cache)
+    assert again["cached"] and again["tile"] == res["tile"]
