@@ -72,6 +72,8 @@ def load(path: str | None = None):
         "gt_get_col_split": ([P, I32P], ctypes.c_int),
         "gt_set_pdl": ([P, ctypes.c_int32], ctypes.c_int),
         "gt_get_pdl": ([P, I32P], ctypes.c_int),
+        "gt_set_graphs": ([P, ctypes.c_int32], ctypes.c_int),
+        "gt_get_graphs": ([P, I32P], ctypes.c_int),
         "gt_adj_set_memory": ([P, ctypes.c_int64], ctypes.c_int),
         "gt_adj_get_memory": ([P, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
         "gt_step_rk4_forced": ([P, D, D, D, D, D, I32P], ctypes.c_int),

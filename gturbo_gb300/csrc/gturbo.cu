@@ -81,6 +81,21 @@ struct gt_handle {
   int col_split = 2;  // use them where the column variant allows (gt_set_col_split: 0, 1, 2)
   int pdl = 1;        // programmatic dependent launch of the pass kernels (gt_set_pdl)
   int64_t adj_mem = 0;  // device memory for whole kept segments of gt_adj_gradient (gt_adj_set_memory)
+  // CUDA graphs of the steps (gt_set_graphs): a few captured steps, keyed by kind, fields and
+  // launch settings; the fused kick's LCG state is the only parameter that changes between calls
+  struct StepGraph {
+    int kind = 0;
+    const void* f[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int variant = 0, row_variant = 0, col_split = 0, pdl = 0;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t kick = nullptr;  // the k_kick_values node of a forced step
+    unsigned long long used = 0;
+  };
+  int graphs = 1;
+  bool graph_failed = false;  // a capture failed once: direct launches from then on
+  std::vector<StepGraph> sg;
+  unsigned long long sg_clock = 0;
+  cudaStream_t cap_stream = nullptr;
   // diagnostics scratch
   double *d_part = nullptr, *d_rowsum = nullptr, *d_bins = nullptr, *d_fl = nullptr, *d_glob = nullptr;
   double* h_diag = nullptr;  // pinned: bins [nbin*4] + fl [nbin*2] + glob [6]
@@ -638,9 +653,13 @@ int gt_create(const gt_params* p, gt_handle** out) {
   return GT_OK;
 }
 
+static void drop_step_graphs(gt_handle* h);
+
 int gt_destroy(gt_handle* h) {
   if (!h) return GT_OK;
   cudaDeviceSynchronize();
+  drop_step_graphs(h);
+  if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   for (cudaEvent_t ev : h->ev_pool) cudaEventDestroy(ev);
   if (h->kick_fork) cudaEventDestroy(h->kick_fork);
   if (h->kick_join) cudaEventDestroy(h->kick_join);
@@ -834,17 +853,14 @@ int stage_chain(gt_handle* h, int nst, const double* const* zin, double* znl, do
   return rc;
 }
 
-int gt_step_rk2(gt_handle* h, double* z, double* znl, double* u, double* v) {
-  if (!h || !z || !znl || !u || !v) return fail(h, GT_ERR_ARG, "gt_step_rk2: null argument");
+static int step_rk2_direct(gt_handle* h, double* z, double* znl, double* u, double* v) {
   const gt::EpiArgs epi[2] = {make_epi(h, gt::EPI_RK2A, znl, nullptr, z),
                               make_epi(h, gt::EPI_RK2B, z, nullptr, z)};
   const double* zin[2] = {z, znl};
   return stage_chain(h, 2, zin, znl, u, v, epi);
 }
 
-int gt_step_rk4(gt_handle* h, double* z, double* znl, double* znew, double* u, double* v) {
-  if (!h || !z || !znl || !znew || !u || !v) return fail(h, GT_ERR_ARG, "gt_step_rk4: null argument");
-  if (h->split) return fail(h, GT_ERR_ARG, "gt_step_rk4: the split integrator exists only for RK2");
+static int step_rk4_direct(gt_handle* h, double* z, double* znl, double* znew, double* u, double* v) {
   const gt::EpiArgs epi[4] = {make_epi(h, gt::EPI_RK4A, znl, znew, z), make_epi(h, gt::EPI_RK4B, znl, znew, z),
                               make_epi(h, gt::EPI_RK4C, znl, znew, z), make_epi(h, gt::EPI_RK4D, z, znew, nullptr)};
   const double* zin[4] = {z, znl, znl, znl};
@@ -855,15 +871,19 @@ int gt_step_rk4(gt_handle* h, double* z, double* znl, double* znew, double* u, d
 // computed on a side stream that forks from the handle's stream before the step, and the final
 // pass C waits for them (the returned event). The sincos of the phases thus stays off the
 // final pass's critical path.
+// the side stream and events of the fused kick, made once per handle (before any capture)
+static int ensure_kick_stream(gt_handle* h) {
+  if (h->kick_stream) return GT_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&h->kick_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->kick_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->kick_join, cudaEventDisableTiming);
+  return e == cudaSuccess ? GT_OK : cuda_fail(h, e, "fused kick: stream set-up");
+}
+
 static int start_fused_kick(gt_handle* h, gt::EpiArgs& E, uint32_t x0, cudaEvent_t* join) {
-  cudaError_t e = cudaSuccess;
-  if (!h->kick_stream) {
-    e = cudaStreamCreateWithFlags(&h->kick_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->kick_fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->kick_join, cudaEventDisableTiming);
-    if (e != cudaSuccess) return cuda_fail(h, e, "fused kick: stream set-up");
-  }
-  e = cudaEventRecord(h->kick_fork, h->stream);
+  int rc = ensure_kick_stream(h);
+  if (rc) return rc;
+  cudaError_t e = cudaEventRecord(h->kick_fork, h->stream);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(h->kick_stream, h->kick_fork, 0);
   if (e != cudaSuccess) return cuda_fail(h, e, "fused kick: fork");
   gt::k_kick_values<<<(h->nf + 127) / 128, 128, 0, h->kick_stream>>>(h->d_kick, h->nf, h->d_lcga, h->d_lcgb,
@@ -880,20 +900,204 @@ static int start_fused_kick(gt_handle* h, gt::EpiArgs& E, uint32_t x0, cudaEvent
   return GT_OK;
 }
 
+// RK2 step with the kick fused into its final stage, from LCG state x0 (nf > 0, fuse_ok)
+static int step_rk2_forced_direct(gt_handle* h, double* z, double* znl, double* u, double* v, uint32_t x0) {
+  gt::EpiArgs epi[2] = {make_epi(h, gt::EPI_RK2A, znl, nullptr, z),
+                        make_epi(h, gt::EPI_RK2B, z, nullptr, z)};
+  cudaEvent_t join = nullptr;
+  int rc = start_fused_kick(h, epi[1], x0, &join);
+  if (rc) return rc;
+  const double* zin[2] = {z, znl};
+  return stage_chain(h, 2, zin, znl, u, v, epi, join);
+}
+
+static int step_rk4_forced_direct(gt_handle* h, double* z, double* znl, double* znew, double* u, double* v,
+                                  uint32_t x0) {
+  gt::EpiArgs epi[4] = {make_epi(h, gt::EPI_RK4A, znl, znew, z), make_epi(h, gt::EPI_RK4B, znl, znew, z),
+                        make_epi(h, gt::EPI_RK4C, znl, znew, z), make_epi(h, gt::EPI_RK4D, z, znew, nullptr)};
+  cudaEvent_t join = nullptr;
+  int rc = start_fused_kick(h, epi[3], x0, &join);
+  if (rc) return rc;
+  const double* zin[4] = {z, znl, znl, znl};
+  return stage_chain(h, 4, zin, znl, u, v, epi, join);
+}
+
+// ---- steps as CUDA graphs ---------------------------------------------------------------
+// A step is a dozen short launches; on small grids the host's launch rate, not the GPU, sets
+// the step time (256^2 RK4: about 100 us of host time per step for about 50 us of kernels). Each
+// step kind is therefore captured once per (fields, launch settings) into a CUDA graph on a
+// capture stream of the handle and replayed on the handle's stream. The graph holds the same
+// launches with the same arguments, so its results are the direct launches' bit for bit. The
+// forced steps' kick increments depend on the LCG state of the call: the k_kick_values node's
+// parameters are rewritten before each replay.
+enum StepKind { SK_RK2 = 1, SK_RK4 = 2, SK_RK2F = 3, SK_RK4F = 4 };
+constexpr size_t kStepGraphs = 4;
+
+static int step_direct(gt_handle* h, int kind, double* const* f, uint32_t x0) {
+  switch (kind) {
+    case SK_RK2: return step_rk2_direct(h, f[0], f[1], f[3], f[4]);
+    case SK_RK4: return step_rk4_direct(h, f[0], f[1], f[2], f[3], f[4]);
+    case SK_RK2F: return step_rk2_forced_direct(h, f[0], f[1], f[3], f[4], x0);
+    default: return step_rk4_forced_direct(h, f[0], f[1], f[2], f[3], f[4], x0);
+  }
+}
+
+static void drop_step_graphs(gt_handle* h) {
+  for (auto& g : h->sg)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  h->sg.clear();
+}
+
+// the kick kernel's parameters for LCG state x0 (the k_kick_values launch of start_fused_kick)
+static cudaError_t set_kick_node(gt_handle* h, cudaGraphExec_t exec, cudaGraphNode_t node, uint32_t x0) {
+  double2* kick = h->d_kick;
+  int nf = h->nf;
+  const uint32_t* lcga = h->d_lcga;
+  const uint32_t* lcgb = h->d_lcgb;
+  const double2* ff = h->d_ff;
+  uint32_t seed0 = x0;
+  double sf = h->sdt * h->p.famp;
+  void* args[] = {&kick, &nf, &lcga, &lcgb, &ff, &seed0, &sf};
+  cudaKernelNodeParams kp = {};
+  kp.func = (void*)gt::k_kick_values;
+  kp.gridDim = dim3((unsigned)((h->nf + 127) / 128));
+  kp.blockDim = dim3(128);
+  kp.sharedMemBytes = 0;
+  kp.kernelParams = args;
+  kp.extra = nullptr;
+  return cudaGraphExecKernelNodeSetParams(exec, node, &kp);
+}
+
+// Captures one step of `kind` on the fields f; on success *out holds the instantiated graph.
+static int capture_step(gt_handle* h, int kind, double* const* f, uint32_t x0, gt_handle::StepGraph* out) {
+  cudaError_t e = cudaSuccess;
+  if (!h->cap_stream) {
+    e = cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(h, e, "step graph: capture stream");
+  }
+  if ((kind == SK_RK2F || kind == SK_RK4F) && ensure_kick_stream(h)) return GT_ERR_CUDA;
+  cudaStream_t saved = h->stream;
+  h->stream = h->cap_stream;
+  e = cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    h->stream = saved;
+    return cuda_fail(h, e, "step graph: cudaStreamBeginCapture");
+  }
+  const int rc = step_direct(h, kind, f, x0);
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(h->cap_stream, &graph);
+  h->stream = saved;
+  if (rc || e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return rc ? rc : cuda_fail(h, e == cudaSuccess ? cudaErrorStreamCaptureInvalidated : e, "step graph: capture");
+  }
+  // the kick node of a forced step
+  cudaGraphNode_t kick = nullptr;
+  if (kind == SK_RK2F || kind == SK_RK4F) {
+    size_t nn = 0;
+    e = cudaGraphGetNodes(graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (e == cudaSuccess && nn) e = cudaGraphGetNodes(graph, nodes.data(), &nn);
+    for (size_t k = 0; k < nn && e == cudaSuccess && !kick; ++k) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(nodes[k], &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+      cudaKernelNodeParams kp = {};
+      if (cudaGraphKernelNodeGetParams(nodes[k], &kp) == cudaSuccess && kp.func == (void*)gt::k_kick_values)
+        kick = nodes[k];
+    }
+    if (e != cudaSuccess || !kick) {
+      cudaGraphDestroy(graph);
+      cudaGetLastError();
+      return cuda_fail(h, e == cudaSuccess ? cudaErrorInvalidValue : e, "step graph: kick node");
+    }
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);  // the instance keeps what it needs; node handles stay valid for it
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_fail(h, e, "step graph: cudaGraphInstantiate");
+  }
+  out->exec = exec;
+  out->kick = kick;
+  return GT_OK;
+}
+
+// One step of `kind`: replayed from its graph where graphs are on, else launched directly.
+static int run_step(gt_handle* h, int kind, double* z, double* znl, double* znew, double* u, double* v, uint32_t x0) {
+  double* const f[5] = {z, znl, znew, u, v};
+  bool use = h->graphs && !h->prof && !h->graph_failed;
+  if (use) {  // a step enqueued into a stream that is itself being captured stays a set of launches
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(h->stream, &cs) != cudaSuccess) {
+      cudaGetLastError();
+      use = false;
+    } else if (cs != cudaStreamCaptureStatusNone) {
+      use = false;
+    }
+  }
+  if (!use) return step_direct(h, kind, f, x0);
+  gt_handle::StepGraph* g = nullptr;
+  for (auto& c : h->sg) {
+    if (c.kind == kind && c.variant == h->variant && c.row_variant == h->row_variant &&
+        c.col_split == h->col_split && c.pdl == h->pdl && c.f[0] == z && c.f[1] == znl && c.f[2] == znew &&
+        c.f[3] == u && c.f[4] == v) {
+      g = &c;
+      break;
+    }
+  }
+  if (!g) {
+    gt_handle::StepGraph ng;
+    ng.kind = kind;
+    for (int k = 0; k < 5; ++k) ng.f[k] = f[k];
+    ng.variant = h->variant;
+    ng.row_variant = h->row_variant;
+    ng.col_split = h->col_split;
+    ng.pdl = h->pdl;
+    const int rc = capture_step(h, kind, f, x0, &ng);
+    if (rc) {  // graphs unavailable here: direct launches from now on
+      h->graph_failed = true;
+      h->err.clear();
+      return step_direct(h, kind, f, x0);
+    }
+    if (h->sg.size() >= kStepGraphs) {  // evict the least recently used
+      size_t lru = 0;
+      for (size_t k = 1; k < h->sg.size(); ++k)
+        if (h->sg[k].used < h->sg[lru].used) lru = k;
+      cudaGraphExecDestroy(h->sg[lru].exec);
+      h->sg.erase(h->sg.begin() + (long)lru);
+    }
+    h->sg.push_back(ng);
+    g = &h->sg.back();
+  }
+  g->used = ++h->sg_clock;
+  cudaError_t e = cudaSuccess;
+  if (g->kick) e = set_kick_node(h, g->exec, g->kick, x0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(g->exec, h->stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "step graph: launch");
+  return GT_OK;
+}
+
+int gt_step_rk2(gt_handle* h, double* z, double* znl, double* u, double* v) {
+  if (!h || !z || !znl || !u || !v) return fail(h, GT_ERR_ARG, "gt_step_rk2: null argument");
+  return run_step(h, SK_RK2, z, znl, nullptr, u, v, 0);
+}
+
+int gt_step_rk4(gt_handle* h, double* z, double* znl, double* znew, double* u, double* v) {
+  if (!h || !z || !znl || !znew || !u || !v) return fail(h, GT_ERR_ARG, "gt_step_rk4: null argument");
+  if (h->split) return fail(h, GT_ERR_ARG, "gt_step_rk4: the split integrator exists only for RK2");
+  return run_step(h, SK_RK4, z, znl, znew, u, v, 0);
+}
+
 int gt_step_rk2_forced(gt_handle* h, double* z, double* znl, double* u, double* v, int32_t* seed) {
   if (!h || !z || !znl || !u || !v || !seed) return fail(h, GT_ERR_ARG, "gt_step_rk2_forced: null argument");
   if (!(h->nf > 0 && h->fuse_ok)) {
     const int rc = gt_step_rk2(h, z, znl, u, v);
     return rc ? rc : gt_forcing(h, z, seed);
   }
-  gt::EpiArgs epi[2] = {make_epi(h, gt::EPI_RK2A, znl, nullptr, z),
-                        make_epi(h, gt::EPI_RK2B, z, nullptr, z)};
   const uint32_t x0 = (uint32_t)(*seed);
-  cudaEvent_t join = nullptr;
-  int rc = start_fused_kick(h, epi[1], x0, &join);
-  if (rc) return rc;
-  const double* zin[2] = {z, znl};
-  rc = stage_chain(h, 2, zin, znl, u, v, epi, join);
+  const int rc = run_step(h, SK_RK2F, z, znl, nullptr, u, v, x0);
   if (rc) return rc;
   *seed = (int32_t)((h->lcga_nf * x0 + h->lcgb_nf) & 0x7FFFFFFFu);
   return GT_OK;
@@ -908,16 +1112,24 @@ int gt_step_rk4_forced(gt_handle* h, double* z, double* znl, double* znew, doubl
     const int rc = gt_step_rk4(h, z, znl, znew, u, v);
     return rc ? rc : gt_forcing(h, z, seed);
   }
-  gt::EpiArgs epi[4] = {make_epi(h, gt::EPI_RK4A, znl, znew, z), make_epi(h, gt::EPI_RK4B, znl, znew, z),
-                        make_epi(h, gt::EPI_RK4C, znl, znew, z), make_epi(h, gt::EPI_RK4D, z, znew, nullptr)};
   const uint32_t x0 = (uint32_t)(*seed);
-  cudaEvent_t join = nullptr;
-  int rc = start_fused_kick(h, epi[3], x0, &join);
-  if (rc) return rc;
-  const double* zin[4] = {z, znl, znl, znl};
-  rc = stage_chain(h, 4, zin, znl, u, v, epi, join);
+  const int rc = run_step(h, SK_RK4F, z, znl, znew, u, v, x0);
   if (rc) return rc;
   *seed = (int32_t)((h->lcga_nf * x0 + h->lcgb_nf) & 0x7FFFFFFFu);
+  return GT_OK;
+}
+
+int gt_set_graphs(gt_handle* h, int32_t on) {
+  if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_graphs: null handle");
+  h->graphs = on ? 1 : 0;
+  if (!on) drop_step_graphs(h);
+  h->graph_failed = false;
+  return GT_OK;
+}
+
+int gt_get_graphs(const gt_handle* h, int32_t* on) {
+  if (!h || !on) return fail(nullptr, GT_ERR_ARG, "gt_get_graphs: null argument");
+  *on = h->graphs && !h->graph_failed;
   return GT_OK;
 }
 

@@ -189,6 +189,17 @@ class Solver:
         self._check(self.lib.gt_set_pdl(self.h, int(bool(on))))
 
     @property
+    def graphs(self) -> bool:
+        """Whether the steps replay CUDA graphs of the handle (gt_get_graphs)."""
+        a = ctypes.c_int32()
+        self._check(self.lib.gt_get_graphs(self.h, ctypes.byref(a)))
+        return bool(a.value)
+
+    @graphs.setter
+    def graphs(self, on: bool) -> None:
+        self._check(self.lib.gt_set_graphs(self.h, int(bool(on))))
+
+    @property
     def adj_memory(self) -> int:
         """Device memory (bytes) the adjoint gradient may hold for whole kept segments
         (gt_adj_get_memory; 0 = only its last segment)."""
