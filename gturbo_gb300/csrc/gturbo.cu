@@ -87,6 +87,7 @@ struct gt_handle {
     int kind = 0;
     const void* f[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int variant = 0, row_variant = 0, col_split = 0, pdl = 0;
+    cudaGraph_t graph = nullptr;     // kept alive: its node handles address the instance
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t kick = nullptr;  // the k_kick_values node of a forced step
     unsigned long long used = 0;
@@ -942,9 +943,15 @@ static int step_direct(gt_handle* h, int kind, double* const* f, uint32_t x0) {
   }
 }
 
+static void free_step_graph(gt_handle::StepGraph& g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.graph) cudaGraphDestroy(g.graph);
+  g.exec = nullptr;
+  g.graph = nullptr;
+}
+
 static void drop_step_graphs(gt_handle* h) {
-  for (auto& g : h->sg)
-    if (g.exec) cudaGraphExecDestroy(g.exec);
+  for (auto& g : h->sg) free_step_graph(g);
   h->sg.clear();
 }
 
@@ -1014,11 +1021,12 @@ static int capture_step(gt_handle* h, int kind, double* const* f, uint32_t x0, g
   }
   cudaGraphExec_t exec = nullptr;
   e = cudaGraphInstantiate(&exec, graph, 0);
-  cudaGraphDestroy(graph);  // the instance keeps what it needs; node handles stay valid for it
   if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
     cudaGetLastError();
     return cuda_fail(h, e, "step graph: cudaGraphInstantiate");
   }
+  out->graph = graph;
   out->exec = exec;
   out->kick = kick;
   return GT_OK;
@@ -1065,7 +1073,7 @@ static int run_step(gt_handle* h, int kind, double* z, double* znl, double* znew
       size_t lru = 0;
       for (size_t k = 1; k < h->sg.size(); ++k)
         if (h->sg[k].used < h->sg[lru].used) lru = k;
-      cudaGraphExecDestroy(h->sg[lru].exec);
+      free_step_graph(h->sg[lru]);
       h->sg.erase(h->sg.begin() + (long)lru);
     }
     h->sg.push_back(ng);
@@ -1075,7 +1083,12 @@ static int run_step(gt_handle* h, int kind, double* z, double* znl, double* znew
   cudaError_t e = cudaSuccess;
   if (g->kick) e = set_kick_node(h, g->exec, g->kick, x0);
   if (e == cudaSuccess) e = cudaGraphLaunch(g->exec, h->stream);
-  if (e != cudaSuccess) return cuda_fail(h, e, "step graph: launch");
+  if (e != cudaSuccess) {  // nothing was enqueued: direct launches from now on
+    cudaGetLastError();
+    drop_step_graphs(h);
+    h->graph_failed = true;
+    return step_direct(h, kind, f, x0);
+  }
   return GT_OK;
 }
 

@@ -49,6 +49,7 @@ def test_graph_steps_bit_identical_to_direct(n, rko, forced):
             a.rk_step(za, wa)
             b.rk_step(zb, wb)
     torch.cuda.synchronize()
+    assert a.graphs  # no fallback to direct launches happened
     assert sa == sb
     assert torch.equal(za, zb)
     # and against the oracle
