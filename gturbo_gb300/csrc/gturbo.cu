@@ -924,10 +924,10 @@ static int step_rk4_forced_direct(gt_handle* h, double* z, double* znl, double* 
 }
 
 // ---- steps as CUDA graphs ---------------------------------------------------------------
-// A step is a dozen short launches; on small grids the host's launch rate, not the GPU, sets
-// the step time (256^2 RK4: about 100 us of host time per step for about 50 us of kernels). Each
-// step kind is therefore captured once per (fields, launch settings) into a CUDA graph on a
-// capture stream of the handle and replayed on the handle's stream. The graph holds the same
+// A step is a dozen short launches. Each step kind is captured once per (fields, launch
+// settings) into a CUDA graph on a capture stream of the handle and replayed on the handle's
+// stream as one launch, which takes the per-launch host work off the step (at 256^2 RK4 the GPU
+// time of the kernels, about 0.1 ms, still sets the step time). The graph holds the same
 // launches with the same arguments, so its results are the direct launches' bit for bit. The
 // forced steps' kick increments depend on the LCG state of the call: the k_kick_values node's
 // parameters are rewritten before each replay.

@@ -360,10 +360,10 @@ int gt_get_col_split(const gt_handle* h, int32_t* active);
 int gt_set_pdl(gt_handle* h, int32_t on);
 int gt_get_pdl(const gt_handle* h, int32_t* on);
 /* CUDA graphs of the steps (gt_step_rk2, gt_step_rk4 and their _forced forms). No counterpart in
- * the reference. A step is a dozen short launches, and on small grids the host's launch rate
- * sets its time: with graphs on (the default), each step is captured once per set of fields and
- * launch settings into a CUDA graph of the handle and replayed (up to 4 graphs per handle, the
- * least recently used evicted). Results are bit-identical to the direct launches. The forced
+ * the reference. A step is a dozen short launches; with graphs on (the default), each step is
+ * captured once per set of fields and launch settings into a CUDA graph of the handle and
+ * replayed as one launch (up to 4 graphs per handle, the least recently used evicted), which
+ * takes the per-launch host work off the step. Results are bit-identical to the direct launches. The forced
  * steps' LCG state is written into the kick kernel's node before each replay. Steps run as
  * direct launches while the handle times its launches (gt_profile), while the handle's stream
  * is itself being captured, and after a capture failed (gt_get_graphs then reports 0).
