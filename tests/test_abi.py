@@ -156,3 +156,108 @@ xlx   yly
     assert p.n == 2048 and p.rko == 2 and p.truncate == 1 and p.imix == 100
     assert p.nu == 4.5e-46 and p.alpnu == 8.0 and p.alpv == 1.0 and p.dt == 2e-5
     assert p.xlx == 2 * np.pi and p.k1f == 20.0 and p.famp == 0.4
+
+
+# ---- the bind(C) module's calling convention, argument by argument ---------------------------
+# ISO_C_BINDING passes a dummy with the VALUE attribute by value and every other dummy (scalar or
+# array) by address; type(c_ptr) is a C object pointer. So a Fortran dummy implies a C parameter
+# of a given base type and pointer depth, and a Fortran function result a C return type.
+_F_KIND = {"c_int": "int", "c_int32_t": "int32", "c_int64_t": "int64", "c_double": "double",
+           "c_float": "float", "c_ptr": "ptr", "gt_params": "gt_params", "gt_info": "gt_info"}
+_C_BASE = {"int": "int", "int32_t": "int32", "int64_t": "int64", "uint64_t": "int64", "double": "double",
+           "float": "float", "gt_params": "gt_params", "gt_info": "gt_info"}
+
+
+def _fortran_interfaces(text):
+    """{name: (result kind, [(arg, kind, by_value, is_array)])} of every bind(C) interface."""
+    import re
+    text = re.sub(r"&\s*\n\s*", " ", text)
+    out = {}
+    for m in re.finditer(r"^\s*(integer|real|type)\((\w+)\)\s+function\s+(\w+)\s*\(([^)]*)\)\s*bind\(C[^)]*\)"
+                         r"(.*?)end function", text, re.S | re.M):
+        kind, name, args, body = _F_KIND[m.group(2)], m.group(3), m.group(4), m.group(5)
+        decl = {}
+        for line in body.splitlines():
+            line = line.split("!")[0].strip()
+            if "::" not in line or line.startswith("import"):
+                continue
+            spec, ents = line.split("::")
+            km = re.match(r"(integer|real|type)\((\w+)\)", spec.strip())
+            by_value = "value" in spec
+            for ent in re.findall(r"(\w+)\s*(\([^)]*\))?", ents):
+                decl[ent[0]] = (_F_KIND[km.group(2)], by_value, bool(ent[1]))
+        names = [a.strip() for a in args.split(",") if a.strip()]
+        out[name] = (kind, [(a, *decl[a]) for a in names])
+    return out
+
+
+def _c_prototypes(header):
+    """{name: (return (base, depth), [(base, depth)])} of every gt_ function in the header."""
+    import re
+    header = re.sub(r"/\*.*?\*/", "", header, flags=re.S)
+    out = {}
+    for m in re.finditer(r"([\w\s\*]+?)\b(gt_\w+)\s*\(([^)]*)\)\s*;", header):
+        def parse(t):
+            depth = t.count("*")
+            words = [w for w in re.sub(r"[\*]", " ", t).split() if w not in ("const", "struct")]
+            base = words[0] if words else "void"
+            if len(words) > 1 and words[-1] not in _C_BASE and words[-1] != base:
+                base = words[0]  # "type name": the first word is the type
+            return _C_BASE.get(base, "ptr" if depth else base), depth
+        ret = parse(m.group(1).strip().split("\n")[-1])
+        params = [parse(p) for p in m.group(3).split(",") if p.strip() and p.strip() != "void"]
+        out[m.group(2)] = (ret, params)
+    return out
+
+
+def test_fortran_module_calling_convention_matches_header():
+    """Every bind(C) interface of include/gturbo_c.f90 passes each argument the way the C
+    prototype in gturbo.h receives it: VALUE dummies as C values of the same type, other
+    dummies as pointers to it, type(c_ptr) VALUE as an object pointer, type(c_ptr) arrays or
+    non-VALUE scalars as pointers to pointers; and the result kinds match the C return types."""
+    fi = _fortran_interfaces(open(os.path.join(ROOT, "include", "gturbo_c.f90")).read())
+    cp = _c_prototypes(open(_lib.HEADER).read())
+    assert len(fi) >= 19
+    for name, (fres, fargs) in fi.items():
+        assert name in cp, name
+        (cret, cdepth), cparams = cp[name]
+        if fres == "ptr":
+            assert cdepth >= 1, name
+        else:
+            assert (fres, 0) == (cret, cdepth), (name, fres, cret, cdepth)
+        assert len(fargs) == len(cparams), name
+        for (arg, kind, by_value, is_array), (cbase, depth) in zip(fargs, cparams):
+            where = f"{name}({arg})"
+            if kind == "ptr":
+                want = 1 if by_value else 2
+                assert depth == want, (where, depth, want)
+            elif by_value:
+                assert (cbase, depth) == (kind, 0), (where, cbase, depth, kind)
+            else:
+                assert (cbase, depth) == (kind, 1), (where, cbase, depth, kind)
+
+
+def test_calling_convention_check_catches_planted_mistakes():
+    """The check above fails on a copy of the module with a VALUE attribute dropped or a kind
+    changed (the mistakes a hand-written bind(C) block makes)."""
+    text = open(os.path.join(ROOT, "include", "gturbo_c.f90")).read()
+    cp = _c_prototypes(open(_lib.HEADER).read())
+
+    def consistent(t):
+        for name, (fres, fargs) in _fortran_interfaces(t).items():
+            _, cparams = cp[name]
+            for (arg, kind, by_value, is_array), (cbase, depth) in zip(fargs, cparams):
+                if kind == "ptr":
+                    if depth != (1 if by_value else 2):
+                        return False
+                elif (cbase, depth) != (kind, 0 if by_value else 1):
+                    return False
+        return True
+
+    assert consistent(text)
+    old = 'function gt_destroy(h) bind(C, name="gt_destroy")\n      import :: c_int, c_ptr\n      type(c_ptr), value :: h'
+    assert old in text
+    assert not consistent(text.replace(old, old.replace("type(c_ptr), value :: h", "type(c_ptr) :: h")))
+    old = "integer(c_int32_t) :: seed"
+    assert old in text
+    assert not consistent(text.replace(old, "integer(c_int64_t) :: seed", 1))
