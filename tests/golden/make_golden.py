@@ -33,6 +33,9 @@ CASES = {
                           dt=1e-3, famp=0.3), 102),
     "n64_a05_rk2_split": (Params(n=64, alpv=0.5, rko=2, k1f=4.0, k2f=6.0, nu=1e-4, alpnu=1.0,
                                  mu=0.0, alpmu=0.0, dt=1e-3, famp=0.2), 103),
+    # a non-square grid, NX = 64 by NY = 32 (the reference's transforms planned as NY x NX)
+    "n64x32_a2_rk4": (Params(n=64, ny=32, alpv=2.0, rko=4, k1f=3.0, k2f=6.0, nu=1e-12, alpnu=4.0,
+                             mu=0.05, dt=1e-3, famp=0.4), 104),
 }
 # main-loop horizon: steps of src/main.f90:97-137 with diagnostics every HORIZON_IMIX steps
 HORIZON_STEPS = 20
@@ -43,9 +46,9 @@ def make_case(name, p, seed):
     from oracle.refcore import Reference
 
     r = Reference(p)
-    n = p.n
+    n, ny = p.n, p.rows
     rng = np.random.default_rng(seed)
-    x = rng.standard_normal((n, n))
+    x = rng.standard_normal((ny, n))
     out = {"n": p.n, "phys_in": x}
     a = r.zeros()
     a[:, :n] = x
@@ -87,7 +90,7 @@ def make_case(name, p, seed):
         r.fft_inv(b)
         path = r.writef2(b, 0, 1, wd)
         raw = np.fromfile(path, dtype=np.uint8)
-    out["dump_record"] = raw[4:-4].view(np.float32).reshape(n, n).copy()
+    out["dump_record"] = raw[4:-4].view(np.float32).reshape(ny, n).copy()
     # main-loop horizon from the same field and the reference's seed
     z, s = zk.copy(), 481929
     work = [r.zeros() for _ in range(4)]

@@ -453,7 +453,7 @@ def test_spectra_50_step_horizon(cfg):
     assert rel_l2(_host(z), ref) < 1e-10
 
 
-@pytest.mark.parametrize("name", ["n32_a2_rk4", "n64_a1_rk2", "n64_a05_rk2_split"])
+@pytest.mark.parametrize("name", ["n32_a2_rk4", "n64_a1_rk2", "n64_a05_rk2_split", "n64x32_a2_rk4"])
 def test_against_golden_vectors(name):
     """The CUDA path against the committed vectors of the reference's own statements
     (tests/golden/make_golden.py: the transliterated Fortran with the cuFFT shim)."""
@@ -463,7 +463,7 @@ def test_against_golden_vectors(name):
     g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{name}.npz"))
     sol = _solver(p)
     n = p.n
-    a = np.zeros((n, n + 2))
+    a = np.zeros((p.rows, n + 2))
     a[:, :n] = g["phys_in"]
     z = _dev(a)
     sol.fft_dir(z)

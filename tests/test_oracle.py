@@ -47,7 +47,7 @@ def test_c_oracle_matches_numpy_restatement(n, alpv, rko):
         assert np.abs(d1[k] - d2[k]).max() <= 1e-13 * np.abs(d2[k]).max(), k
 
 
-@pytest.mark.parametrize("name", ["n32_a2_rk4", "n64_a1_rk2", "n64_a05_rk2_split"])
+@pytest.mark.parametrize("name", ["n32_a2_rk4", "n64_a1_rk2", "n64_a05_rk2_split", "n64x32_a2_rk4"])
 def test_c_oracle_against_golden(name):
     from tests.golden.make_golden import CASES
     p, _ = CASES[name]
@@ -57,7 +57,7 @@ def test_c_oracle_against_golden(name):
     ik, jk = o.forcing_modes()
     assert np.array_equal(ik, g["ikxf"]) and np.array_equal(jk, g["ikyf"])
     assert o.info.inpe == pytest.approx(float(g["inpe"][0]), rel=1e-14)
-    a = np.zeros((n, n + 2))
+    a = o.zeros()
     a[:, :n] = g["phys_in"]
     o.fft_dir(a)
     assert rel_l2(a, g["fft_dir"]) < 1e-14

@@ -183,7 +183,7 @@ def test_restart_files_round_trip_through_reference():
 
 
 @needs_ref
-@pytest.mark.parametrize("name", ["n32_a2_rk4", "n64_a1_rk2", "n64_a05_rk2_split"])
+@pytest.mark.parametrize("name", ["n32_a2_rk4", "n64_a1_rk2", "n64_a05_rk2_split", "n64x32_a2_rk4"])
 def test_golden_vectors_are_the_reference(name, tmp_path, monkeypatch):
     """The committed fixtures equal a fresh computation by the transliterated reference."""
     from tests.golden import make_golden
@@ -198,7 +198,7 @@ def test_golden_vectors_are_the_reference(name, tmp_path, monkeypatch):
         assert np.array_equal(fresh[k], g[k]), k
 
 
-@pytest.mark.parametrize("name", ["n32_a2_rk4", "n64_a1_rk2", "n64_a05_rk2_split"])
+@pytest.mark.parametrize("name", ["n32_a2_rk4", "n64_a1_rk2", "n64_a05_rk2_split", "n64x32_a2_rk4"])
 def test_oracle_main_loop_against_golden_horizon(name):
     """The oracle reproduces the reference's 20-step main-loop fixture (no reference needed)."""
     from tests.golden.make_golden import CASES as GC, HORIZON_IMIX, HORIZON_STEPS
