@@ -614,6 +614,74 @@ __device__ __forceinline__ void tlm_colfwd_field_tile(const TlmArgs& a, int unit
   }
 }
 
+// Tangent pass C with the column's four CTAs (A, B, dA, dB) as one 4-CTA cluster. Each CTA keeps
+// its transformed field (kx-scaled for A and dA) in its own shared memory for the rows the others
+// combine; after a cluster barrier CTA f forms N and dN for the rows j = t + s T with s = f, f + 4,
+// ..., reading the other three fields from the partners' shared memory, and runs the stage update
+// there (the per-value arithmetic of tlm_colfwd_field_tile). A second barrier keeps the shared
+// memory alive until the partners have read it. The transformed B and dB are not written back:
+// nothing reads them after this pass.
+template <int N, int R>
+__device__ __forceinline__ void tlm_colfwd_cluster_tile(const TlmArgs& a, int unit) {
+  constexpr int T = N / R, NH = N / 2 + 1;
+  extern __shared__ double2 smem[];
+  const int i = unit / 4, f = unit % 4, t = threadIdx.x;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const double scale = 0.5 / ((double)N * (double)N);
+  const double2* own = f == 0 ? a.u : f == 1 ? a.v : f == 2 ? a.du : a.dv;
+  double2 v[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = own[(size_t)(t + s * T) * NH + i];
+  fft_regs<N, R, false, 1>(v, smem, t, a.tw, 0);
+  if ((f & 1) == 0) {
+    const double kxs = __ldg(&a.fkx[i]) * scale;
+#pragma unroll
+    for (int s = 0; s < R; ++s) v[s] = make_double2(kxs * v[s].x, kxs * v[s].y);
+  }
+  // fft_regs ends with a barrier after its last shared-memory read: the buffer is free
+#pragma unroll
+  for (int s = 0; s < R; ++s)
+    if (s % 4 != f) smem[t + s * T] = v[s];
+  cluster.sync();
+  const double2* pa = cluster.map_shared_rank(smem, 0u);
+  const double2* pb = cluster.map_shared_rank(smem, 1u);
+  const double2* pda = cluster.map_shared_rank(smem, 2u);
+  const double2* pdb = cluster.map_shared_rank(smem, 3u);
+  const int kc = a.truncate ? __ldg(&a.kcut[i]) : N;
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    if (s % 4 != f) continue;
+    const int j = t + s * T;
+    const size_t o = (size_t)j * NH + i;
+    const double2 fa = f == 0 ? v[s] : pa[j];
+    const double2 fb = f == 1 ? v[s] : pb[j];
+    const double2 dfa = f == 2 ? v[s] : pda[j];
+    const double2 dfb = f == 3 ? v[s] : pdb[j];
+    const double kys = __ldg(&a.fky[j]) * scale;
+    double2 nh = make_double2(fma(kys, fb.y, fa.y), -fma(kys, fb.x, fa.x));
+    double2 dn = make_double2(fma(kys, dfb.y, dfa.y), -fma(kys, dfb.x, dfa.x));
+    if (min(j, N - j) > kc || (i == 0 && j == 0 && a.truncate)) {
+      nh = czero();
+      dn = czero();
+    }
+    a.u[o] = nh;   // N and dN in place of A and dA (TLM_PLAIN reads them there)
+    a.du[o] = dn;
+    if (a.mode == TLM_PLAIN) continue;
+    const double e = stage_e(a.emk, a.emkx, a.emky, a.split, i, j, NH);
+    const bool origin = (i == 0 && j == 0);
+    const double2 z = a.z[o], dz = a.dz[o];
+    if (a.mode == TLM_STAGE_A) {
+      a.w[o] = origin ? czero() : make_double2(e * (z.x + a.dt2 * nh.x), e * (z.y + a.dt2 * nh.y));
+      a.dw[o] = origin ? czero() : make_double2(e * (dz.x + a.dt2 * dn.x), e * (dz.y + a.dt2 * dn.y));
+    } else {
+      a.z[o] = origin ? czero() : make_double2(e * (e * z.x + a.dt * nh.x), e * (e * z.y + a.dt * nh.y));
+      a.dz[o] = origin ? czero() : make_double2(e * (e * dz.x + a.dt * dn.x), e * (e * dz.y + a.dt * dn.y));
+    }
+  }
+  cluster.sync();
+}
+
 // ---- field-split transposed column tiles (one field of one column per CTA, C = 1) ---------------
 
 // Fields of the transposed pass A: q, u, v from x (f = 0, 1, 2) and a, b from lin (3, 4); with
@@ -869,6 +937,13 @@ template <int N, int V>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_adj_colinv_fs(AdjArgs a) {
   pdl_enter();
   if constexpr (AdjSplitVar<N, V>::OK) adj_colinv_field_tile<N, Var<N, V>::R>(a, blockIdx.x);
+}
+// the tangent pass C with the column's four CTAs as one cluster (grid 4 NH)
+template <int N, int V>
+__global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB)
+    k_tlm_colfwd_cl(TlmArgs a) {
+  pdl_enter();
+  if constexpr (AdjSplitVar<N, V>::OK) tlm_colfwd_cluster_tile<N, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_adj_colfwd_fs(AdjArgs a) {

@@ -346,3 +346,21 @@ def test_c5_configuration_fd_tlm_and_dot_product():
     fd = (forward_objective(Solver(p.replace(famp=p.famp + hf)), z0, nsteps, SEED, KMIN, KMAX)
           - forward_objective(Solver(p.replace(famp=p.famp - hf)), z0, nsteps, SEED, KMIN, KMAX)) / (2 * hf)
     assert fd == pytest.approx(dJf, rel=1e-6)
+
+
+@pytest.mark.parametrize("rko", [2, 4])
+def test_tlm_cluster_pass_c_matches_counter_form(rko):
+    """The tangent pass C as 4-CTA clusters (split mode 2, the default) against its per-column
+    counter form (mode 1): the same arithmetic per value, so J and dJ agree to rounding."""
+    from gturbo_gb300.adjoint import tlm_run
+    from gturbo_gb300.solver import Solver
+    p, sol, z0, ns = _setup(n=256, nsteps=6)
+    if rko == 4:
+        sol = Solver(p.replace(rko=4))
+    dz = _direction(z0, 11)
+    out = {}
+    for mode in (2, 1):
+        sol.col_split = mode
+        out[mode] = tlm_run(sol, z0, dz, 0.2, ns, SEED, KMIN, KMAX)
+    assert out[2][0] == pytest.approx(out[1][0], rel=1e-14)
+    assert out[2][1] == pytest.approx(out[1][1], rel=1e-12)
