@@ -204,3 +204,31 @@ def test_square_only_paths_reject_non_square():
     keys = (ctypes.c_uint64 * 1)(7)
     h = ctypes.c_void_p()
     assert lib.gt_ens_create(arr, 1, keys, ctypes.byref(h)) == 1
+
+
+@pytest.mark.parametrize("nx,ny,xlx,xly,rko", [(256, 256, 2.0, 4.0, 2), (256, 256, 2.0, 1.0, 4),
+                                               (512, 256, 2.0, 3.0, 4), (128, 512, 1.0, 2.0, 2)])
+def test_rectangular_domains(nx, ny, xlx, xly, rko):
+    """Box lengths xlx != xly (params.dat's first record, src/inieuler.f90:13), so dkx != dky:
+    the nonlinear term, the step, the kick and the diagnostics against the oracle."""
+    import math
+    p = _params(nx, ny, rko=rko, alpv=2.0, xlx=xlx * math.pi, xly=xly * math.pi, k1f=3.0, k2f=6.0)
+    orc, sol = Oracle(p), _solver(p)
+    assert sol.info.dkx != sol.info.dky or xlx == xly
+    zk = rand_field(orc, 21)
+    z, u, v = _dev(zk), sol.field(), sol.field()
+    sol.nlt(z, u, v)
+    b = zk.copy()
+    orc.nlt(b)
+    assert rel_l2(_host(z), b) < TOL
+    d = sol.diag(_dev(zk), _dev(b))
+    do = orc.diag(zk, b)
+    for k in ("sp", "sz", "fle", "flz", "glob"):
+        assert np.abs(d[k] - do[k]).max() <= 1e-12 * np.abs(do[k]).max(), k
+    z = _dev(zk)
+    s = sol.rk_step_forced(z, sol.work(), 481929)
+    a = zk.copy()
+    orc.rk_step(a)
+    s2 = orc.forcing(a, 481929)
+    assert s == s2
+    assert rel_l2(_host(z), a) < TOL

@@ -48,6 +48,13 @@ CASES += [
     _p(64, ny=256, alpv=2.0, rko=2, nu=1e-4, alpnu=1.0, mu=0.0, alpmu=0.0),  # split integrator
 ]
 IDS += ["n64x32a1rk2", "n32x64a2rk4", "n128x64a05rk4", "n64x256a2rk2_split"]
+# rectangular domains xlx != xly (params.dat carries both, inieuler.f90:13): dkx != dky
+import math  # noqa: E402
+CASES += [
+    _p(64, xly=4.0 * math.pi, alpv=1.0, rko=2, k1f=2.0, k2f=4.0),
+    _p(64, ny=128, xlx=math.pi, xly=3.0 * math.pi, alpv=2.0, rko=4, k1f=3.0, k2f=6.0),
+]
+IDS += ["n64a1rk2_Ly2", "n64x128a2rk4_Lx05_Ly15"]
 
 
 @needs_ref
