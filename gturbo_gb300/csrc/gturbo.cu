@@ -93,7 +93,8 @@ struct gt_handle {
     unsigned long long used = 0;
   };
   int graphs = 1;
-  bool graph_failed = false;  // a capture failed once: direct launches from then on
+  bool graph_failed = false;  // a capture failed once, or captures kept evicting one another
+  unsigned long long sg_captures = 0, sg_replays = 0;
   std::vector<StepGraph> sg;
   unsigned long long sg_clock = 0;
   cudaStream_t cap_stream = nullptr;
@@ -932,7 +933,7 @@ static int step_rk4_forced_direct(gt_handle* h, double* z, double* znl, double* 
 // forced steps' kick increments depend on the LCG state of the call: the k_kick_values node's
 // parameters are rewritten before each replay.
 enum StepKind { SK_RK2 = 1, SK_RK4 = 2, SK_RK2F = 3, SK_RK4F = 4 };
-constexpr size_t kStepGraphs = 4;
+constexpr size_t kStepGraphs = 8;
 
 static int step_direct(gt_handle* h, int kind, double* const* f, uint32_t x0) {
   switch (kind) {
@@ -1069,6 +1070,14 @@ static int run_step(gt_handle* h, int kind, double* z, double* znl, double* znew
       h->err.clear();
       return step_direct(h, kind, f, x0);
     }
+    // a handle that cycles through more field sets than it keeps graphs for would capture on
+    // almost every step: after 16 captures with fewer than two replays each, launch directly
+    if (++h->sg_captures >= 16 && h->sg_replays < 2 * h->sg_captures) {
+      free_step_graph(ng);
+      drop_step_graphs(h);
+      h->graph_failed = true;
+      return step_direct(h, kind, f, x0);
+    }
     if (h->sg.size() >= kStepGraphs) {  // evict the least recently used
       size_t lru = 0;
       for (size_t k = 1; k < h->sg.size(); ++k)
@@ -1080,6 +1089,7 @@ static int run_step(gt_handle* h, int kind, double* z, double* znl, double* znew
     g = &h->sg.back();
   }
   g->used = ++h->sg_clock;
+  ++h->sg_replays;
   cudaError_t e = cudaSuccess;
   if (g->kick) e = set_kick_node(h, g->exec, g->kick, x0);
   if (e == cudaSuccess) e = cudaGraphLaunch(g->exec, h->stream);
@@ -1137,6 +1147,7 @@ int gt_set_graphs(gt_handle* h, int32_t on) {
   h->graphs = on ? 1 : 0;
   if (!on) drop_step_graphs(h);
   h->graph_failed = false;
+  h->sg_captures = h->sg_replays = 0;
   return GT_OK;
 }
 

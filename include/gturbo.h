@@ -362,11 +362,13 @@ int gt_get_pdl(const gt_handle* h, int32_t* on);
 /* CUDA graphs of the steps (gt_step_rk2, gt_step_rk4 and their _forced forms). No counterpart in
  * the reference. A step is a dozen short launches; with graphs on (the default), each step is
  * captured once per set of fields and launch settings into a CUDA graph of the handle and
- * replayed as one launch (up to 4 graphs per handle, the least recently used evicted), which
+ * replayed as one launch (up to 8 graphs per handle, the least recently used evicted), which
  * takes the per-launch host work off the step. Results are bit-identical to the direct launches. The forced
  * steps' LCG state is written into the kick kernel's node before each replay. Steps run as
  * direct launches while the handle times its launches (gt_profile), while the handle's stream
- * is itself being captured, and after a capture failed (gt_get_graphs then reports 0).
+ * is itself being captured, after a capture failed, and once a handle that cycles through more
+ * field sets than it keeps graphs for has captured 16 times with fewer than two replays per
+ * capture (gt_get_graphs then reports 0; gt_set_graphs(h, 1) tries again).
  * gt_set_graphs(h, 0) frees the handle's graphs. */
 int gt_set_graphs(gt_handle* h, int32_t on);
 int gt_get_graphs(const gt_handle* h, int32_t* on);

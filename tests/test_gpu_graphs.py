@@ -67,8 +67,8 @@ def test_graphs_follow_settings_fields_and_profiling():
     orc = Oracle(p)
     a, b = _pair(p)
     f0 = rand_field(orc, 8)
-    # more field sets than the handle keeps graphs for: every step still right
-    fields = [(torch.from_numpy(f0).cuda(), a.work()) for _ in range(6)]
+    # more field sets than the handle keeps graphs for (8): every step still right
+    fields = [(torch.from_numpy(f0).cuda(), a.work()) for _ in range(10)]
     ref = torch.from_numpy(f0).cuda()
     wb = b.work()
     for rnd in range(2):
@@ -99,4 +99,25 @@ def test_graphs_follow_settings_fields_and_profiling():
     prof = a.profile_read()
     a.profile(False)
     assert sum(v[1] for v in prof.values()) >= 12
+    assert a.graphs
+
+
+def test_handle_cycling_through_many_fields_falls_back_to_direct_launches():
+    """A handle stepping more field sets in turn than it keeps graphs for would capture on every
+    step; it goes back to direct launches (results unchanged) and gt_set_graphs(h, 1) re-arms it."""
+    p = _params(128, 2)
+    orc = Oracle(p)
+    a, b = _pair(p)
+    f0 = rand_field(orc, 9)
+    fields = [(torch.from_numpy(f0).cuda(), a.work()) for _ in range(12)]
+    ref, wb = torch.from_numpy(f0).cuda(), b.work()
+    for _ in range(3):
+        for z, w in fields:
+            a.rk_step(z, w)
+        b.rk_step(ref, wb)
+    torch.cuda.synchronize()
+    for z, _ in fields:
+        assert torch.equal(z, ref)
+    assert not a.graphs
+    a.graphs = True
     assert a.graphs
