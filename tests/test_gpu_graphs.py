@@ -78,6 +78,7 @@ def test_graphs_follow_settings_fields_and_profiling():
     torch.cuda.synchronize()
     for z, _ in fields:
         assert torch.equal(z, ref)
+    a.graphs = True  # cycling through more field sets than it keeps graphs for turned them off
     # a change of launch variants or split mode captures a new graph
     for cv, rv, split in ((2, 2, 0), (3, 2, 0), (2, 1, 2)):
         a.variants = (cv, rv)
