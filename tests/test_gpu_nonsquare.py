@@ -232,3 +232,35 @@ def test_rectangular_domains(nx, ny, xlx, xly, rko):
     s2 = orc.forcing(a, 481929)
     assert s == s2
     assert rel_l2(_host(z), a) < TOL
+
+
+@pytest.mark.parametrize("nx,ny,kw", [
+    (512, 256, dict(alpnu=1.0, nu=1e-4, mu=0.0, alpmu=0.0)),  # split integrator (RK2)
+    (256, 512, dict(truncate=0)),                             # no dealiasing
+    (256, 1024, dict(rko=4, alpv=3.0)),
+])
+def test_edge_configurations(nx, ny, kw):
+    p = _params(nx, ny, **kw)
+    orc, sol = Oracle(p), _solver(p)
+    if "alpnu" in kw:
+        assert sol.info.split == 1
+    a = rand_field(orc, 31, truncate=bool(p.truncate))
+    ref = a.copy()
+    orc.rk_step(ref)
+    z = _dev(a)
+    sol.rk_step(z, sol.work())
+    assert rel_l2(_host(z), ref) < TOL
+
+
+@pytest.mark.parametrize("nx,ny", [(512, 256), (256, 1024)])
+def test_untruncated_input(nx, ny):
+    """An input with modes beyond the 2/3 ellipse (the untruncated-input flag path of the column
+    passes, with the column count at run time)."""
+    p = _params(nx, ny)
+    orc, sol = Oracle(p), _solver(p)
+    a = rand_field(orc, 32, truncate=False)
+    ref = a.copy()
+    orc.nlt(ref)
+    z, u, v = _dev(a), sol.field(), sol.field()
+    sol.nlt(z, u, v)
+    assert rel_l2(_host(z), ref) < TOL
