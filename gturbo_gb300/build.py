@@ -29,7 +29,8 @@ def _nvcc() -> str:
 
 
 def sources() -> list[str]:
-    units = sorted(f for f in os.listdir(CSRC) if f.startswith("gt_inst_") and f.endswith(".cu"))
+    units = sorted(f for f in os.listdir(CSRC)
+                   if f.startswith(("gt_inst_", "gt_ens_r")) and f.endswith(".cu"))
     return [os.path.join(CSRC, f) for f in units] + [os.path.join(CSRC, "gturbo.cu"),
                                                       os.path.join(CSRC, "gt_ens.cu"),
                                                       os.path.join(CSRC, "gt_adj.cu")]

@@ -18,83 +18,10 @@
 
 #include "../../include/gturbo.h"
 #include "gt_internal.h"
+#include "gt_ens_kernels.cuh"
 #include "gt_philox.h"
 
 namespace gt {
-
-// Tile families of the ensemble passes: R complex values per thread and 2048 / R threads per CTA.
-// Every CTA holds 2048 values (C = 2048/N columns or rows of a size-N member) in every family, so
-// the work lists and the shared memory do not depend on the family; gt_ens_autotune times the
-// families on the ensemble's own members and keeps the fastest. MINB: CTAs per SM requested from
-// ptxas (3 for 256 threads caps a thread at 85 registers, as the 8-value tiles need).
-template <int R>
-struct EnsFam {
-  static constexpr int THREADS = 2048 / R;
-  static constexpr int MINB = R == 8 ? kEnsMinBlocks : R == 16 ? 3 : 2;
-};
-
-template <int R>
-__global__ void __launch_bounds__(EnsFam<R>::THREADS, EnsFam<R>::MINB)
-k_ens_colinv(const NltArgs* __restrict__ args, const EnsTile* __restrict__ tiles) {
-  const EnsTile w = tiles[blockIdx.x];
-  const NltArgs a = args[w.member];
-  switch (a.n) {
-    case 128: colinv_tile<128, 16, R>(a, w.tile); break;
-    case 256: colinv_tile<256, 8, R>(a, w.tile); break;
-    case 512: colinv_tile<512, 4, R>(a, w.tile); break;
-    case 1024: colinv_tile<1024, 2, R>(a, w.tile); break;
-    case 2048: colinv_tile<2048, 1, R>(a, w.tile); break;
-    default: break;
-  }
-}
-
-template <int R>
-__global__ void __launch_bounds__(EnsFam<R>::THREADS, EnsFam<R>::MINB)
-k_ens_row(const NltArgs* __restrict__ args, const EnsTile* __restrict__ tiles) {
-  const EnsTile w = tiles[blockIdx.x];
-  const NltArgs a = args[w.member];
-  switch (a.n) {
-    case 128: row_tile<128, 16, R>(a, w.tile); break;
-    case 256: row_tile<256, 8, R>(a, w.tile); break;
-    case 512: row_tile<512, 4, R>(a, w.tile); break;
-    case 1024: row_tile<1024, 2, R>(a, w.tile); break;
-    case 2048: row_tile<2048, 1, R>(a, w.tile); break;
-    default: break;
-  }
-}
-
-template <int R>
-__global__ void __launch_bounds__(EnsFam<R>::THREADS, EnsFam<R>::MINB)
-k_ens_colfwd(const NltArgs* __restrict__ args, const EnsTile* __restrict__ tiles) {
-  const EnsTile w = tiles[blockIdx.x];
-  const NltArgs a = args[w.member];
-  switch (a.n) {
-    case 128: colfwd_tile<128, 16, R>(a, w.tile); break;
-    case 256: colfwd_tile<256, 8, R>(a, w.tile); break;
-    case 512: colfwd_tile<512, 4, R>(a, w.tile); break;
-    case 1024: colfwd_tile<1024, 2, R>(a, w.tile); break;
-    case 2048: colfwd_tile<2048, 1, R>(a, w.tile); break;
-    default: break;
-  }
-}
-
-// pass C of stage cur[m] fused with pass A of stage next[m] (same tiles)
-template <int R>
-__global__ void __launch_bounds__(EnsFam<R>::THREADS, EnsFam<R>::MINB)
-k_ens_colfwd_inv(const NltArgs* __restrict__ cur, const NltArgs* __restrict__ next,
-                 const EnsTile* __restrict__ tiles) {
-  const EnsTile w = tiles[blockIdx.x];
-  const NltArgs a = cur[w.member];
-  const NltArgs b = next[w.member];
-  switch (a.n) {
-    case 128: colfwd_colinv_tile<128, 16, R>(a, b, w.tile); break;
-    case 256: colfwd_colinv_tile<256, 8, R>(a, b, w.tile); break;
-    case 512: colfwd_colinv_tile<512, 4, R>(a, b, w.tile); break;
-    case 1024: colfwd_colinv_tile<1024, 2, R>(a, b, w.tile); break;
-    case 2048: colfwd_colinv_tile<2048, 1, R>(a, b, w.tile); break;
-    default: break;
-  }
-}
 
 struct ForceMember {
   double2* z;
@@ -227,36 +154,15 @@ void free_ens(gt_ens* e) {
 
 bool valid_ens_n(int n) { return n >= 128 && n <= 2048 && (n & (n - 1)) == 0; }
 
-// the passes of one step in tile family R
-template <int R>
-void enqueue_passes(gt_ens* e, cudaStream_t s) {
-  constexpr int TH = gt::EnsFam<R>::THREADS;
-  // pass A of stage 0, then per stage: pass B, and pass C fused with the next stage's pass A
-  gt::k_ens_colinv<R><<<e->ncol, TH, gt::kEnsColSmem, s>>>(e->d_args, e->d_col);
-  for (int st = 0; st < e->stages; ++st) {
-    const NltArgs* a = e->d_args + (size_t)st * e->nm;
-    gt::k_ens_row<R><<<e->nrow, TH, gt::kEnsRowSmem, s>>>(a, e->d_row);
-    if (st + 1 < e->stages)
-      gt::k_ens_colfwd_inv<R><<<e->ncol, TH, gt::kEnsColSmem, s>>>(a, a + e->nm, e->d_col);
-    else
-      gt::k_ens_colfwd<R><<<e->ncol, TH, gt::kEnsColSmem, s>>>(a, e->d_col);
-  }
-}
-
-template <int R>
-cudaError_t prepare_family() {
-  const cudaFuncAttribute attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  cudaError_t c = cudaFuncSetAttribute(gt::k_ens_colinv<R>, attr, (int)gt::kEnsColSmem);
-  if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_colfwd<R>, attr, (int)gt::kEnsColSmem);
-  if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_colfwd_inv<R>, attr, (int)gt::kEnsColSmem);
-  if (c == cudaSuccess) c = cudaFuncSetAttribute(gt::k_ens_row<R>, attr, (int)gt::kEnsRowSmem);
-  return c;
+// the launch parameters of one step's passes (gt_ens_kernels.cuh)
+gt::EnsLaunch ens_launch(const gt_ens* e) {
+  return gt::EnsLaunch{e->ncol, e->nrow, e->stages, e->nm, e->d_args, e->d_col, e->d_row};
 }
 
 int enqueue_step(gt_ens* e, cudaStream_t s) {
-  if (e->tile_r == 16) enqueue_passes<16>(e, s);
-  else if (e->tile_r == 4) enqueue_passes<4>(e, s);
-  else enqueue_passes<8>(e, s);
+  if (e->tile_r == 16) gt::ens_passes_r16(ens_launch(e), s);
+  else if (e->tile_r == 4) gt::ens_passes_r4(ens_launch(e), s);
+  else gt::ens_passes_r8(ens_launch(e), s);
   if (e->nmodes > 0)
     gt::k_forcing_philox_ens<<<(e->nmodes + 127) / 128, 128, 0, s>>>(e->d_fm, e->d_modes, e->nmodes,
                                                                     e->d_step, e->d_done);
@@ -342,9 +248,9 @@ int gt_ens_create(const gt_params* members, int32_t nmembers, const uint64_t* ke
   up((void**)&e->d_fm, nullptr, sizeof(ForceMember) * nmembers);
   up((void**)&e->d_step, nullptr, sizeof(uint64_t));
   up((void**)&e->d_done, nullptr, sizeof(unsigned));
-  if (c == cudaSuccess) c = prepare_family<16>();
-  if (c == cudaSuccess) c = prepare_family<8>();
-  if (c == cudaSuccess) c = prepare_family<4>();
+  if (c == cudaSuccess) c = gt::ens_prepare_r16();
+  if (c == cudaSuccess) c = gt::ens_prepare_r8();
+  if (c == cudaSuccess) c = gt::ens_prepare_r4();
   if (c == cudaSuccess) c = cudaStreamCreateWithFlags(&e->own, cudaStreamNonBlocking);
   if (c == cudaSuccess) c = cudaEventCreateWithFlags(&e->ev_in, cudaEventDisableTiming);
   if (c == cudaSuccess) c = cudaEventCreateWithFlags(&e->ev_out, cudaEventDisableTiming);
