@@ -625,7 +625,12 @@ def adjoint_run(torch, rko=2):
     sol.adj_memory = 0
     g = torch.Generator(device="cpu").manual_seed(3)
     dz = torch.randn(z0.shape, generator=g, dtype=torch.float64).cuda() * (z0.abs().max() / 4)
+    torch.cuda.synchronize()
+    e0.record(s)
     _, dJ = tlm_run(sol, z0, dz, 0.0, nsteps, SEED, kmin, kmax)
+    e1.record(s)
+    torch.cuda.synchronize()
+    t_tlm = e0.elapsed_time(e1)
     adj = float((gz * dz).sum().item())
     h = 1e-6
     fd = (forward_objective(sol, z0 + h * dz, nsteps, SEED, kmin, kmax)
@@ -638,6 +643,7 @@ def adjoint_run(torch, rko=2):
             "min_memory": {"segments_kept": 1, "adjoint_forward_sweep_ms": tf0,
                            "adjoint_backward_sweep_ms": tb0,
                            "gradient_over_forward": (tf0 + tb0) / t_fwd},
+            "tlm_ms": t_tlm, "tlm_over_forward": t_tlm / t_fwd,
             "J": J, "J_plain_forward": J_fwd, "dJdfamp": gf,
             "dot_test_rel": abs(adj - dJ) / abs(dJ), "fd_vs_tlm_rel": abs(fd - dJ) / abs(dJ),
             "fd_step": h}
