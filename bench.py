@@ -81,11 +81,16 @@ def run_config(args):
     """The JSON line's `config`, built the same way by both arms from the workload alone (the
     GPU arm's launch settings go to its own `settings` object)."""
     p, _, desc = workload(args.config)
+    # fields of the integrator, the emk and kainv tables (S together), and the q scratch of the
+    # field-split column passes (N <= 2048)
+    s = 16 * p.n * (p.n // 2 + 1)
+    ws = s * ((4 if p.rko == 2 else 5) + 1 + (1 if p.n <= 2048 else 0))
+    l2 = (f"no flush: working set ~{ws / 1e6:.0f} MB > 126 MB L2" if ws > 126e6 else
+          f"no flush: the working set (~{ws / 1e6:.0f} MB) fits in L2 (small grid)")
     return {"workload": desc, "n": p.n, "alpha": p.alpv, "rk": p.rko, "dt": p.dt,
             "imix": p.imix,
             "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single",
-            "l2": "no flush: working set ~202 MB > 126 MB L2" if p.n >= 2048 else
-                  "no flush: the working set fits in L2 (small grid)"}
+            "l2": l2}
 
 
 # ---------------------------------------------------------------------------------------

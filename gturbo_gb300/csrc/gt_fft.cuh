@@ -265,14 +265,28 @@ GT_HD_INL void dft_tw(double2* a, const double2* wl, const double2* lh) {
 // addition absorb those factors as an FMA multiplier. Per thread and butterfly this takes radix 16
 // from 188 to 174 FP64 instructions, radix 8 from 72 to 66 and radix 4 from 24 to 22.
 __host__ __device__ constexpr int lf_entry_doubles(int rp) { return rp == 16 ? 34 : rp == 8 ? 16 : rp == 4 ? 6 : 0; }
-// Offset (in double2) of the radix-rp pass table in the twiddle buffer of a length-n table.
-__host__ __device__ constexpr int lf_table_offset(int rp, int n) {
-  return 2 * n + (rp <= 8 ? (n / 16) * (lf_entry_doubles(16) / 2) : 0) +
-         (rp <= 4 ? (n / 8) * (lf_entry_doubles(8) / 2) : 0);
+// A pass of radix RP that follows passes of total radix Ns (span P = Ns RP) takes the entries of
+// the base angles m = k n / P, i.e. the twiddles W_P^(r k), for k = b mod Ns. Each such pass has a
+// table of its own in the twiddle buffer of a length-n table, for Ns = 2, 4, ..., n / RP, stored
+// field by field: the double2 q of entry k sits at lf_pass_table(RP, n, Ns) + q Ns + k. The
+// threads of a warp hold consecutive k, so each of their loads reads one contiguous run (2–4
+// L1 lines) instead of one line per thread. The entries depend on P alone, so the tables of a
+// length-n buffer also serve the transforms of length n/2 that read it with twshift = 1.
+// Number of double2 of the radix-rp tables (all Ns) of a length-n buffer.
+__host__ __device__ constexpr int lf_section_size(int rp, int n) {
+  return n / rp >= 2 ? (lf_entry_doubles(rp) / 2) * (2 * (n / rp) - 2) : 0;
+}
+// Offset (in double2) of the radix-rp tables: after the n twiddles and their n Linzer-Feig forms.
+__host__ __device__ constexpr int lf_section_offset(int rp, int n) {
+  return 2 * n + (rp <= 8 ? lf_section_size(16, n) : 0) + (rp <= 4 ? lf_section_size(8, n) : 0);
+}
+// Offset (in double2) of the radix-rp table of the pass that follows total radix ns (ns >= 2).
+__host__ __device__ constexpr int lf_pass_table(int rp, int n, int ns) {
+  return lf_section_offset(rp, n) + (lf_entry_doubles(rp) / 2) * (ns - 2);
 }
 // Number of double2 in the whole twiddle buffer of a length-n table.
 __host__ __device__ constexpr int twiddle_buffer_size(int n) {
-  return lf_table_offset(4, n) + (n / 4) * (lf_entry_doubles(4) / 2);
+  return lf_section_offset(4, n) + lf_section_size(4, n);
 }
 
 // The pass-table entry of base angle m (host side): lf[j] = (c_j, t_j), j < n, the Linzer-Feig
@@ -358,7 +372,7 @@ GT_HD_INL void dft_lf(double2* a, const double* e) {
 //   sm  : exchange buffer; element o lives at sm[padix(o) * SS]
 //   tw  : twiddle buffer of a length-n table, n = L << twshift: tw[k] = exp(-2 pi i k / n) and
 //         tw[n + k] = (c, t) with tw[k] = c (1 + i t), k < n, then the pass tables of dft_lf
-//         (lf_table_offset; twiddle_buffer_size(n) double2 in all)
+//         (lf_pass_table; twiddle_buffer_size(n) double2 in all)
 template <int L, int R, int Ns, bool INV, int SS>
 struct StockhamPass {
   static constexpr int RP = (L / Ns >= R) ? R : (L / Ns);
@@ -380,14 +394,12 @@ struct StockhamPass {
         const double2 lh = __ldg(&tw[(L << twshift) + ((k * (L / (Ns * 2))) << twshift)]);
         dft_tw<2, INV>(a, nullptr, &lh);
       } else if constexpr (Ns > 1) {
-        constexpr int E = lf_entry_doubles(RP), STRIDE = L / (Ns * RP);
-        const int n = L << twshift;
-        const double2* __restrict__ ent =
-            tw + lf_table_offset(RP, n) + (size_t)((k * STRIDE) << twshift) * (E / 2);
+        constexpr int E = lf_entry_doubles(RP);
+        const double2* __restrict__ ent = tw + lf_pass_table(RP, L << twshift, Ns) + k;
         double e[E];
 #pragma unroll
         for (int q = 0; q < E / 2; ++q) {
-          const double2 p = __ldg(&ent[q]);
+          const double2 p = __ldg(&ent[q * Ns]);
           e[2 * q] = p.x;
           e[2 * q + 1] = p.y;
         }

@@ -233,7 +233,8 @@ int natural_row_variant(int v) { return v; }
 
 // The twiddle buffer of the FFT passes (gt_fft.cuh): exp(-2 pi i k / n) for k in [0, n), each
 // value from an argument reduced to [0, pi/4]; then the Linzer-Feig forms tw[n + k] = (c, t) with
-// tw[k] = c (1 + i t); then the radix-16, 8 and 4 pass tables built from those (make_lf_entry).
+// tw[k] = c (1 + i t); then the radix-16, 8 and 4 pass tables built from those (make_lf_entry),
+// one per pass span, field by field (lf_pass_table).
 // c = Re tw[k], except at k = n/4 and 3n/4 (Re tw[k] = 0), where c = 2^-60 and
 // t = Im tw[k] / c = -+2^60: c t is exact and Re(c (1 + i t)) = 2^-60 is far below the rounding
 // of the other entries.
@@ -268,8 +269,14 @@ void make_twiddles(int n, std::vector<double2>& tw) {
   auto fill = [&](auto rp_tag) {
     constexpr int RP = decltype(rp_tag)::value;
     constexpr int E = gt::lf_entry_doubles(RP);
-    double* base = reinterpret_cast<double*>(tw.data() + gt::lf_table_offset(RP, n));
-    for (int m = 0; m < n / RP; ++m) gt::make_lf_entry<RP>(lf, n, m, base + (size_t)m * E);
+    double e[E];
+    for (int ns = 2; ns <= n / RP; ns *= 2) {
+      double2* tab = tw.data() + gt::lf_pass_table(RP, n, ns);
+      for (int k = 0; k < ns; ++k) {
+        gt::make_lf_entry<RP>(lf, n, k * (n / (ns * RP)), e);
+        for (int q = 0; q < E / 2; ++q) tab[(size_t)q * ns + k] = make_double2(e[2 * q], e[2 * q + 1]);
+      }
+    }
   };
   fill(std::integral_constant<int, 16>());
   fill(std::integral_constant<int, 8>());
