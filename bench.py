@@ -62,7 +62,7 @@ def parse():
                     help="launch the pass kernels without programmatic dependent launch")
     ap.add_argument("--adjoint-rk", type=int, choices=[2, 4], default=2,
                     help="integrator of the --only adjoint leg (the bench's own leg is RK2)")
-    ap.add_argument("--only", choices=["ensemble", "adjoint"], default=None,
+    ap.add_argument("--only", choices=["ensemble", "adjoint", "next"], default=None,
                     help="run one secondary leg alone and print its JSON object (profiling)")
     return ap.parse_args()
 
@@ -540,6 +540,12 @@ def ours_arm(args):
             except Exception as e:
                 extras["adjoint"] = {"unavailable": str(e)[:300]}
 
+            # ---- dumps and restarts, the split integrator, a non-square grid ------------
+            try:
+                extras["next_rows"] = next_rows_run(torch, fp64)
+            except Exception as e:
+                extras["next_rows"] = {"unavailable": str(e)[:300]}
+
             # ---- CPU baseline: the reference's statements on the host cores (the oracle
             # port where they are absent), and the oracle port beside it --------------------
             try:
@@ -582,6 +588,175 @@ def ours_arm(args):
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def step_flops(p):
+    """FFT-convention FLOPs of the transforms one RK step of an NX x NY grid runs: per nonlinear
+    term 5 column transforms of length NY over the columns up to the 2/3 cut (kx <= rtrunc NX/2;
+    the others hold no retained mode and are not transformed) and 5 real row transforms of
+    length NX over the NY rows."""
+    nx, ny = p.n, p.rows
+    cols = int(p.rtrunc * (nx // 2) + 1e-9) + 1
+    per_nlt = 5 * cols * 5 * ny * math.log2(ny) + 5 * ny * 2.5 * nx * math.log2(nx)
+    return (4 if p.rko == 4 else 2) * per_nlt
+
+
+def _gpu_rate(sol, z, steps, torch):
+    """Main-loop steps/s (forced, no diagnostics) of sol on z, CUDA events on its stream."""
+    work = sol.work()
+    seed = SEED
+    for _ in range(3):
+        seed, _ = sol.main_step(z, seed, work)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(sol.stream)
+    for _ in range(steps):
+        seed, _ = sol.main_step(z, seed, work)
+    e1.record(sol.stream)
+    torch.cuda.synchronize()
+    assert bool(torch.isfinite(z).all().item())
+    return steps / (e0.elapsed_time(e1) / 1e3)
+
+
+def _cpu_ref_rate(p, z, budget_s):
+    """Main-loop steps/s of the reference's statements (oracle/_ref, all host cores) on z."""
+    import numpy as np
+
+    from oracle import refcore
+
+    if not refcore.available():
+        return None
+    ref = refcore.Reference(p)
+    z = np.array(z, copy=True)
+    work = [ref.zeros() for _ in range(4)]
+    t0 = time.perf_counter()
+    seed, _ = ref.main_step(z, SEED, 1, 10 ** 9, work)
+    k = max(1, int(budget_s / max(time.perf_counter() - t0, 1e-6)))
+    t0 = time.perf_counter()
+    for ipas in range(2, k + 2):
+        seed, _ = ref.main_step(z, seed, ipas, 10 ** 9, work)
+    dt = time.perf_counter() - t0
+    return {"value": k / dt, "unit": "steps/s", "cores": ref.threads, "steps": k, "kind": "reference"}
+
+
+def next_rows_run(torch, fp64_tflops, cpu_budget_s=4.0):
+    """The paths beside the main-loop step, each timed on the GPU against the FP64 roofline of
+    its transforms and beside the reference's statements on the host cores (oracle/_ref):
+      * dump and restart at 2048^2: gt_dump_real4 (inverse 2D transform with the real(4)
+        conversion of src/write.f90:29-51 fused into its row pass, then the N x N floats to the
+        host) and gt_load_real4 (the floats to the device, widening fused into the forward
+        transform, trunc: src/read.f90 + src/main.f90:89-92), against the reference's
+        fft_inv / fft_dir of the same field;
+      * the split integrator emkx(i) emky(j) (src/rkstep.f90:21-27, 51-57) at 2048^2, RK2,
+        alpha=2 with Laplacian viscosity and linear drag, against the emk table on the same run;
+      * a non-square 4096 x 2048 (NX x NY) grid, the c2 workload's alpha=1 RK2 step."""
+    import numpy as np
+
+    from gturbo_gb300.ic import random_phase_ic
+    from gturbo_gb300.params import IC_K0, config
+    from gturbo_gb300.solver import Solver
+    from oracle import refcore
+
+    out = {}
+    dev = torch.device("cuda", torch.cuda.current_device())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    # ---- dump and restart -----------------------------------------------------------------
+    p = config("c2")
+    n = p.n
+    sol = Solver(p)
+    z = torch.from_numpy(random_phase_ic(p, IC_K0["c2"], 0.5, seed=1)).to(dev)
+    fl2d = (n // 2 + 1) * 5 * n * math.log2(n) + n * 2.5 * n * math.log2(n)
+    work = z.clone()
+    wdev = torch.empty((n, n), dtype=torch.float32, device=dev)
+    zr = sol.field()
+    reps = 20
+    t_dump = t_load = 0.0
+    for it in range(reps + 2):  # device time of the kernels of one call (first two: warm-up)
+        work.copy_(z)
+        e0.record(sol.stream)
+        sol._check(sol.lib.gt_dump_real4(sol.h, sol._ptr(work), wdev.data_ptr()))
+        e1.record(sol.stream)
+        torch.cuda.synchronize()
+        t_dump += e0.elapsed_time(e1) if it >= 2 else 0.0
+        e0.record(sol.stream)
+        sol._check(sol.lib.gt_load_real4(sol.h, wdev.data_ptr(), sol._ptr(zr)))
+        e1.record(sol.stream)
+        torch.cuda.synchronize()
+        t_load += e0.elapsed_time(e1) if it >= 2 else 0.0
+    t_dump, t_load = t_dump / reps, t_load / reps
+    w = sol.dump_real4(z)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        w = sol.dump_real4(z)
+    t_dump_e2e = (time.perf_counter() - t0) / reps * 1e3
+    sol.load_real4(w, zr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sol.load_real4(w, zr)
+    torch.cuda.synchronize()
+    t_load_e2e = (time.perf_counter() - t0) / reps * 1e3
+    dump = {"grid": f"{n}^2", "dump_ms": t_dump, "restart_ms": t_load,
+            "dump_e2e_ms": t_dump_e2e, "restart_e2e_ms": t_load_e2e,
+            "e2e_note": "Solver.dump_real4 / load_real4 from and to pageable host numpy arrays "
+                        f"({n * n * 4} bytes of real(4) per call), host wall clock",
+            "transform_tflops": {"dump": fl2d / (t_dump / 1e3) / 1e12,
+                                 "restart": fl2d / (t_load / 1e3) / 1e12,
+                                 "peak": fp64_tflops, "unit": "TFLOP/s (FFT convention)"}}
+    try:
+        if refcore.available():
+            ref = refcore.Reference(p)
+            a = z.cpu().numpy()
+            for name in ("fft_inv", "fft_dir"):
+                b = a.copy()
+                t0 = time.perf_counter()
+                getattr(ref, name)(b)
+                k = max(1, int(cpu_budget_s / 2 / max(time.perf_counter() - t0, 1e-6)))
+                t0 = time.perf_counter()
+                for _ in range(k):
+                    b[:] = a
+                    getattr(ref, name)(b)
+                dump["reference_" + name + "_ms"] = (time.perf_counter() - t0) / k * 1e3
+            dump["reference_cores"] = ref.threads
+    except Exception as e:
+        dump["reference"] = {"unavailable": str(e)[:200]}
+    out["dump_restart"] = dump
+    sol.close()
+    del work, wdev, zr
+
+    # ---- split integrator -------------------------------------------------------------------
+    pe = config("c2").replace(alpv=2.0, alpnu=1.0, nu=1e-5, alpmu=0.0, mu=0.1)
+    ze = random_phase_ic(pe, IC_K0["c2"], 0.5, seed=2)
+    rates = {}
+    for split in (1, 0):
+        s2 = Solver(pe.replace(split=split))
+        rates[split] = _gpu_rate(s2, torch.from_numpy(ze).to(dev), 100, torch)
+        s2.close()
+    split_row = {"grid": f"{n}^2 RK2, alpha=2, nu k^2, mu (Ekman-NS)",
+                 "split_steps_s": rates[1], "table_steps_s": rates[0],
+                 "split_tflops": step_flops(pe) * rates[1] / 1e12, "peak": fp64_tflops}
+    try:
+        split_row["cpu_reference"] = _cpu_ref_rate(pe, ze, cpu_budget_s)
+    except Exception as e:
+        split_row["cpu_reference"] = {"unavailable": str(e)[:200]}
+    out["split_integrator"] = split_row
+
+    # ---- non-square grid ----------------------------------------------------------------------
+    pn = config("c2").replace(n=2 * n, ny=n)
+    zn = random_phase_ic(pn, IC_K0["c2"], 0.5, seed=3)
+    s3 = Solver(pn)
+    r = _gpu_rate(s3, torch.from_numpy(zn).to(dev), 50, torch)
+    s3.close()
+    ns_row = {"grid": f"{pn.n} x {pn.rows} (NX x NY), alpha=1 RK2 (the c2 step)", "steps_s": r,
+              "tflops": step_flops(pn) * r / 1e12, "peak": fp64_tflops,
+              "square_2048_step_flops_ratio": step_flops(pn) / step_flops(p)}
+    try:
+        ns_row["cpu_reference"] = _cpu_ref_rate(pn, zn, cpu_budget_s)
+    except Exception as e:
+        ns_row["cpu_reference"] = {"unavailable": str(e)[:200]}
+    out["non_square"] = ns_row
+    return out
 
 
 # Device memory the adjoint leg lets the gradient hold for whole kept segments (gt_adj_set_memory):
@@ -781,6 +956,8 @@ def main():
             res = ensemble_run(args.steps, max(3, args.warmup), torch, shard=world > 1, pdl=not args.no_pdl)
             if world > 1:
                 dist.destroy_process_group()
+        elif rank == 0 and args.only == "next":
+            res = next_rows_run(torch, fp64_gemm_tflops(torch, torch.device("cuda", torch.cuda.current_device())))
         elif rank == 0:
             res = adjoint_run(torch, args.adjoint_rk)
         else:

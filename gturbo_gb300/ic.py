@@ -19,11 +19,12 @@ from .params import TWO_PI, Params
 
 
 def wavenumbers(p: Params):
-    n = p.n
+    """fkx over the NX/2+1 columns and fky over the NY rows (src/defk.f90:18-30)."""
+    n, ny = p.n, p.rows
     dkx, dky = TWO_PI / p.xlx, TWO_PI / p.xly
     fkx = np.arange(n // 2 + 1) * dkx
-    j = np.arange(n)
-    fky = np.where(j <= n // 2, j, j - n) * dky
+    j = np.arange(ny)
+    fky = np.where(j <= ny // 2, j, j - ny) * dky
     return fkx, fky
 
 
@@ -31,13 +32,12 @@ def trunc_mask(p: Params) -> np.ndarray:
     """True where src/trunc.f90:10-20 zeroes a mode (same arithmetic order)."""
     fkx, fky = wavenumbers(p)
     fkxs, fkys = fkx * fkx, fky * fky
-    n = p.n
-    k1 = fkys / fkys[n // 2]
-    return (k1[:, None] + (fkxs / fkxs[n // 2])[None, :]) > p.rtrunc * p.rtrunc
+    k1 = fkys / fkys[p.rows // 2]
+    return (k1[:, None] + (fkxs / fkxs[p.n // 2])[None, :]) > p.rtrunc * p.rtrunc
 
 
 def energy(p: Params, zk: np.ndarray) -> float:
-    """The reference's global energy ee of a spectral field (N, N/2+1) complex."""
+    """The reference's global energy ee of a spectral field (NY, NX/2+1) complex."""
     fkx, fky = wavenumbers(p)
     k2 = fky[:, None] ** 2 + fkx[None, :] ** 2
     k2[0, 0] = 1.0
@@ -50,13 +50,13 @@ def energy(p: Params, zk: np.ndarray) -> float:
 
 
 def random_phase_ic(p: Params, k0: float, e0: float = 0.5, seed: int = 1) -> np.ndarray:
-    """Spectral initial field q_hat as an (N, N+2) float64 array (the ABI's memory layout)."""
-    n, nh = p.n, p.n // 2 + 1
+    """Spectral initial field q_hat as an (NY, NX+2) float64 array (the ABI's memory layout)."""
+    n, ny, nh = p.n, p.rows, p.n // 2 + 1
     fkx, fky = wavenumbers(p)
     k2 = fky[:, None] ** 2 + fkx[None, :] ** 2
     k = np.sqrt(k2)
     rng = np.random.default_rng(seed)
-    theta = rng.uniform(0.0, 2.0 * np.pi, size=(n, nh))
+    theta = rng.uniform(0.0, 2.0 * np.pi, size=(ny, nh))
     with np.errstate(divide="ignore", invalid="ignore"):
         ek = k ** 4 * np.exp(-(k / k0) ** 2)
         # per-mode |q|^2 so that a shell of ~pi k half-plane modes carries E(k): |q|^2 / k^alpha
@@ -64,16 +64,16 @@ def random_phase_ic(p: Params, k0: float, e0: float = 0.5, seed: int = 1) -> np.
     zk = np.sqrt(amp2) * np.exp(1j * theta)
     # Hermitian symmetry on the kx=0 and Nyquist columns: q(-ky) = conj q(ky)
     for col in (0, nh - 1):
-        zk[n // 2 + 1:, col] = np.conj(zk[1:n // 2, col][::-1])
+        zk[ny // 2 + 1:, col] = np.conj(zk[1:ny // 2, col][::-1])
         zk[0, col] = zk[0, col].real
-        zk[n // 2, col] = zk[n // 2, col].real
+        zk[ny // 2, col] = zk[ny // 2, col].real
     zk[0, 0] = 0.0
     if p.truncate == 1:
         zk[trunc_mask(p)] = 0.0
     e = energy(p, zk)
     if e > 0.0:
         zk *= np.sqrt(e0 / e)
-    out = np.ascontiguousarray(zk.astype(np.complex128)).view(np.float64).reshape(n, n + 2)
+    out = np.ascontiguousarray(zk.astype(np.complex128)).view(np.float64).reshape(ny, n + 2)
     return out.copy()
 
 

@@ -24,6 +24,25 @@ def test_ic_energy_symmetry_truncation(cfg, k0):
     assert not np.array_equal(a, random_phase_ic(p, k0, 0.5, seed=2))
 
 
+@pytest.mark.parametrize("nx,ny", [(128, 64), (64, 256)])
+def test_ic_non_square(nx, ny):
+    """NX x NY grids: the field is (NY, NX+2), carries E = 0.5 by the oracle's budgets, is
+    truncated as the oracle's trunc truncates it, and is Hermitian on the kx=0 and Nyquist
+    columns."""
+    p = Params(n=nx, ny=ny, alpv=1.0)
+    a = random_phase_ic(p, 6.0, 0.5, seed=4)
+    assert a.shape == (ny, nx + 2)
+    s = spec(a)
+    orc = Oracle(p)
+    assert orc.diag(a)["glob"][0] == pytest.approx(0.5, rel=1e-12)
+    b = a.copy()
+    orc.trunc(b)
+    assert np.array_equal(a, b)
+    assert np.all(s[trunc_mask(p)] == 0) and s[0, 0] == 0
+    for col in (0, nx // 2):
+        assert np.allclose(s[ny // 2 + 1:, col], np.conj(s[1:ny // 2, col][::-1]))
+
+
 def test_ic_spectrum_shape():
     p = config("c1")
     a = random_phase_ic(p, 5.0, 0.5, seed=3)
