@@ -164,6 +164,38 @@ def test_main_loop_horizon_against_reference(p):
 
 
 @needs_ref
+@pytest.mark.parametrize("cfg,steps", [("c1", 6), ("c5", 3), ("c2", 3)])
+def test_workload_configurations_against_reference(cfg, steps):
+    """The benchmark workloads' own configurations (256^2 RK4; 1024^2 and 2048^2 alpha=1 RK2),
+    from their random-phase initial fields: main-loop iterations with the diagnostics every
+    second one, the state to 1e-12 and the spectra to 1e-9 against the reference's statements,
+    the LCG seed exactly, and the tables, mode list and forcing inputs bit for bit."""
+    from gturbo_gb300.ic import random_phase_ic
+    from gturbo_gb300.params import IC_K0, config
+
+    p = config(cfg)
+    r, o = refcore.Reference(p), Oracle(p)
+    assert np.array_equal(r.tables()["emk"], o.emk())
+    ik, jk = r.forcing_modes()
+    ik2, jk2 = o.forcing_modes()
+    assert np.array_equal(ik, ik2) and np.array_equal(jk, jk2)
+    info = r.info()
+    assert info["nf"] == o.info.nf and info["inpe"] == o.info.inpe and info["inpz"] == o.info.inpz
+    z1 = random_phase_ic(p, IC_K0[cfg], 0.5, seed=1)
+    z2 = z1.copy()
+    s1 = s2 = 481929
+    work = [o.zeros() for _ in range(4)]
+    for ipas in range(1, steps + 1):
+        s1, d1 = r.main_step(z1, s1, ipas, 2)
+        s2, d2 = o.main_step(z2, s2, diag=(ipas % 2 == 0), work=work)
+        assert s1 == s2
+        if d1 is not None:
+            for k in ("sp", "sz", "fle", "flz"):
+                assert np.abs(d1[k] - d2[k]).max() <= 1e-9 * np.abs(d2[k]).max(), k
+    assert rel_l2(z1, z2) < 1e-12
+
+
+@needs_ref
 def test_restart_files_round_trip_through_reference():
     """writef2 then readf (write.f90:29-51, read.f90:3-27): the real(4) record of the dump and its
     widened restart, against the oracle's fft_inv rounded to real(4)."""
