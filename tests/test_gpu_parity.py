@@ -3,6 +3,8 @@
 Tolerance: relative L2 <= 1e-12 (the single-step bound of the specification); integer and
 mask work (trunc, forcing's LCG state, forced-mode table) must match exactly.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -412,6 +414,26 @@ def test_step_large_grids(n, rko):
     z = _dev(a)
     sol.rk_step(z, sol.work())
     assert rel_l2(_host(z), ref) < TOL
+
+
+def test_headline_workload_against_reference_fixture():
+    """The headline workload (2048^2, alpha=1, RK2, the reference's forcing and seed, from its
+    random-phase initial field) against the reference's own run of it: tests/golden/c2_workload.npz,
+    made by the transliterated reference (make_golden.make_workload). Main-loop iterations with the
+    fused kick, diagnostics on every second one; seed, spectra, budgets and sampled modes."""
+    from gturbo_gb300.ic import random_phase_ic
+    from gturbo_gb300.params import IC_K0, config
+    from tests.golden import make_golden as m
+    from tests.helpers import check_workload_fixture, workload_run
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{m.WORKLOAD}_workload.npz"))
+    p = config(m.WORKLOAD)
+    sol = _solver(p)
+    z = _dev(random_phase_ic(p, IC_K0[m.WORKLOAD], 0.5, seed=1))
+    work = sol.work()
+    seed, spectra, globs = workload_run(lambda zz, s, ipas, dg: sol.main_step(zz, s, work, diag=dg), z,
+                                        m.WORKLOAD_STEPS, m.WORKLOAD_IMIX)
+    check_workload_fixture(g, _host(z), seed, spectra, globs)
 
 
 def test_step_2048_rk2_headline():

@@ -18,7 +18,7 @@ import pytest
 from gturbo_gb300.params import Params
 from oracle import refcore
 from oracle.coracle import Oracle, spec
-from tests.helpers import rand_field, rel_l2
+from tests.helpers import check_workload_fixture, rand_field, rel_l2, workload_run
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 needs_ref = pytest.mark.skipif(not refcore.available(), reason="reference sources not present")
@@ -260,3 +260,36 @@ def test_oracle_main_loop_against_golden_horizon(name):
     for k in range(4):
         assert np.abs(got[:, k] - ref[:, k]).max() <= 1e-9 * np.abs(ref[:, k]).max()
     assert np.array_equal(o.emk(), g["emk"])
+
+
+@needs_ref
+def test_workload_fixture_is_the_reference(tmp_path, monkeypatch):
+    """The committed headline-workload fixture equals a fresh computation by the reference."""
+    from tests.golden import make_golden
+
+    monkeypatch.setattr(make_golden, "OUT", str(tmp_path))
+    make_golden.make_workload()
+    fresh = np.load(tmp_path / f"{make_golden.WORKLOAD}_workload.npz")
+    g = np.load(os.path.join(GOLDEN, f"{make_golden.WORKLOAD}_workload.npz"))
+    assert sorted(fresh.files) == sorted(g.files)
+    for k in g.files:
+        assert np.array_equal(fresh[k], g[k]), k
+
+
+def test_oracle_against_workload_fixture():
+    """The C oracle runs the headline workload (2048^2, alpha=1, RK2, from its random-phase
+    initial field) as the reference did for the fixture."""
+    from gturbo_gb300.ic import random_phase_ic
+    from gturbo_gb300.params import IC_K0, config
+    from tests.golden import make_golden as m
+
+    g = np.load(os.path.join(GOLDEN, f"{m.WORKLOAD}_workload.npz"))
+    p = config(m.WORKLOAD)
+    o = Oracle(p)
+    z = random_phase_ic(p, IC_K0[m.WORKLOAD], 0.5, seed=1)
+    assert np.array_equal(m.workload_mode_index(p, z), g["mode_index"])
+    work = [o.zeros() for _ in range(4)]
+    seed, spectra, globs = workload_run(
+        lambda zz, s, ipas, dg: o.main_step(zz, s, diag=dg, work=work), z, m.WORKLOAD_STEPS,
+        m.WORKLOAD_IMIX)
+    check_workload_fixture(g, z, seed, spectra, globs)
