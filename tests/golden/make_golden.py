@@ -105,11 +105,12 @@ def make_case(name, p, seed):
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
 
 
-# the headline workload (2048^2, alpha=1, RK2, the reference's forcing and seed) from its own
-# random-phase initial field: WORKLOAD_STEPS main-loop iterations, diagnostics every
-# WORKLOAD_IMIX; the field itself (67 MB) is summarised by sampled retained modes and a checksum
-WORKLOAD = "c2"
-WORKLOAD_STEPS = 3
+# the benchmark workloads from their own random-phase initial fields (the reference's forcing and
+# seed): steps main-loop iterations each, diagnostics every WORKLOAD_IMIX; a field is summarised by
+# sampled retained modes and a checksum (a 2048^2 field is 67 MB)
+WORKLOADS = {"c1": 4, "c5": 3, "c2": 3, "c3": 2}  # name: main-loop iterations
+WORKLOAD = "c2"  # the headline
+WORKLOAD_STEPS = WORKLOADS[WORKLOAD]
 WORKLOAD_IMIX = 2
 WORKLOAD_MODES = 512
 
@@ -123,26 +124,26 @@ def workload_mode_index(p, z):
     return np.sort(np.random.default_rng(7).choice(nz, WORKLOAD_MODES, replace=False))
 
 
-def make_workload():
+def make_workload(cfg=WORKLOAD):
     from gturbo_gb300.ic import random_phase_ic
     from gturbo_gb300.params import IC_K0, config
     from oracle.coracle import spec
     from oracle.refcore import Reference
 
-    p = config(WORKLOAD)
+    p = config(cfg)
     r = Reference(p)
-    z = random_phase_ic(p, IC_K0[WORKLOAD], 0.5, seed=1)
+    z = random_phase_ic(p, IC_K0[cfg], 0.5, seed=1)
     idx = workload_mode_index(p, z)
     work = [r.zeros() for _ in range(4)]
     s = 481929
     spectra, globs = [], []
-    for ipas in range(1, WORKLOAD_STEPS + 1):
+    for ipas in range(1, WORKLOADS[cfg] + 1):
         s, d = r.main_step(z, s, ipas, WORKLOAD_IMIX, work)
         if d is not None:
             spectra.append(np.stack([d["sp"], d["sz"], d["fle"], d["flz"]]))
             globs.append(d["glob"])
     zc = spec(z).ravel()
-    np.savez_compressed(os.path.join(OUT, f"{WORKLOAD}_workload.npz"), mode_index=idx,
+    np.savez_compressed(os.path.join(OUT, f"{cfg}_workload.npz"), mode_index=idx,
                         modes=zc[idx], sum_abs2=np.array([float(np.sum(np.abs(zc) ** 2))]),
                         seed=np.array([s], np.int64), spectra=np.stack(spectra),
                         glob=np.stack(globs))
@@ -170,5 +171,6 @@ if __name__ == "__main__":
     for name, (p, seed) in CASES.items():
         make_case(name, p, seed)
     make_lcg()
-    make_workload()
+    for cfg in WORKLOADS:
+        make_workload(cfg)
     print("written:", sorted(f for f in os.listdir(OUT) if f.endswith(".npz")))

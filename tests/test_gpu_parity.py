@@ -416,23 +416,25 @@ def test_step_large_grids(n, rko):
     assert rel_l2(_host(z), ref) < TOL
 
 
-def test_headline_workload_against_reference_fixture():
-    """The headline workload (2048^2, alpha=1, RK2, the reference's forcing and seed, from its
-    random-phase initial field) against the reference's own run of it: tests/golden/c2_workload.npz,
-    made by the transliterated reference (make_golden.make_workload). Main-loop iterations with the
-    fused kick, diagnostics on every second one; seed, spectra, budgets and sampled modes."""
+@pytest.mark.parametrize("cfg", ["c1", "c5", "c2", "c3"])
+def test_workload_against_reference_fixture(cfg):
+    """Each benchmark workload (256^2 RK4, 1024^2 and the 2048^2 headline RK2, 8192^2 RK4; the
+    reference's forcing and seed, from the workload's random-phase initial field) against the
+    reference's own run of it: tests/golden/<cfg>_workload.npz, made by the transliterated
+    reference (make_golden.make_workload). Main-loop iterations with the fused kick, diagnostics
+    on every second one; seed, spectra, budgets and sampled modes."""
     from gturbo_gb300.ic import random_phase_ic
     from gturbo_gb300.params import IC_K0, config
     from tests.golden import make_golden as m
     from tests.helpers import check_workload_fixture, workload_run
 
-    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{m.WORKLOAD}_workload.npz"))
-    p = config(m.WORKLOAD)
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{cfg}_workload.npz"))
+    p = config(cfg)
     sol = _solver(p)
-    z = _dev(random_phase_ic(p, IC_K0[m.WORKLOAD], 0.5, seed=1))
+    z = _dev(random_phase_ic(p, IC_K0[cfg], 0.5, seed=1))
     work = sol.work()
     seed, spectra, globs = workload_run(lambda zz, s, ipas, dg: sol.main_step(zz, s, work, diag=dg), z,
-                                        m.WORKLOAD_STEPS, m.WORKLOAD_IMIX)
+                                        m.WORKLOADS[cfg], m.WORKLOAD_IMIX)
     check_workload_fixture(g, _host(z), seed, spectra, globs)
 
 

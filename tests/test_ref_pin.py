@@ -262,34 +262,39 @@ def test_oracle_main_loop_against_golden_horizon(name):
     assert np.array_equal(o.emk(), g["emk"])
 
 
+WORKLOADS = ["c1", "c5", "c2", "c3"]
+
+
 @needs_ref
-def test_workload_fixture_is_the_reference(tmp_path, monkeypatch):
-    """The committed headline-workload fixture equals a fresh computation by the reference."""
+@pytest.mark.parametrize("cfg", WORKLOADS)
+def test_workload_fixture_is_the_reference(cfg, tmp_path, monkeypatch):
+    """The committed workload fixtures equal a fresh computation by the reference."""
     from tests.golden import make_golden
 
     monkeypatch.setattr(make_golden, "OUT", str(tmp_path))
-    make_golden.make_workload()
-    fresh = np.load(tmp_path / f"{make_golden.WORKLOAD}_workload.npz")
-    g = np.load(os.path.join(GOLDEN, f"{make_golden.WORKLOAD}_workload.npz"))
+    make_golden.make_workload(cfg)
+    fresh = np.load(tmp_path / f"{cfg}_workload.npz")
+    g = np.load(os.path.join(GOLDEN, f"{cfg}_workload.npz"))
     assert sorted(fresh.files) == sorted(g.files)
     for k in g.files:
         assert np.array_equal(fresh[k], g[k]), k
 
 
-def test_oracle_against_workload_fixture():
-    """The C oracle runs the headline workload (2048^2, alpha=1, RK2, from its random-phase
-    initial field) as the reference did for the fixture."""
+@pytest.mark.parametrize("cfg", WORKLOADS)
+def test_oracle_against_workload_fixture(cfg):
+    """The C oracle runs each benchmark workload (from its random-phase initial field) as the
+    reference did for the fixture."""
     from gturbo_gb300.ic import random_phase_ic
     from gturbo_gb300.params import IC_K0, config
     from tests.golden import make_golden as m
 
-    g = np.load(os.path.join(GOLDEN, f"{m.WORKLOAD}_workload.npz"))
-    p = config(m.WORKLOAD)
+    g = np.load(os.path.join(GOLDEN, f"{cfg}_workload.npz"))
+    p = config(cfg)
     o = Oracle(p)
-    z = random_phase_ic(p, IC_K0[m.WORKLOAD], 0.5, seed=1)
+    z = random_phase_ic(p, IC_K0[cfg], 0.5, seed=1)
     assert np.array_equal(m.workload_mode_index(p, z), g["mode_index"])
     work = [o.zeros() for _ in range(4)]
     seed, spectra, globs = workload_run(
-        lambda zz, s, ipas, dg: o.main_step(zz, s, diag=dg, work=work), z, m.WORKLOAD_STEPS,
+        lambda zz, s, ipas, dg: o.main_step(zz, s, diag=dg, work=work), z, m.WORKLOADS[cfg],
         m.WORKLOAD_IMIX)
     check_workload_fixture(g, z, seed, spectra, globs)
