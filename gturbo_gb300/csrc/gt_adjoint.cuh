@@ -884,7 +884,7 @@ struct AdjVar {
   using W = Var<N, V>;
   static constexpr size_t TLM_ROW_SMEM = (size_t)3 * padded(N) * W::ROWS * sizeof(double2);
   static constexpr size_t ADJ_ROW_SMEM = (size_t)(2 * padded(N) + padded(N / 2)) * W::ROWS * sizeof(double2);
-  static constexpr bool OK = W::OK && !W::GROUPED && AdjShape<N>::OK;
+  static constexpr bool OK = W::OK && !W::GROUPED && V != 5 && AdjShape<N>::OK;  // 5: the tiles of 2
 };
 
 template <int N, int V>
@@ -921,7 +921,7 @@ __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_adjv_colfwd(AdjArgs 
 // the field-split transposed column passes (variants with one column per CTA, no groups)
 template <int N, int V>
 struct AdjSplitVar {
-  static constexpr bool OK = SplitVar<N, V>::OK && AdjShape<N>::OK;
+  static constexpr bool OK = SplitVar<N, V>::OK && V != 5 && AdjShape<N>::OK;
 };
 template <int N, int V>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_tlm_colinv_fs(TlmArgs a) {

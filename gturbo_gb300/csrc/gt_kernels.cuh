@@ -944,17 +944,21 @@ k_nlt_colfwd_inv(NltArgs cur, NltArgs next) {
 //        latency-bound regime where a pass leaves most SMs idle);
 // V = 3: R = 4,  grouped tiles: a column's transforms side by side in 3 thread groups, a row's
 //        u + i v and q transforms side by side in 2;
-// V = 4: R = 8,  grouped tiles.
+// V = 4: R = 8,  grouped tiles;
+// V = 5: CR = 2 in the column passes (one column per CTA with twice the threads of V = 2, for
+//        grids whose column passes have fewer warps than the SMs have sub-partitions); it has
+//        no row form (the row pass's half-length q transform needs R >= 4).
 // The row pass and the column passes take their variants separately (GtOp::row_variant).
 template <int N, int V>
 struct Var {
-  static constexpr bool GROUPED = V >= 3;
+  static constexpr bool GROUPED = V == 3 || V == 4;
   static constexpr int R = V == 0 ? 16 : (V == 1 || V == 4) ? 8 : 4;
+  static constexpr int CR = V == 5 ? 2 : R;  // values per thread of the column passes
   static constexpr int T = N / R;
   static constexpr int NH = N / 2 + 1;
   static constexpr int COLS = V == 0 ? Shape<N>::COLS : 1;
   static constexpr int ROWS = V == 0 ? Shape<N>::ROWS : 1;
-  static constexpr int COL_THREADS = (GROUPED ? kColGroups : COLS) * T;
+  static constexpr int COL_THREADS = GROUPED ? kColGroups * T : COLS * (N / CR);
   static constexpr int ROW_THREADS = (GROUPED ? 2 : ROWS) * T;
   static constexpr int COL_CTAS = (NH + COLS - 1) / COLS;
   static constexpr int ROW_CTAS = N / ROWS;
@@ -962,7 +966,8 @@ struct Var {
   // grouped rows: two length-N exchange buffers (u + i v and q)
   static constexpr size_t ROW_SMEM = GROUPED ? (size_t)2 * padded(N) * sizeof(double2)
                                              : (size_t)(padded(N) + padded(N / 2)) * ROWS * sizeof(double2);
-  static constexpr bool OK = V == 0 || (V == 1 && N <= 4096) || (V >= 2 && V <= 4 && N <= 1024);
+  static constexpr bool OK = V == 0 || (V == 1 && N <= 4096) || (V >= 2 && V <= 4 && N <= 1024) ||
+                              (V == 5 && N >= 32 && N <= 512);
 };
 
 // RT = true: the column count at run time (non-square grids; ungrouped variants only)
@@ -970,7 +975,7 @@ template <int N, int V, bool RT = false>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colinv(NltArgs a) {
   pdl_enter();
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colinv_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
-  else if constexpr (Var<N, V>::OK) colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R, RT>(a, blockIdx.x);
+  else if constexpr (Var<N, V>::OK) colinv_tile<N, Var<N, V>::COLS, Var<N, V>::CR, RT>(a, blockIdx.x);
 }
 // Without a CTA count ptxas keeps the 8-value row kernels at 76-80 registers (3 CTAs per SM);
 // an explicit count of 1 lets them grow to 164. GT_VROW_MINB sets a count for the 8-value rows
@@ -990,7 +995,7 @@ template <int N, int V, bool RT = false>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd(NltArgs a) {
   pdl_enter();
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) colfwd_grp_tile<N, Var<N, V>::R, true>(a, blockIdx.x);
-  else if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::R, true, RT>(a, blockIdx.x);
+  else if constexpr (Var<N, V>::OK) colfwd_tile<N, Var<N, V>::COLS, Var<N, V>::CR, true, RT>(a, blockIdx.x);
 }
 template <int N, int V, bool RT = false>
 __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltArgs cur, NltArgs next) {
@@ -998,7 +1003,7 @@ __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltA
   if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED)
     colfwd_colinv_grp_tile<N, Var<N, V>::R>(cur, next, blockIdx.x);
   else if constexpr (Var<N, V>::OK)
-    colfwd_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::R, RT>(cur, next, blockIdx.x);
+    colfwd_colinv_tile<N, Var<N, V>::COLS, Var<N, V>::CR, RT>(cur, next, blockIdx.x);
 }
 
 // Field-split column kernels (variants with one column per CTA and no thread groups).
@@ -1013,27 +1018,27 @@ __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colfwd_inv(NltA
 template <int N, int V>
 struct SplitVar {
   static constexpr bool OK = Var<N, V>::OK && !Var<N, V>::GROUPED && Var<N, V>::COLS == 1;
-  static constexpr int THREADS = N / Var<N, V>::R;
+  static constexpr int THREADS = N / Var<N, V>::CR;
   static constexpr int MINB = V == 0 ? MinBlocks<N>::COL : min_blocks(GT_SPLIT_MINB, THREADS, GT_SPLIT_REGS);
   static constexpr size_t SMEM = (size_t)padded(N) * sizeof(double2);
 };
 template <int N, int V, bool RT = false>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_nlt_colinv_fs(NltArgs a) {
   pdl_enter();
-  if constexpr (SplitVar<N, V>::OK) colinv_field_tile<N, Var<N, V>::R, RT>(a, blockIdx.x);
+  if constexpr (SplitVar<N, V>::OK) colinv_field_tile<N, Var<N, V>::CR, RT>(a, blockIdx.x);
 }
 // KICK: the final stage with the fused forcing kick
 template <int N, int V, bool KICK, bool RT = false>
 __global__ void __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB) k_nlt_colfwd_fs(NltArgs a) {
   pdl_enter();
-  if constexpr (SplitVar<N, V>::OK) colfwd_field_tile<N, Var<N, V>::R, KICK, RT>(a, blockIdx.x);
+  if constexpr (SplitVar<N, V>::OK) colfwd_field_tile<N, Var<N, V>::CR, KICK, RT>(a, blockIdx.x);
 }
 // the same pass with the column's two CTAs as one cluster (grid 2 NH)
 template <int N, int V, bool KICK, bool RT = false>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(SplitVar<N, V>::THREADS, SplitVar<N, V>::MINB)
     k_nlt_colfwd_cl(NltArgs a) {
   pdl_enter();
-  if constexpr (SplitVar<N, V>::OK) colfwd_cluster_tile<N, Var<N, V>::R, KICK, RT>(a, blockIdx.x);
+  if constexpr (SplitVar<N, V>::OK) colfwd_cluster_tile<N, Var<N, V>::CR, KICK, RT>(a, blockIdx.x);
 }
 
 // ---- ensemble kernels: one launch per pass for every member ------------------------------

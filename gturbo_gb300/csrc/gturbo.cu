@@ -228,8 +228,9 @@ bool col_variant_ok(const gt_handle* h, int v) {
   return gt_variant_supported(h->NY, v) && (!h->rt || v == 1 || v == 2);
 }
 
-// The row variant that goes with column variant v in gt_set_variant: the same launch variant.
-int natural_row_variant(int v) { return v; }
+// The row variant that goes with column variant v in gt_set_variant: the same launch variant,
+// or, for column variant 5 (which has no row form), row variant 2.
+int natural_row_variant(int v) { return v == 5 ? 2 : v; }
 
 // The twiddle buffer of the FFT passes (gt_fft.cuh): exp(-2 pi i k / n) for k in [0, n), each
 // value from an argument reduced to [0, pi/4]; then the Linzer-Feig forms tw[n + k] = (c, t) with
@@ -395,7 +396,8 @@ int run(gt_handle* h, const GtOp& op) {
 // The field-split column passes run when the handle has their scratch (N <= 2048), the user
 // has not turned them off, and the column variant has one column per CTA without thread groups.
 bool split_active(const gt_handle* h) {
-  const bool one_col = (h->variant == 0 && h->NY >= 1024) || h->variant == 1 || h->variant == 2;
+  const bool one_col =
+      (h->variant == 0 && h->NY >= 1024) || h->variant == 1 || h->variant == 2 || h->variant == 5;
   return h->col_split && h->d_qscr && one_col;
 }
 
@@ -472,12 +474,12 @@ int gt_create(const gt_params* p, gt_handle** out) {
   h->dispatch = dispatch_for(NY);
   h->dispatch_row = dispatch_for(N);
   // The launch variants that timed fastest on GB300 for this grid size (RK2 and RK4 alike).
-  // Columns: grouped with 4 values per thread up to 256^2, 4 values per thread at 512^2 and
-  // 1024^2, 8 at 2048^2, 16 from 4096^2 up. Rows: grouped with 4 values per thread up to
-  // 128^2, 4 values per thread at 256^2 and 512^2, 8 at 1024^2 and 2048^2, 16 from 4096^2 up.
-  // gt_autotune re-times.
+  // Columns: grouped with 4 values per thread at 16^2, 2 values per thread from 32^2 to 256^2,
+  // 4 at 512^2 and 1024^2, 8 at 2048^2, 16 from 4096^2 up. Rows: grouped with 4 values per
+  // thread up to 128^2, 4 values per thread at 256^2 and 512^2, 8 at 1024^2 and 2048^2, 16
+  // from 4096^2 up. gt_autotune re-times.
   // (Columns follow the column length NY, rows the row length NX.)
-  h->variant = NY <= 256 ? 3 : NY <= 1024 ? 2 : NY == 2048 ? 1 : 0;
+  h->variant = NY < 32 ? 3 : NY <= 256 ? 5 : NY <= 1024 ? 2 : NY == 2048 ? 1 : 0;
   if (h->rt) h->variant = NY <= 1024 ? 2 : 1;
   h->row_variant = N <= 128 ? 3 : N <= 512 ? 2 : N <= 2048 ? 1 : 0;
   // inieuler.f90:22-36, 237-244
@@ -1320,6 +1322,7 @@ int gt_variant_supported(int32_t n, int32_t variant) {
     case 2:
     case 3:
     case 4: return n <= 1024;
+    case 5: return n >= 32 && n <= 512;
     default: return 0;
   }
 }
@@ -1327,7 +1330,8 @@ int gt_variant_supported(int32_t n, int32_t variant) {
 int gt_row_variant_supported(int32_t n, int32_t row_variant) {
   return row_variant >= 0 && row_variant < GT_NROW_VARIANTS && gt_variant_supported(n, row_variant);
 }
-static_assert(GT_NROW_VARIANTS == GT_NVARIANTS, "row and column variants share their numbering");
+static_assert(GT_NROW_VARIANTS + 1 == GT_NVARIANTS,
+              "row and column variants share their numbering; column variant 5 has no row form");
 
 int gt_set_variants(gt_handle* h, int32_t col_variant, int32_t row_variant) {
   if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_variants: null handle");

@@ -142,7 +142,7 @@ class Solver:
         return {k: (ms[i], cnt[i]) for i, k in enumerate(self.PROF_KINDS)}
 
     # -- launch variants (gt_set_variant / gt_autotune) -----------------------------------
-    NVARIANTS = 5
+    NVARIANTS = 6
 
     @property
     def variant(self) -> int:

@@ -321,10 +321,12 @@ int gt_profile_read(gt_handle* h, double* ms, int64_t* launches);
  * block (large grids); 1 = 8 values per thread, one column/row per block (n <= 4096);
  * 2 = 4 values per thread, one column/row per block (n <= 1024, for small latency-bound
  * grids); 3 and 4 = 4 and 8 values per thread with the independent transforms of a column
- * (u, v, q; A, B) run side by side by three thread groups of the block (n <= 1024). The
- * variants differ only in the radix decomposition of the transforms, so their results agree
- * to rounding (relative differences of order 1e-15 per step). */
-#define GT_NVARIANTS 5
+ * (u, v, q; A, B) run side by side by three thread groups of the block (n <= 1024); 5 = 2
+ * values per thread in the column passes, one column per block (32 <= n <= 512; it has no row
+ * form, and gt_set_variant pairs it with row variant 2). The variants differ only in the radix
+ * decomposition of the transforms, so their results agree to rounding (relative differences of
+ * order 1e-15 per step). */
+#define GT_NVARIANTS 6
 /* The row pass takes its own launch variant, numbered like the column variants: 0, 1, 2 =
  * 16, 8, 4 values per thread; 3, 4 = 4 and 8 values per thread with the u + i v and q
  * transforms of a row run side by side by two thread groups (n <= 1024). */
@@ -340,7 +342,7 @@ int gt_get_variant(const gt_handle* h, int32_t* variant);
 int gt_set_variants(gt_handle* h, int32_t col_variant, int32_t row_variant);
 int gt_get_variants(const gt_handle* h, int32_t* col_variant, int32_t* row_variant);
 /* Field-split column passes (N <= 2048, column variants with one column per CTA and no
- * thread groups: 0 from N = 1024, 1, 2): each CTA transforms one field of one column, so a
+ * thread groups: 0 from N = 1024, 1, 2, 5): each CTA transforms one field of one column, so a
  * column pass has 3 (pass A) or 2 (pass C) work units per column and the SMs finish together;
  * q then lives in the handle's scratch field. on = 1: pass C's epilogue is run by the column's
  * CTA that finishes second, which reads the other field back through L2 (a per-column counter);

@@ -12,7 +12,7 @@ module gturbo_c
 
   integer(c_int), parameter :: GT_OK = 0, GT_ERR_ARG = 1, GT_ERR_CUDA = 2, GT_ERR_NFORC = 3, &
                                GT_ERR_STATE = 4, GT_ERR_NOMEM = 5, GT_ERR_NONFINITE = 6
-  integer(c_int), parameter :: GT_NVARIANTS = 5
+  integer(c_int), parameter :: GT_NVARIANTS = 6
 
   ! struct gt_params: params.dat plus the derived switches (src/inieuler.f90:13-36)
   type, bind(C) :: gt_params
