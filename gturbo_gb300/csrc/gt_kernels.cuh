@@ -945,26 +945,29 @@ k_nlt_colfwd_inv(NltArgs cur, NltArgs next) {
 // V = 3: R = 4,  grouped tiles: a column's transforms side by side in 3 thread groups, a row's
 //        u + i v and q transforms side by side in 2;
 // V = 4: R = 8,  grouped tiles;
-// V = 5: CR = 2 in the column passes (one column per CTA with twice the threads of V = 2, for
-//        grids whose column passes have fewer warps than the SMs have sub-partitions); it has
-//        no row form (the row pass's half-length q transform needs R >= 4).
+// V = 5: 2 values per thread: the column passes one column per CTA with twice the threads of
+//        V = 2 (grids whose column passes have fewer warps than the SMs have sub-partitions),
+//        the row pass grouped like V = 3 (its q transform at full length, so no half-length
+//        transform needs R >= 4).
 // The row pass and the column passes take their variants separately (GtOp::row_variant).
 template <int N, int V>
 struct Var {
-  static constexpr bool GROUPED = V == 3 || V == 4;
+  static constexpr bool GROUPED = V == 3 || V == 4;           // grouped column tiles
+  static constexpr bool ROW_GROUPED = V == 3 || V == 4 || V == 5;
   static constexpr int R = V == 0 ? 16 : (V == 1 || V == 4) ? 8 : 4;
   static constexpr int CR = V == 5 ? 2 : R;  // values per thread of the column passes
+  static constexpr int RR = V == 5 ? 2 : R;  // values per thread of the row pass
   static constexpr int T = N / R;
   static constexpr int NH = N / 2 + 1;
   static constexpr int COLS = V == 0 ? Shape<N>::COLS : 1;
   static constexpr int ROWS = V == 0 ? Shape<N>::ROWS : 1;
   static constexpr int COL_THREADS = GROUPED ? kColGroups * T : COLS * (N / CR);
-  static constexpr int ROW_THREADS = (GROUPED ? 2 : ROWS) * T;
+  static constexpr int ROW_THREADS = ROW_GROUPED ? 2 * (N / RR) : ROWS * T;
   static constexpr int COL_CTAS = (NH + COLS - 1) / COLS;
   static constexpr int ROW_CTAS = N / ROWS;
   static constexpr size_t COL_SMEM = (size_t)padded(N) * (GROUPED ? kColGroups : COLS) * sizeof(double2);
   // grouped rows: two length-N exchange buffers (u + i v and q)
-  static constexpr size_t ROW_SMEM = GROUPED ? (size_t)2 * padded(N) * sizeof(double2)
+  static constexpr size_t ROW_SMEM = ROW_GROUPED ? (size_t)2 * padded(N) * sizeof(double2)
                                              : (size_t)(padded(N) + padded(N / 2)) * ROWS * sizeof(double2);
   static constexpr bool OK = V == 0 || (V == 1 && N <= 4096) || (V >= 2 && V <= 4 && N <= 1024) ||
                               (V == 5 && N >= 32 && N <= 512);
@@ -988,7 +991,7 @@ __global__ void __launch_bounds__(Var<N, V>::COL_THREADS) k_nltv_colinv(NltArgs 
 template <int N, int V>
 __global__ void GT_VROW_BOUNDS(N, V) k_nltv_row(NltArgs a) {
   pdl_enter();
-  if constexpr (Var<N, V>::OK && Var<N, V>::GROUPED) row_grp_tile<N, Var<N, V>::R>(a, blockIdx.x);
+  if constexpr (Var<N, V>::OK && Var<N, V>::ROW_GROUPED) row_grp_tile<N, Var<N, V>::RR>(a, blockIdx.x);
   else if constexpr (Var<N, V>::OK) row_tile<N, Var<N, V>::ROWS, Var<N, V>::R>(a, blockIdx.x);
 }
 template <int N, int V, bool RT = false>

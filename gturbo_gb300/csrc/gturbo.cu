@@ -228,9 +228,8 @@ bool col_variant_ok(const gt_handle* h, int v) {
   return gt_variant_supported(h->NY, v) && (!h->rt || v == 1 || v == 2);
 }
 
-// The row variant that goes with column variant v in gt_set_variant: the same launch variant,
-// or, for column variant 5 (which has no row form), row variant 2.
-int natural_row_variant(int v) { return v == 5 ? 2 : v; }
+// The row variant that goes with column variant v in gt_set_variant: the same launch variant.
+int natural_row_variant(int v) { return v; }
 
 // The twiddle buffer of the FFT passes (gt_fft.cuh): exp(-2 pi i k / n) for k in [0, n), each
 // value from an argument reduced to [0, pi/4]; then the Linzer-Feig forms tw[n + k] = (c, t) with
@@ -476,12 +475,12 @@ int gt_create(const gt_params* p, gt_handle** out) {
   // The launch variants that timed fastest on GB300 for this grid size (RK2 and RK4 alike).
   // Columns: grouped with 4 values per thread at 16^2, 2 values per thread from 32^2 to 256^2,
   // 4 at 512^2 and 1024^2, 8 at 2048^2, 16 from 4096^2 up. Rows: grouped with 4 values per
-  // thread up to 128^2, 4 values per thread at 256^2 and 512^2, 8 at 1024^2 and 2048^2, 16
-  // from 4096^2 up. gt_autotune re-times.
+  // thread at 16^2, grouped with 2 from 32^2 to 128^2, 4 values per thread at 256^2 and 512^2,
+  // 8 at 1024^2 and 2048^2, 16 from 4096^2 up. gt_autotune re-times.
   // (Columns follow the column length NY, rows the row length NX.)
   h->variant = NY < 32 ? 3 : NY <= 256 ? 5 : NY <= 1024 ? 2 : NY == 2048 ? 1 : 0;
   if (h->rt) h->variant = NY <= 1024 ? 2 : 1;
-  h->row_variant = N <= 128 ? 3 : N <= 512 ? 2 : N <= 2048 ? 1 : 0;
+  h->row_variant = N < 32 ? 3 : N <= 128 ? 5 : N <= 512 ? 2 : N <= 2048 ? 1 : 0;
   // inieuler.f90:22-36, 237-244
   int split = 0;
   if (p->alpnu < 1.0005 && p->alpnu > 0.9995 && p->alpmu < 0.0005 && p->alpmu > -0.0005) split = 1;
@@ -1330,8 +1329,7 @@ int gt_variant_supported(int32_t n, int32_t variant) {
 int gt_row_variant_supported(int32_t n, int32_t row_variant) {
   return row_variant >= 0 && row_variant < GT_NROW_VARIANTS && gt_variant_supported(n, row_variant);
 }
-static_assert(GT_NROW_VARIANTS + 1 == GT_NVARIANTS,
-              "row and column variants share their numbering; column variant 5 has no row form");
+static_assert(GT_NROW_VARIANTS == GT_NVARIANTS, "row and column variants share their numbering");
 
 int gt_set_variants(gt_handle* h, int32_t col_variant, int32_t row_variant) {
   if (!h) return fail(nullptr, GT_ERR_ARG, "gt_set_variants: null handle");
@@ -1417,15 +1415,27 @@ int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best)
       ms[v] = time_pair(v, row_for(v));
       if (!rc && (ms[best_c] < 0.0 || ms[v] < ms[best_c])) best_c = v;
     }
-    // stage 2: the row variants under the best column variant
+    // stage 2: every row variant under each of the two fastest column variants (a column
+    // variant's own row tiles need not be its best partner); ms[c] becomes column variant c's
+    // best time over the rows tried with it
+    int cand[2] = {best_c, -1};
+    for (int v = 0; v < GT_NVARIANTS; ++v)
+      if (v != best_c && ms[v] >= 0.0 && (cand[1] < 0 || ms[v] < ms[cand[1]])) cand[1] = v;
     int best_r = row_for(best_c);
     double best_ms = ms[best_c];
-    for (int r = 0; r < GT_NROW_VARIANTS && !rc; ++r) {
-      if (r == best_r || !gt_row_variant_supported(h->N, r)) continue;
-      const double t = time_pair(best_c, r);
-      if (!rc && t < best_ms) {
-        best_ms = t;
-        best_r = r;
+    for (int ci = 0; ci < 2 && !rc; ++ci) {
+      const int c = cand[ci];
+      if (c < 0) continue;
+      for (int r = 0; r < GT_NROW_VARIANTS && !rc; ++r) {
+        if (r == row_for(c) || !gt_row_variant_supported(h->N, r)) continue;
+        const double t = time_pair(c, r);
+        if (rc || t < 0.0) break;
+        if (t < ms[c]) ms[c] = t;
+        if (t < best_ms) {
+          best_ms = t;
+          best_c = c;
+          best_r = r;
+        }
       }
     }
     // stage 3: the best pair with one CTA per column, where the field-split passes ran

@@ -322,15 +322,14 @@ int gt_profile_read(gt_handle* h, double* ms, int64_t* launches);
  * 2 = 4 values per thread, one column/row per block (n <= 1024, for small latency-bound
  * grids); 3 and 4 = 4 and 8 values per thread with the independent transforms of a column
  * (u, v, q; A, B) run side by side by three thread groups of the block (n <= 1024); 5 = 2
- * values per thread in the column passes, one column per block (32 <= n <= 512; it has no row
- * form, and gt_set_variant pairs it with row variant 2). The variants differ only in the radix
- * decomposition of the transforms, so their results agree to rounding (relative differences of
- * order 1e-15 per step). */
+ * values per thread, one column per block (32 <= n <= 512). The variants differ only in the
+ * radix decomposition of the transforms, so their results agree to rounding (relative
+ * differences of order 1e-15 per step). */
 #define GT_NVARIANTS 6
 /* The row pass takes its own launch variant, numbered like the column variants: 0, 1, 2 =
- * 16, 8, 4 values per thread; 3, 4 = 4 and 8 values per thread with the u + i v and q
- * transforms of a row run side by side by two thread groups (n <= 1024). */
-#define GT_NROW_VARIANTS 5
+ * 16, 8, 4 values per thread; 3, 4, 5 = 4, 8 and 2 values per thread with the u + i v and q
+ * transforms of a row run side by side by two thread groups (3, 4: n <= 1024; 5: 32 <= n <= 512). */
+#define GT_NROW_VARIANTS 6
 /* 1 if launch variant `variant` exists for grid size n, else 0 (host only, no GPU needed). */
 int gt_variant_supported(int32_t n, int32_t variant);
 int gt_row_variant_supported(int32_t n, int32_t row_variant);
@@ -376,11 +375,11 @@ int gt_set_graphs(gt_handle* h, int32_t on);
 int gt_get_graphs(const gt_handle* h, int32_t* on);
 /* Time `steps` steps of the handle's integrator (RK2 or RK4) on zero fields of its own
  * (allocated and freed here, 5 fields; nothing when only one variant exists): first every
- * supported column variant with its own row tiles, then the other row variants under the
- * fastest column variant, then (where the field-split column passes ran) that pair with one
- * CTA per column, turning the split off if that is faster. Keeps the fastest pair; returns ms
- * per step of each column variant
- * in ms_per_step[GT_NVARIANTS] (-1 for unsupported variants) and the column choice in *best
+ * supported column variant with its own row tiles, then the other row variants under each of
+ * the two fastest column variants, then (where the field-split column passes ran) the best pair
+ * with one CTA per column, turning the split off if that is faster. Keeps the fastest pair;
+ * returns, per column variant, its best ms per step over the row variants tried with it in
+ * ms_per_step[GT_NVARIANTS] (-1 for unsupported variants) and the column choice in *best
  * (either pointer may be null; gt_get_variants gives the pair). Synchronous. */
 int gt_autotune(gt_handle* h, int32_t steps, double* ms_per_step, int32_t* best);
 
