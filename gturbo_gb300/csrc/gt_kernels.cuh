@@ -969,7 +969,7 @@ struct Var {
   // grouped rows: two length-N exchange buffers (u + i v and q)
   static constexpr size_t ROW_SMEM = ROW_GROUPED ? (size_t)2 * padded(N) * sizeof(double2)
                                              : (size_t)(padded(N) + padded(N / 2)) * ROWS * sizeof(double2);
-  static constexpr bool OK = V == 0 || (V == 1 && N <= 4096) || (V >= 2 && V <= 4 && N <= 1024) ||
+  static constexpr bool OK = V == 0 || (V == 1 && N <= 8192) || (V >= 2 && V <= 4 && N <= 1024) ||
                               (V == 5 && N >= 32 && N <= 512);
 };
 

@@ -474,11 +474,11 @@ int gt_create(const gt_params* p, gt_handle** out) {
   h->dispatch_row = dispatch_for(N);
   // The launch variants that timed fastest on GB300 for this grid size (RK2 and RK4 alike).
   // Columns: grouped with 4 values per thread at 16^2, 2 values per thread from 32^2 to 256^2,
-  // 4 at 512^2 and 1024^2, 8 at 2048^2, 16 from 4096^2 up. Rows: grouped with 4 values per
+  // 4 at 512^2 and 1024^2, 8 at 2048^2, 16 at 4096^2, 8 at 8192^2. Rows: grouped with 4 values per
   // thread at 16^2, grouped with 2 from 32^2 to 128^2, 4 values per thread at 256^2 and 512^2,
   // 8 at 1024^2 and 2048^2, 16 from 4096^2 up. gt_autotune re-times.
   // (Columns follow the column length NY, rows the row length NX.)
-  h->variant = NY < 32 ? 3 : NY <= 256 ? 5 : NY <= 1024 ? 2 : NY == 2048 ? 1 : 0;
+  h->variant = NY < 32 ? 3 : NY <= 256 ? 5 : NY <= 1024 ? 2 : (NY == 2048 || NY == 8192) ? 1 : 0;
   if (h->rt) h->variant = NY <= 1024 ? 2 : 1;
   h->row_variant = N < 32 ? 3 : N <= 128 ? 5 : N <= 512 ? 2 : N <= 2048 ? 1 : 0;
   // inieuler.f90:22-36, 237-244
@@ -1317,7 +1317,7 @@ int gt_variant_supported(int32_t n, int32_t variant) {
   if (!pow2_in_range(n)) return 0;
   switch (variant) {
     case 0: return 1;
-    case 1: return n <= 4096;
+    case 1: return n <= 8192;
     case 2:
     case 3:
     case 4: return n <= 1024;

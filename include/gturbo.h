@@ -318,7 +318,7 @@ int gt_profile_read(gt_handle* h, double* ms, int64_t* launches);
 /* No counterpart in the reference, whose transforms are cuFFT plans (src/fft_dir.f90,
  * src/fft_inv.f90) that the library tunes internally. The three passes of the nonlinear
  * term come in GT_NVARIANTS launch shapes: 0 = 16 values per thread, several columns/rows per
- * block (large grids); 1 = 8 values per thread, one column/row per block (n <= 4096);
+ * block (large grids); 1 = 8 values per thread, one column/row per block (n <= 8192);
  * 2 = 4 values per thread, one column/row per block (n <= 1024, for small latency-bound
  * grids); 3 and 4 = 4 and 8 values per thread with the independent transforms of a column
  * (u, v, q; A, B) run side by side by three thread groups of the block (n <= 1024); 5 = 2

@@ -130,15 +130,15 @@ def test_null_arguments_are_errors_not_crashes(lib):
 
 
 def test_variant_table(lib):
-    """Launch variants by grid size: 0 always, 1 up to 4096, 2-4 up to 1024, 5 from 32 to 512
+    """Launch variants by grid size: 0 always, 1 up to 8192, 2-4 up to 1024, 5 from 32 to 512
     (host only)."""
     for n in (16, 32, 64, 512, 1024, 2048, 4096, 8192):
         got = [lib.gt_variant_supported(n, v) for v in range(6)]
-        assert got == [1, int(n <= 4096)] + [int(n <= 1024)] * 3 + [int(32 <= n <= 512)], n
+        assert got == [1, int(n <= 8192)] + [int(n <= 1024)] * 3 + [int(32 <= n <= 512)], n
     assert lib.gt_variant_supported(100, 0) == 0 and lib.gt_variant_supported(64, 6) == 0
     for n in (16, 64, 512, 2048, 8192):
         assert [lib.gt_row_variant_supported(n, r) for r in range(7)] == \
-            [1, int(n <= 4096)] + [int(n <= 1024)] * 3 + [int(32 <= n <= 512), 0], n
+            [1, int(n <= 8192)] + [int(n <= 1024)] * 3 + [int(32 <= n <= 512), 0], n
     assert lib.gt_set_variant(None, 0) == 1 and lib.gt_autotune(None, 1, None, None) == 1
 
 
